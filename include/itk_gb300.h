@@ -1,0 +1,188 @@
+/*
+ * itk_gb300.h -- C ABI of the GB300 registration-metric library.
+ *
+ * One GPU, one process.  Plain pointers and sizes only: no C++ or torch types
+ * cross this boundary.  Every function returns an int status (GB_OK = 0).
+ * Caller buffers are borrowed for the duration of a call; device memory
+ * belongs to the handle that allocated it.  Handles are independent and may
+ * be used from different host threads; one call at a time per handle.
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the ITK source tree, Modules/).  The ITK-side shim that binds these
+ * entry points behind itk::ObjectFactoryBase overrides is in INTEGRATION.md.
+ */
+#ifndef ITK_GB300_H
+#define ITK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  GB_OK = 0,
+  GB_ERR_BAD_ARG = 1,
+  /* no sample mapped inside both buffers.  MeanSquares still returns
+   * value = DBL_MAX and a zero derivative (ObjectToObjectMetric::
+   * VerifyNumberOfValidPoints, Numerics/Optimizersv4/include/itkObjectToObjectMetric.hxx:512-527);
+   * Mattes raises (itkMattesMutualInformationImageToImageMetricv4.hxx:360-366). */
+  GB_ERR_NO_VALID_POINTS = 2,
+  GB_ERR_JOINT_PDF_SUM_ZERO = 3, /* itkMattesMutualInformationImageToImageMetricv4.hxx:367-370 */
+  GB_ERR_FIXED_CONSTANT = 4,     /* itkMattesMutualInformationImageToImageMetricv4.hxx:284-292 */
+  GB_ERR_MOVING_CONSTANT = 5,    /* itkMattesMutualInformationImageToImageMetricv4.hxx:299-307 */
+  GB_ERR_FIXED_EMPTY = 6,        /* itkMattesMutualInformationImageToImageMetricv4.hxx:278-283 */
+  GB_ERR_MOVING_EMPTY = 7,       /* itkMattesMutualInformationImageToImageMetricv4.hxx:293-298 */
+  GB_ERR_OUT_OF_MEMORY = 8,
+  GB_ERR_CUDA = 9,
+  GB_ERR_TIMEOUT = 10,
+  GB_ERR_NOT_INITIALIZED = 11,
+  GB_ERR_UNSUPPORTED = 12,
+  GB_ERR_ADMISSION = 13
+};
+
+/* metric kinds */
+enum { GB_METRIC_MEAN_SQUARES = 0, GB_METRIC_MATTES = 1 };
+/* image slots */
+enum { GB_IMAGE_FIXED = 0, GB_IMAGE_MOVING = 1 };
+/* moving transform kinds (flat encodings below) */
+enum { GB_TRANSFORM_AFFINE = 0, GB_TRANSFORM_BSPLINE = 1, GB_TRANSFORM_COMPOSITE = 2 };
+/* moving-gradient source */
+enum {
+  GB_GRADIENT_IMAGE = 0,              /* caller-supplied gradient image (filter output) */
+  GB_GRADIENT_CENTRAL_DIFFERENCE = 1, /* per-point CentralDifferenceImageFunction */
+  GB_GRADIENT_RECURSIVE_GAUSSIAN = 2  /* gradient image computed on the device */
+};
+
+typedef struct gb_ctx gb_ctx;
+typedef struct gb_metric gb_metric;
+
+/* Text of the last error raised on the calling host thread (never NULL).
+ * Mattes/MeanSquares errors reuse the reference's exception text. */
+const char *gb_last_error(void);
+/* Library version string. */
+const char *gb_version(void);
+
+/* ---- device context ---------------------------------------------------- */
+/* Binds a CUDA device; the context owns no stream of its own. */
+int gb_ctx_create(int device, gb_ctx **out);
+int gb_ctx_destroy(gb_ctx *ctx);
+/* Number of SMs and total/free device memory in bytes. */
+int gb_ctx_info(gb_ctx *ctx, int *sm_count, uint64_t *total_bytes, uint64_t *free_bytes);
+
+/* ---- metric handle ----------------------------------------------------- */
+/* Replaces MeanSquaresImageToImageMetricv4<Image<float,3>,...>::New() and
+ * MattesMutualInformationImageToImageMetricv4<Image<float,3>,...>::New()
+ * (Registration/Metricsv4/include/itkMattesMutualInformationImageToImageMetricv4.hxx:31-60).
+ * Each handle owns a CUDA stream and its device buffers. */
+int gb_metric_create(gb_ctx *ctx, int kind, gb_metric **out);
+int gb_metric_destroy(gb_metric *m);
+
+/* SetNumberOfHistogramBins, clamped to >= 5
+ * (itkMattesMutualInformationImageToImageMetricv4.h:146). */
+int gb_metric_set_number_of_histogram_bins(gb_metric *m, uint64_t bins);
+
+/* SetFixedImage / SetMovingImage (itkImageToImageMetricv4.h SetFixedImage /
+ * SetMovingImage): float voxels, x fastest, size[3] = (nx, ny, nz), start
+ * index 0, direction row-major 3x3.  The voxels are copied into HBM. */
+int gb_metric_set_image(gb_metric *m, int which, const float *voxels, const int64_t size[3],
+                        const double spacing[3], const double origin[3], const double direction[9]);
+/* Same, from a device pointer (no host round trip; copied device-to-device). */
+int gb_metric_set_image_device(gb_metric *m, int which, const float *device_voxels, const int64_t size[3],
+                               const double spacing[3], const double origin[3], const double direction[9]);
+
+/* Moving-image gradient.  GB_GRADIENT_IMAGE expects a call to
+ * gb_metric_set_moving_gradient_image (the CovariantVector<double,3> image the
+ * metric's gradient filter produces, itkImageToImageMetricv4.hxx:449-455);
+ * GB_GRADIENT_CENTRAL_DIFFERENCE evaluates CentralDifferenceImageFunction at
+ * each mapped point (SetUseMovingImageGradientFilter(false),
+ * Core/ImageFunction/include/itkCentralDifferenceImageFunction.hxx:256-316);
+ * GB_GRADIENT_RECURSIVE_GAUSSIAN runs GradientRecursiveGaussianImageFilter on
+ * the device (sigma = max spacing, normalized across scale, image direction
+ * applied; itkImageToImageMetricv4.hxx:488-503). */
+int gb_metric_set_gradient_source(gb_metric *m, int source);
+/* gradient: 3 doubles per voxel (x, y, z), same grid as the moving image */
+int gb_metric_set_moving_gradient_image(gb_metric *m, const double *gradient_xyz);
+
+/* Virtual domain (SetVirtualDomain, itkImageToImageMetricv4.h); when never
+ * set, the fixed image geometry is used (itkImageToImageMetricv4.hxx:98-112). */
+int gb_metric_set_virtual_domain(gb_metric *m, const int64_t size[3], const double spacing[3],
+                                 const double origin[3], const double direction[9]);
+
+/* Sampled point sets: float xyz, n points.  virtual_space = 1 replaces
+ * SetVirtualSampledPointSet + UseVirtualSampledPointSetOn (what
+ * ImageRegistrationMethodv4::SetMetricSamplePoints installs,
+ * Registration/RegistrationMethodsv4/include/itkImageRegistrationMethodv4.hxx:1010-1021);
+ * virtual_space = 0 replaces SetFixedSampledPointSet (mapped to the virtual
+ * domain by MapFixedSampledPointSetToVirtual, itkImageToImageMetricv4.hxx:568-612). */
+int gb_metric_set_sampled_points(gb_metric *m, const float *xyz, int64_t n, int virtual_space);
+/* SetUseSampledPointSet(on) */
+int gb_metric_use_sampled_point_set(gb_metric *m, int on);
+
+/* Moving transform (SetMovingTransform).  Flat encodings:
+ *   AFFINE    params = 12 (row-major matrix, translation), fixed = centre (3)
+ *             -- AffineTransform<double,3>, Core/Transform/include/itkMatrixOffsetTransformBase.hxx:464-561
+ *   BSPLINE   params = 3*nper coefficients, fixed = 18 (grid size, origin,
+ *             spacing, direction) -- BSplineTransform<double,3,3>,
+ *             Core/Transform/include/itkBSplineTransform.hxx:243-283
+ *   COMPOSITE params = 3*nper B-spline coefficients (optimized), fixed = 18
+ *             B-spline fixed parameters + 12 initial-affine parameters + 3
+ *             initial-affine centre -- CompositeTransform [affine, bspline]
+ *             with only the B-spline optimized, Core/Transform/include/itkCompositeTransform.hxx:60-70,466-580 */
+int gb_metric_set_moving_transform(gb_metric *m, int kind, const double *params, int64_t nparams,
+                                   const double *fixed, int64_t nfixed);
+/* SetParameters of the optimized transform (per optimizer iteration). */
+int gb_metric_set_parameters(gb_metric *m, const double *params, int64_t nparams);
+/* UpdateTransformParameters(update, factor): params += factor*update
+ * (Core/Transform/include/itkTransform.hxx:71-120). */
+int gb_metric_update_transform_parameters(gb_metric *m, const double *update, int64_t nparams, double factor);
+int gb_metric_get_parameters(gb_metric *m, double *params, int64_t nparams);
+int gb_metric_get_number_of_parameters(gb_metric *m, int64_t *nparams);
+
+/* Initialize() (itkImageToImageMetricv4.hxx:72-172; Mattes bins and ranges
+ * itkMattesMutualInformationImageToImageMetricv4.hxx:75-327).  Builds the
+ * device sample list, the fixed values / fixed Parzen bins, the packed moving
+ * image and its gradient. */
+int gb_metric_initialize(gb_metric *m);
+
+/* GetValueAndDerivative(value, derivative) (itkImageToImageMetricv4.hxx:218-231):
+ * derivative has nparams entries and is overwritten. */
+int gb_metric_get_value_and_derivative(gb_metric *m, double *value, double *derivative, int64_t nparams);
+/* GetValue() (itkImageToImageMetricv4.hxx:182-196). */
+int gb_metric_get_value(gb_metric *m, double *value);
+/* GetNumberOfValidPoints() of the last evaluation. */
+int gb_metric_get_number_of_valid_points(gb_metric *m, uint64_t *nvalid);
+/* GetNumberOfDomainPoints(): samples (or virtual voxels) evaluated per call. */
+int gb_metric_get_number_of_domain_points(gb_metric *m, uint64_t *n);
+/* GetJointPDF() of the last Mattes evaluation: bins*bins doubles, row = fixed bin. */
+int gb_metric_get_joint_pdf(gb_metric *m, double *out, int64_t n);
+/* Mattes ranges: fixed min, fixed max, moving min, moving max, fixed bin size,
+ * moving bin size, fixed normalized min, moving normalized min. */
+int gb_metric_get_mattes_state(gb_metric *m, double out8[8]);
+
+/* ---- device-resident form (no host copies) ----------------------------- */
+/* CUDA stream the handle launches on (cudaStream_t as an integer). */
+int gb_metric_get_stream(gb_metric *m, uint64_t *stream);
+/* Enqueue one evaluation on the handle's stream with the parameters already
+ * in device memory (nparams doubles) and write value, derivative and the
+ * valid-point count (as a double) to device memory: out = [value, nvalid,
+ * derivative...].  Asynchronous; use gb_metric_status_device for the status. */
+int gb_metric_evaluate_device(gb_metric *m, const double *device_params, double *device_out, int with_derivative);
+/* Synchronize the handle's stream and return the status of the last enqueued evaluation. */
+int gb_metric_synchronize(gb_metric *m);
+
+/* ---- observability ----------------------------------------------------- */
+/* Per-kernel CUDA-event timing of evaluations (the reference's TimeProbe,
+ * Core/Common/include/itkTimeProbe.h:44, at kernel granularity).  When on,
+ * each evaluation records an event before and after every kernel it launches. */
+int gb_metric_set_profiling(gb_metric *m, int on);
+/* Device milliseconds of each kernel of the last evaluation, in launch order
+ * (MeanSquares: 1 kernel; Mattes: pass 1, finalize, pass 2).  Synchronizes. */
+int gb_metric_get_kernel_times(gb_metric *m, double *ms, int max_kernels, int *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ITK_GB300_H */

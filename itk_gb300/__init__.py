@@ -1,0 +1,18 @@
+"""GB300-native ITK registration-metric hot path.
+
+GetValueAndDerivative of MeanSquaresImageToImageMetricv4 and
+MattesMutualInformationImageToImageMetricv4 on Image<float,3> under affine,
+B-spline and [affine, B-spline] composite transforms, computed by hand-written
+sm_103a CUDA kernels behind the C ABI in include/itk_gb300.h.
+"""
+from ._capi import ExceptionObject, lib, library_path
+from .image import GradientImage, Image
+from .metrics import (ImageToImageMetricv4, MattesMutualInformationImageToImageMetricv4,
+                      MeanSquaresImageToImageMetricv4, context)
+from .transforms import AffineTransform, BSplineTransform, CompositeTransform
+
+__all__ = [
+    "AffineTransform", "BSplineTransform", "CompositeTransform", "ExceptionObject", "GradientImage", "Image",
+    "ImageToImageMetricv4", "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
+    "context", "lib", "library_path",
+]

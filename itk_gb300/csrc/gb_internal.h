@@ -1,0 +1,127 @@
+// gb_internal.h -- host-side state shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/itk_gb300.h"
+
+namespace gb {
+
+// Image geometry (start index 0, x fastest), as ImageBase holds it.
+struct Geom {
+  int64_t size[3] = {0, 0, 0};
+  double spacing[3] = {1, 1, 1};
+  double origin[3] = {0, 0, 0};
+  double dir[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  double i2p[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};  // direction * diag(spacing)
+  double p2i[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};  // inverse of i2p
+  bool set = false;
+  int64_t voxels() const { return size[0] * size[1] * size[2]; }
+};
+
+int geom_init(Geom& g, const int64_t size[3], const double spacing[3], const double origin[3], const double dir[9]);
+
+// Owning device buffer (cudaMalloc / cudaFree).
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    reset();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    else p = nullptr;
+    return e;
+  }
+};
+
+cudaError_t sort_pairs_u64(const uint64_t* keys_in, uint64_t* keys_out, const uint32_t* vals_in, uint32_t* vals_out,
+                           int64_t n, int end_bit, cudaStream_t stream);
+
+// Per-thread last-error text (gb_last_error()).
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+
+}  // namespace gb
+
+struct gb_ctx {
+  int device = 0;
+  int sm_count = 0;
+};
+
+struct gb_metric {
+  gb_ctx* ctx = nullptr;
+  int kind = GB_METRIC_MEAN_SQUARES;
+  int64_t bins = 50;
+  cudaStream_t stream = nullptr;
+
+  gb::Geom fixed, moving, virt;
+  bool virt_user = false;
+  gb::DevBuf<float> d_fixed, d_moving;
+  gb::DevBuf<double> d_grad_in;  // caller-supplied gradient image (xyz doubles)
+  int grad_source = GB_GRADIENT_IMAGE;
+  bool grad_set = false;
+
+  std::vector<float> h_points;
+  bool points_virtual = true;
+  bool use_sampled = false;
+
+  int tkind = -1;
+  std::vector<double> tparams, tfixed;
+  int64_t nper = 0;  // B-spline nodes per dimension
+
+  // set by Initialize
+  bool initialized = false;
+  int64_t ndomain = 0;   // candidate points (samples or virtual voxels)
+  int64_t nsamples = 0;  // samples with a valid fixed value, sorted
+  gb::DevBuf<float4> d_mov4;     // packed moving image: (value, gx, gy, gz)
+  gb::DevBuf<float4> d_samples;  // (x, y, z, fixed value | fixed Parzen bin)
+  gb::DevBuf<float4> d_cache;    // per-sample pass-1 result for the derivative pass
+  gb::DevBuf<int4> d_bsp;        // per-sample B-spline support: start index, cell
+  gb::DevBuf<float4> d_bspf;     // per-sample B-spline fractions (fx, fy, fz, valid)
+  gb::DevBuf<int64_t> d_cell_chunks;  // [chunk] -> begin sample of a same-cell chunk
+  int64_t ncell_chunks = 0;
+  double mstate[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+
+  // evaluation buffers
+  gb::DevBuf<double> d_params;
+  gb::DevBuf<double> d_coeff_f;  // spare
+  gb::DevBuf<unsigned char> d_acc;  // accumulators, cleared per evaluation
+  size_t acc_bytes = 0;
+  gb::DevBuf<double> d_out;         // [value, nvalid, derivative...]
+  gb::DevBuf<int> d_status;
+  gb::DevBuf<float> d_pratio;       // bins*bins log(p/pm) table
+  gb::DevBuf<double> d_pdf;         // normalized joint PDF of the last evaluation
+  double* h_params = nullptr;       // pinned staging
+  double* h_out = nullptr;          // pinned staging, 2 + P doubles
+  int* h_status = nullptr;
+  uint64_t last_nvalid = 0;
+  int last_status = GB_OK;
+
+  // per-kernel event timing (gb_metric_set_profiling)
+  bool profiling = false;
+  static constexpr int kMaxEvents = 8;
+  cudaEvent_t events[kMaxEvents] = {};
+  int nevents = 0;
+  void mark() {
+    if (!profiling || nevents >= kMaxEvents) return;
+    if (!events[nevents]) cudaEventCreate(&events[nevents]);
+    cudaEventRecord(events[nevents], stream);
+    ++nevents;
+  }
+};

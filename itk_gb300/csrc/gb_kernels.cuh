@@ -1,0 +1,474 @@
+// gb_kernels.cuh -- kernel argument blocks and the kernels of one metric
+// evaluation (MeanSquares single pass; Mattes pass 1 / finalize / pass 2).
+//
+// Reference semantics restated here (paths relative to ITK's Modules/):
+//   per-point skeleton   Registration/Metricsv4/include/itkImageToImageMetricv4GetValueAndDerivativeThreaderBase.hxx:176-273
+//   MeanSquares          Registration/Metricsv4/include/itkMeanSquaresImageToImageMetricv4GetValueAndDerivativeThreader.hxx:31-84
+//   Mattes point         Registration/Metricsv4/include/itkMattesMutualInformationImageToImageMetricv4GetValueAndDerivativeThreader.hxx:220-387
+//   Mattes results       Registration/Metricsv4/include/itkMattesMutualInformationImageToImageMetricv4.hxx:358-542
+//   affine Jacobian      Core/Transform/include/itkMatrixOffsetTransformBase.hxx:566-594
+//
+// Mattes derivative by linearity: instead of the reference's
+// JointPDFDerivatives[f][m][mu] array (P x bins^2 scattered adds per sample),
+// pass 2 re-reads each sample's cached Parzen term and gradient and forms
+//   w = sum_k log(p/pm)[f][m_k] * beta3'(m_k - term),
+//   derivative[mu] = -1/(binsize * N) * sum_samples w * (J^T grad)[mu],
+// which is ComputeResults' contraction (Mattes...v4.hxx:446-461) reordered.
+#pragma once
+
+#include <cfloat>
+
+#include "gb_device.cuh"
+
+namespace gb {
+
+enum { kGradImage = 0, kGradCentralDifference = 1 };
+enum { kXfAffine = 0, kXfBSpline = 1, kXfComposite = 2 };
+
+constexpr int kBlock = 256;
+constexpr float kQScale = 67108864.f;  // 2^26 fixed-point scale for warp-aggregated histogram weights
+constexpr float kQInv = 1.f / 67108864.f;
+
+struct EvalArgs {
+  const float4* __restrict__ samples;
+  int64_t n;
+  const float4* __restrict__ mov4;  // (value, gx, gy, gz)
+  const float* __restrict__ mov1;   // scalar moving image (central difference path)
+  int nx, ny, nz;
+  double m_p2i[9];
+  double m_origin[3];
+  float cd_off[9];        // [3*d + k]: index-space offset along k of +0.5 spacing on physical axis d
+  float cd_inv_delta[3];  // 1 / (spacing[d])
+  // transform
+  const double* params;
+  int nparams;
+  double center[3];  // affine centre
+  // B-spline / composite
+  const int4* __restrict__ bsp;    // per-sample support start (x, y, z), valid flag
+  const float4* __restrict__ bspf; // per-sample fractions inside the support cell
+  int gx, gy, gz;
+  int64_t nper;
+  double init_M[9];       // initial affine of a composite transform
+  double init_offset[3];
+  const int64_t* __restrict__ cell_chunks;
+  int64_t ncell_chunks;
+  // Mattes
+  int bins;
+  float mmin, mmax, m_inv_bs;
+  double m_bs;
+  // accumulators / outputs
+  double* acc;                  // [value, derivative...]
+  unsigned long long* acc_n;
+  unsigned* tickets;
+  double* hist;                 // bins*bins
+  unsigned long long* fmarg;    // bins
+  float4* cache;
+  float* pratio;
+  double* pdf_out;
+  double* out;                  // [value, nvalid, derivative...]
+  int* status;
+  int with_derivative;
+};
+
+// ---------------------------------------------------------------------------
+// transform constants, computed once per block from the device parameters
+
+struct AffConst {
+  double Ad[9];  // virtual point -> moving continuous index: cidx = Ad x + bd
+  double bd[3];
+  float A[9];
+  float c[3];    // affine centre (Jacobian)
+};
+
+// MatrixOffsetTransformBase::ComputeOffset (itkMatrixOffsetTransformBase.hxx:612-631)
+// composed with ImageBase::TransformPhysicalPointToContinuousIndex (itkImageBase.h:515-531).
+__device__ __forceinline__ void affine_consts(const EvalArgs& a, AffConst& K) {
+  const double* p = a.params;
+  double M[9], off[3];
+  for (int i = 0; i < 9; ++i) M[i] = p[i];
+  for (int i = 0; i < 3; ++i) {
+    double o = p[9 + i] + a.center[i];
+    for (int j = 0; j < 3; ++j) o -= M[i * 3 + j] * a.center[j];
+    off[i] = o;
+  }
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += a.m_p2i[r * 3 + k] * M[k * 3 + c];
+      K.Ad[r * 3 + c] = s;
+      K.A[r * 3 + c] = (float)s;
+    }
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) s += a.m_p2i[r * 3 + k] * (off[k] - a.m_origin[k]);
+    K.bd[r] = s;
+  }
+  for (int i = 0; i < 3; ++i) K.c[i] = (float)a.center[i];
+}
+
+__device__ __forceinline__ void affine_map_d(const AffConst& K, float x, float y, float z, double ci[3]) {
+  const double X = x, Y = y, Z = z;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) ci[r] = K.Ad[3 * r] * X + K.Ad[3 * r + 1] * Y + K.Ad[3 * r + 2] * Z + K.bd[r];
+}
+
+// ---------------------------------------------------------------------------
+// moving-image evaluation at a mapped continuous index
+
+// CentralDifferenceImageFunction::EvaluateSpecialized (point form, image direction on),
+// Core/ImageFunction/include/itkCentralDifferenceImageFunction.hxx:256-316
+__device__ __forceinline__ float3 central_difference(const EvalArgs& a, const CIdx& c) {
+  float g[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    CIdx n1, n2;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) split_add(c.b[k], c.f[k] - a.cd_off[3 * d + k], n1.b[k], n1.f[k]);
+    if (!ci_inside(n1, a.nx, a.ny, a.nz)) { g[d] = 0.f; continue; }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) split_add(c.b[k], c.f[k] + a.cd_off[3 * d + k], n2.b[k], n2.f[k]);
+    if (!ci_inside(n2, a.nx, a.ny, a.nz)) { g[d] = 0.f; continue; }
+    const float v1 = gather1(a.mov1, make_stencil(n1, a.nx, a.ny, a.nz), a.nx, a.ny);
+    const float v2 = gather1(a.mov1, make_stencil(n2, a.nx, a.ny, a.nz), a.nx, a.ny);
+    g[d] = (v2 - v1) * a.cd_inv_delta[d];
+  }
+  return make_float3(g[0], g[1], g[2]);
+}
+
+// TransformAndEvaluateMovingPoint + ComputeMovingImageGradientAtPoint
+// (itkImageToImageMetricv4.hxx:331-425): buffer test, trilinear value, gradient.
+template <int GRAD>
+__device__ __forceinline__ bool eval_moving(const EvalArgs& a, const CIdx& c, bool need_grad, float& m, float3& g) {
+  if (!ci_inside(c, a.nx, a.ny, a.nz)) return false;
+  const Stencil st = make_stencil(c, a.nx, a.ny, a.nz);
+  if (GRAD == kGradImage) {
+    const float4 v = gather4(a.mov4, st, a.nx, a.ny);
+    m = v.x;
+    g = make_float3(v.y, v.z, v.w);
+  } else {
+    m = gather1(a.mov1, st, a.nx, a.ny);
+    g = need_grad ? central_difference(a, c) : make_float3(0.f, 0.f, 0.f);
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// block reduction: NV Kahan sums + a count, committed with FP64 atomics
+
+template <int NV>
+__device__ __forceinline__ void block_commit(KahanF (&acc)[NV], unsigned nv, double* gacc, unsigned long long* gn,
+                                             double (*red)[NV + 1]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float v[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(acc[k].value());
+  const unsigned n = warp_sum_u(nv);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) red[warp][k] = (double)v[k];
+    red[warp][NV] = (double)n;
+  }
+  __syncthreads();
+  const int nwarps = blockDim.x >> 5;
+  if (threadIdx.x < NV) {
+    double s = 0.0;
+    for (int w = 0; w < nwarps; ++w) s += red[w][threadIdx.x];
+    if (gacc) atomicAdd(&gacc[threadIdx.x], s);
+  } else if (threadIdx.x == NV && gn) {
+    double s = 0.0;
+    for (int w = 0; w < nwarps; ++w) s += red[w][NV];
+    atomicAdd(gn, (unsigned long long)s);
+  }
+  __threadfence();
+}
+
+// true in exactly one block: the last to finish (threadFenceReduction pattern)
+__device__ __forceinline__ bool last_block(unsigned* ticket) {
+  __shared__ bool is_last;
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+
+// ---------------------------------------------------------------------------
+// MeanSquares, affine: value = sum (f - m)^2 / N, d[p] = sum 2 (f - m) (J^T g)[p] / N
+
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
+  __shared__ AffConst K;
+  __shared__ double red[kBlock / 32][14];
+  if (threadIdx.x == 0) affine_consts(a, K);
+  __syncthreads();
+  KahanF acc[13];
+#pragma unroll
+  for (int k = 0; k < 13; ++k) acc[k].zero();
+  unsigned nv = 0;
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < a.n; base += stride) {
+    const int64_t i = base + lane;
+    const bool live = i < a.n;
+    const float4 s = live ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    Anchor an;
+    if (lane == 0) {
+      double ci[3];
+      affine_map_d(K, s.x, s.y, s.z, ci);
+      anchor_set(an, s.x, s.y, s.z, ci);
+    }
+    an = anchor_bcast(an, 0);
+    if (!live) continue;
+    float m;
+    float3 g;
+    const CIdx c = map_from_anchor(an, K.A, s.x, s.y, s.z);
+    if (!eval_moving<GRAD>(a, c, a.with_derivative != 0, m, g)) continue;
+    const float diff = s.w - m;  // FixedImagePixelType diff, MeanSquares...Threader.hxx:46
+    acc[0].add(diff * diff);
+    ++nv;
+    if (a.with_derivative) {
+      const float t = 2.f * diff;
+      const float vx = s.x - K.c[0], vy = s.y - K.c[1], vz = s.z - K.c[2];
+      const float t0 = t * g.x, t1 = t * g.y, t2 = t * g.z;
+      acc[1].add(t0 * vx); acc[2].add(t0 * vy); acc[3].add(t0 * vz);
+      acc[4].add(t1 * vx); acc[5].add(t1 * vy); acc[6].add(t1 * vz);
+      acc[7].add(t2 * vx); acc[8].add(t2 * vy); acc[9].add(t2 * vz);
+      acc[10].add(t0); acc[11].add(t1); acc[12].add(t2);
+    }
+  }
+  block_commit<13>(acc, nv, a.acc, a.acc_n, red);
+  if (!last_block(a.tickets)) return;
+  if (threadIdx.x == 0) {
+    // AfterThreadedExecution + VerifyNumberOfValidPoints (ThreaderBase.hxx:116-172)
+    const unsigned long long N = __ldcg(a.acc_n);
+    const int P = a.with_derivative ? a.nparams : 0;
+    if (N == 0) {
+      a.out[0] = DBL_MAX;
+      a.out[1] = 0.0;
+      for (int p = 0; p < P; ++p) a.out[2 + p] = 0.0;
+      *a.status = GB_ERR_NO_VALID_POINTS;
+    } else {
+      const double inv = 1.0 / (double)N;
+      a.out[0] = __ldcg(&a.acc[0]) / (double)N;
+      a.out[1] = (double)N;
+      for (int p = 0; p < P; ++p) a.out[2 + p] = __ldcg(&a.acc[1 + p]) * inv;
+      *a.status = GB_OK;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mattes pass 1, affine: joint histogram (Parzen: box on fixed, cubic B-spline
+// on moving), fixed marginal counts, valid count, per-sample cache.
+
+__device__ __forceinline__ void parzen_weights(float term, int B, int& pdfm, float& arg, float w[4]) {
+  int midx = (int)term;  // static_cast<OffsetValueType>, Mattes...Threader.hxx:249
+  midx = midx < 2 ? 2 : (midx > B - 3 ? B - 3 : midx);
+  pdfm = midx - 1;
+  arg = (float)pdfm - term;
+  w[0] = bspline3(arg);
+  w[1] = bspline3(arg + 1.f);
+  w[2] = bspline3(arg + 2.f);
+  w[3] = bspline3(arg + 3.f);
+}
+
+// Adds one sample's four Parzen weights into the block histogram.  Lanes with
+// the same (fixed bin, first moving bin) key are summed in 2^26 fixed point
+// with one redux per weight, and only the group leader issues the shared atomics.
+__device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, const float w[4], float* hist,
+                                                    unsigned* fm) {
+  const unsigned okmask = __ballot_sync(0xffffffffu, ok);
+  if (!ok) return;
+  const unsigned peers = __match_any_sync(okmask, key);
+  const int leader = __ffs(peers) - 1;
+  const int lane = threadIdx.x & 31;
+  unsigned s[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) s[k] = __reduce_add_sync(peers, __float2uint_rn(w[k] * kQScale));
+  if (lane == leader) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (s[k]) atomicAdd(&hist[key + k], (float)s[k] * kQInv);
+    atomicAdd(&fm[fidx], (unsigned)__popc(peers));
+  }
+}
+
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
+  extern __shared__ float smem[];
+  const int B = a.bins;
+  float* hist = smem;
+  unsigned* fm = reinterpret_cast<unsigned*>(smem + B * B);
+  __shared__ AffConst K;
+  __shared__ double red[kBlock / 32][2];
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) hist[k] = 0.f;
+  for (int k = threadIdx.x; k < B; k += blockDim.x) fm[k] = 0u;
+  if (threadIdx.x == 0) affine_consts(a, K);
+  __syncthreads();
+  unsigned nv = 0;
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < a.n; base += stride) {
+    const int64_t i = base + lane;
+    const bool live = i < a.n;
+    const float4 s = live ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    Anchor an;
+    if (lane == 0) {
+      double ci[3];
+      affine_map_d(K, s.x, s.y, s.z, ci);
+      anchor_set(an, s.x, s.y, s.z, ci);
+    }
+    an = anchor_bcast(an, 0);
+    float m = 0.f;
+    float3 g = make_float3(0.f, 0.f, 0.f);
+    bool ok = false;
+    if (live) {
+      const CIdx c = map_from_anchor(an, K.A, s.x, s.y, s.z);
+      ok = eval_moving<GRAD>(a, c, a.with_derivative != 0, m, g);
+      // reject moving values outside [MovingImageTrueMin, MovingImageTrueMax], Mattes...Threader.hxx:238-245
+      ok = ok && !(m < a.mmin) && !(m > a.mmax);
+    }
+    // m / binsize - normalizedMin == (m - min) / binsize + 2 (padding), Mattes...v4.hxx:309-317
+    const float term = fmaf(m - a.mmin, a.m_inv_bs, 2.f);
+    if (a.with_derivative && live)
+      __stcs(a.cache + i, ok ? make_float4(term, g.x, g.y, g.z) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f));
+    int pdfm = 0;
+    float arg, w[4] = {0.f, 0.f, 0.f, 0.f};
+    const int fidx = __float_as_int(s.w);
+    if (ok) parzen_weights(term, B, pdfm, arg, w);
+    hist_add_aggregated(ok, fidx * B + pdfm, fidx, w, hist, fm);
+    nv += ok ? 1u : 0u;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) {
+    const float h = hist[k];
+    if (h != 0.f) atomicAdd(&a.hist[k], (double)h);
+  }
+  for (int k = threadIdx.x; k < B; k += blockDim.x) {
+    const unsigned c = fm[k];
+    if (c) atomicAdd(&a.fmarg[k], (unsigned long long)c);
+  }
+  KahanF dummy[1];
+  dummy[0].zero();
+  block_commit<1>(dummy, nv, nullptr, a.acc_n, red);
+}
+
+// Mattes finalize: one block per fixed bin.  FP64 normalization, marginals,
+// sum p (log(p/pm) - log pf), and the FP32 log(p/pm) table for pass 2
+// (ComputeResults, Mattes...v4.hxx:358-499; JointPDFSum .hxx:533-541).
+__global__ void k_mattes_finalize(EvalArgs a) {
+  extern __shared__ double colsum[];
+  __shared__ double sh_total, sh_logpf;
+  __shared__ double red[32];
+  const int B = a.bins;
+  const int f = blockIdx.x;
+  for (int m = threadIdx.x; m < B; m += blockDim.x) {
+    double s = 0.0;
+    for (int ff = 0; ff < B; ++ff) s += __ldcg(&a.hist[ff * B + m]);
+    colsum[m] = s;
+  }
+  __syncthreads();
+  const unsigned long long N = __ldcg(a.acc_n);
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int m = 0; m < B; ++m) t += colsum[m];
+    sh_total = t;
+    const double pf = (t > 0.0) ? (double)__ldcg(&a.fmarg[f]) / t : 0.0;
+    sh_logpf = pf > DBL_EPSILON ? log(pf) : 0.0;
+  }
+  __syncthreads();
+  const double total = sh_total;
+  const bool bad = (N == 0) || !(total >= DBL_EPSILON);
+  double part = 0.0;
+  if (!bad) {
+    const double nf = 1.0 / total;
+    const double pf = (double)__ldcg(&a.fmarg[f]) * nf;
+    for (int m = threadIdx.x; m < B; m += blockDim.x) {
+      const double p = __ldcg(&a.hist[f * B + m]) * nf;
+      const double pm = colsum[m] * nf;
+      a.pdf_out[f * B + m] = p;
+      float pr = 0.f;
+      if (pf > DBL_EPSILON && pm > DBL_EPSILON && p > DBL_EPSILON) {
+        const double lr = log(p / pm);
+        part += p * (lr - sh_logpf);
+        pr = (float)lr;
+      }
+      a.pratio[f * B + m] = pr;
+    }
+  } else {
+    for (int m = threadIdx.x; m < B; m += blockDim.x) {
+      a.pratio[f * B + m] = 0.f;
+      a.pdf_out[f * B + m] = 0.0;
+    }
+  }
+  part = warp_sum_d(part);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    if (s != 0.0) atomicAdd(&a.acc[0], s);
+    __threadfence();
+  }
+  if (!last_block(a.tickets + 1)) return;
+  if (threadIdx.x == 0) {
+    const int st = N == 0 ? GB_ERR_NO_VALID_POINTS : (bad ? GB_ERR_JOINT_PDF_SUM_ZERO : GB_OK);
+    *a.status = st;
+    if (!a.with_derivative) {
+      a.out[0] = st == GB_OK ? -1.0 * __ldcg(&a.acc[0]) : 0.0;  // metrics minimize: value = -MI
+      a.out[1] = (double)N;
+    }
+  }
+}
+
+// Mattes pass 2, affine: derivative from the cached Parzen terms and gradients.
+__global__ void __launch_bounds__(kBlock) k_mattes_pass2_affine(EvalArgs a) {
+  extern __shared__ float pr[];
+  __shared__ float c[3];
+  __shared__ double red[kBlock / 32][13];
+  const int B = a.bins;
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) pr[k] = __ldcg(&a.pratio[k]);
+  if (threadIdx.x < 3) c[threadIdx.x] = (float)a.center[threadIdx.x];
+  __syncthreads();
+  KahanF acc[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) acc[k].zero();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 cc = __ldcs(a.cache + i);
+    if (cc.x != cc.x) continue;  // rejected sample
+    const float4 s = __ldcs(a.samples + i);
+    int pdfm;
+    float arg;
+    int midx = (int)cc.x;
+    midx = midx < 2 ? 2 : (midx > B - 3 ? B - 3 : midx);
+    pdfm = midx - 1;
+    arg = (float)pdfm - cc.x;
+    const float* row = pr + __float_as_int(s.w) * B + pdfm;
+    const float w = row[0] * bspline3_deriv(arg) + row[1] * bspline3_deriv(arg + 1.f) +
+                    row[2] * bspline3_deriv(arg + 2.f) + row[3] * bspline3_deriv(arg + 3.f);
+    const float vx = s.x - c[0], vy = s.y - c[1], vz = s.z - c[2];
+    const float t0 = w * cc.y, t1 = w * cc.z, t2 = w * cc.w;
+    acc[0].add(t0 * vx); acc[1].add(t0 * vy); acc[2].add(t0 * vz);
+    acc[3].add(t1 * vx); acc[4].add(t1 * vy); acc[5].add(t1 * vz);
+    acc[6].add(t2 * vx); acc[7].add(t2 * vy); acc[8].add(t2 * vz);
+    acc[9].add(t0); acc[10].add(t1); acc[11].add(t2);
+  }
+  block_commit<12>(acc, 0u, a.acc + 1, nullptr, red);
+  if (!last_block(a.tickets + 2)) return;
+  if (threadIdx.x == 0) {
+    const unsigned long long N = __ldcg(a.acc_n);
+    const int st = __ldcg(a.status);
+    a.out[1] = (double)N;
+    if (st != GB_OK) {
+      a.out[0] = 0.0;
+      for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = 0.0;
+      return;
+    }
+    // nFactor = -1 / (MovingImageBinSize * N), Mattes...Threader.hxx:446-457
+    const double nFactor = -1.0 / (a.m_bs * (double)N);
+    a.out[0] = -1.0 * __ldcg(&a.acc[0]);
+    for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = __ldcg(&a.acc[1 + p]) * nFactor;
+  }
+}
+
+}  // namespace gb

@@ -1,0 +1,724 @@
+// gb_metric.cu -- C ABI of the registration-metric library (include/itk_gb300.h):
+// context and metric handles, Initialize, and one evaluation as a short
+// sequence of kernels on the handle's stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gb_init.cuh"
+#include "gb_internal.h"
+#include "gb_kernels.cuh"
+
+namespace gb {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* where) {
+  return fail(GB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define GB_CUDA(call)                                  \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+static int inv3(const double a[9], double out[9]) {
+  const double c00 = a[4] * a[8] - a[5] * a[7];
+  const double c01 = a[5] * a[6] - a[3] * a[8];
+  const double c02 = a[3] * a[7] - a[4] * a[6];
+  const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+  if (det == 0.0 || !std::isfinite(det)) return GB_ERR_BAD_ARG;
+  const double id = 1.0 / det;
+  out[0] = c00 * id;
+  out[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+  out[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+  out[3] = c01 * id;
+  out[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+  out[5] = (a[2] * a[3] - a[0] * a[5]) * id;
+  out[6] = c02 * id;
+  out[7] = (a[1] * a[6] - a[0] * a[7]) * id;
+  out[8] = (a[0] * a[4] - a[1] * a[3]) * id;
+  return GB_OK;
+}
+
+int geom_init(Geom& g, const int64_t size[3], const double spacing[3], const double origin[3], const double dir[9]) {
+  for (int i = 0; i < 3; ++i) {
+    if (size[i] <= 0 || size[i] > (1 << 20)) return fail(GB_ERR_BAD_ARG, "image size must be in [1, 2^20] per axis");
+    if (!(spacing[i] > 0.0) || !std::isfinite(spacing[i])) return fail(GB_ERR_BAD_ARG, "image spacing must be > 0");
+    g.size[i] = size[i];
+    g.spacing[i] = spacing[i];
+    g.origin[i] = origin[i];
+  }
+  for (int i = 0; i < 9; ++i) g.dir[i] = dir[i];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) g.i2p[r * 3 + c] = dir[r * 3 + c] * spacing[c];
+  if (inv3(g.i2p, g.p2i) != GB_OK) return fail(GB_ERR_BAD_ARG, "image direction matrix is singular");
+  g.set = true;
+  return GB_OK;
+}
+
+// host twins of float_to_ordered / ordered_to_float (gb_device.cuh)
+static int float_to_ordered_host(float f) {
+  int i;
+  memcpy(&i, &f, 4);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+static float ordered_to_float_host(int i) {
+  const int j = i >= 0 ? i : i ^ 0x7fffffff;
+  float f;
+  memcpy(&f, &j, 4);
+  return f;
+}
+
+static DGeom to_dgeom(const Geom& g) {
+  DGeom d;
+  for (int i = 0; i < 3; ++i) {
+    d.n[i] = g.size[i];
+    d.origin[i] = g.origin[i];
+  }
+  for (int i = 0; i < 9; ++i) {
+    d.i2p[i] = g.i2p[i];
+    d.p2i[i] = g.p2i[i];
+  }
+  return d;
+}
+
+static int grid_for(const gb_metric* m, int64_t n, int per_sm) {
+  const int64_t want = (n + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)m->ctx->sm_count * per_sm;
+  return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+// ===========================================================================
+// context
+
+extern "C" const char* gb_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" const char* gb_version(void) { return "itk_gb300 0.1 (sm_103a)"; }
+
+extern "C" int gb_ctx_create(int device, gb_ctx** out) {
+  if (!out) return fail(GB_ERR_BAD_ARG, "null output pointer");
+  int count = 0;
+  GB_CUDA(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) return fail(GB_ERR_BAD_ARG, "device index out of range");
+  GB_CUDA(cudaSetDevice(device));
+  int sms = 0;
+  GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  gb_ctx* c = new gb_ctx;
+  c->device = device;
+  c->sm_count = sms;
+  *out = c;
+  return GB_OK;
+}
+
+extern "C" int gb_ctx_destroy(gb_ctx* ctx) {
+  delete ctx;
+  return GB_OK;
+}
+
+extern "C" int gb_ctx_info(gb_ctx* ctx, int* sm_count, uint64_t* total_bytes, uint64_t* free_bytes) {
+  if (!ctx) return fail(GB_ERR_BAD_ARG, "null context");
+  GB_CUDA(cudaSetDevice(ctx->device));
+  size_t fr = 0, tot = 0;
+  GB_CUDA(cudaMemGetInfo(&fr, &tot));
+  if (sm_count) *sm_count = ctx->sm_count;
+  if (total_bytes) *total_bytes = tot;
+  if (free_bytes) *free_bytes = fr;
+  return GB_OK;
+}
+
+// ===========================================================================
+// metric handle
+
+extern "C" int gb_metric_create(gb_ctx* ctx, int kind, gb_metric** out) {
+  if (!ctx || !out) return fail(GB_ERR_BAD_ARG, "null argument");
+  if (kind != GB_METRIC_MEAN_SQUARES && kind != GB_METRIC_MATTES) return fail(GB_ERR_BAD_ARG, "unknown metric kind");
+  GB_CUDA(cudaSetDevice(ctx->device));
+  gb_metric* m = new gb_metric;
+  m->ctx = ctx;
+  m->kind = kind;
+  cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost(&m->h_status, sizeof(int) * 4);
+  if (e != cudaSuccess) {
+    delete m;
+    return cuda_fail(e, "gb_metric_create");
+  }
+  *out = m;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_destroy(gb_metric* m) {
+  if (!m) return GB_OK;
+  cudaSetDevice(m->ctx->device);
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  if (m->h_params) cudaFreeHost(m->h_params);
+  if (m->h_out) cudaFreeHost(m->h_out);
+  if (m->h_status) cudaFreeHost(m->h_status);
+  for (int i = 0; i < gb_metric::kMaxEvents; ++i)
+    if (m->events[i]) cudaEventDestroy(m->events[i]);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_number_of_histogram_bins(gb_metric* m, uint64_t bins) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  if (bins < 5) bins = 5;  // itkSetClampMacro(NumberOfHistogramBins, SizeValueType, 5, max)
+  if (bins > 4096) return fail(GB_ERR_BAD_ARG, "number of histogram bins above 4096");
+  m->bins = (int64_t)bins;
+  m->initialized = false;
+  return GB_OK;
+}
+
+static int set_image_common(gb_metric* m, int which, const float* src, bool device_src, const int64_t size[3],
+                            const double spacing[3], const double origin[3], const double direction[9]) {
+  if (!m || !src || !size || !spacing || !origin || !direction) return fail(GB_ERR_BAD_ARG, "null argument");
+  if (which != GB_IMAGE_FIXED && which != GB_IMAGE_MOVING) return fail(GB_ERR_BAD_ARG, "unknown image slot");
+  GB_CUDA(cudaSetDevice(m->ctx->device));
+  Geom g;
+  int rc = geom_init(g, size, spacing, origin, direction);
+  if (rc) return rc;
+  DevBuf<float>& buf = which == GB_IMAGE_FIXED ? m->d_fixed : m->d_moving;
+  const size_t n = (size_t)g.voxels();
+  buf.reset();
+  GB_CUDA(buf.alloc(n));
+  GB_CUDA(cudaMemcpyAsync(buf.p, src, n * sizeof(float), device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                          m->stream));
+  GB_CUDA(cudaStreamSynchronize(m->stream));
+  (which == GB_IMAGE_FIXED ? m->fixed : m->moving) = g;
+  if (which == GB_IMAGE_MOVING) m->grad_set = false;
+  m->initialized = false;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_image(gb_metric* m, int which, const float* voxels, const int64_t size[3],
+                                   const double spacing[3], const double origin[3], const double direction[9]) {
+  return set_image_common(m, which, voxels, false, size, spacing, origin, direction);
+}
+
+extern "C" int gb_metric_set_image_device(gb_metric* m, int which, const float* device_voxels, const int64_t size[3],
+                                          const double spacing[3], const double origin[3],
+                                          const double direction[9]) {
+  return set_image_common(m, which, device_voxels, true, size, spacing, origin, direction);
+}
+
+extern "C" int gb_metric_set_gradient_source(gb_metric* m, int source) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  if (source != GB_GRADIENT_IMAGE && source != GB_GRADIENT_CENTRAL_DIFFERENCE &&
+      source != GB_GRADIENT_RECURSIVE_GAUSSIAN)
+    return fail(GB_ERR_BAD_ARG, "unknown gradient source");
+  m->grad_source = source;
+  m->initialized = false;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_moving_gradient_image(gb_metric* m, const double* gradient_xyz) {
+  if (!m || !gradient_xyz) return fail(GB_ERR_BAD_ARG, "null argument");
+  if (!m->moving.set) return fail(GB_ERR_BAD_ARG, "set the moving image before its gradient image");
+  GB_CUDA(cudaSetDevice(m->ctx->device));
+  const size_t n = (size_t)m->moving.voxels() * 3;
+  m->d_grad_in.reset();
+  GB_CUDA(m->d_grad_in.alloc(n));
+  GB_CUDA(cudaMemcpyAsync(m->d_grad_in.p, gradient_xyz, n * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  GB_CUDA(cudaStreamSynchronize(m->stream));
+  m->grad_set = true;
+  m->initialized = false;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_virtual_domain(gb_metric* m, const int64_t size[3], const double spacing[3],
+                                            const double origin[3], const double direction[9]) {
+  if (!m || !size || !spacing || !origin || !direction) return fail(GB_ERR_BAD_ARG, "null argument");
+  Geom g;
+  int rc = geom_init(g, size, spacing, origin, direction);
+  if (rc) return rc;
+  m->virt = g;
+  m->virt_user = true;
+  m->initialized = false;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_sampled_points(gb_metric* m, const float* xyz, int64_t n, int virtual_space) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  if (n < 0 || (n > 0 && !xyz)) return fail(GB_ERR_BAD_ARG, "bad point array");
+  if (n > (int64_t)0x7fffffff) return fail(GB_ERR_BAD_ARG, "more than 2^31-1 sample points");
+  m->h_points.assign(xyz, xyz + 3 * n);
+  m->points_virtual = virtual_space != 0;
+  m->initialized = false;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_use_sampled_point_set(gb_metric* m, int on) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  m->use_sampled = on != 0;
+  m->initialized = false;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_moving_transform(gb_metric* m, int kind, const double* params, int64_t nparams,
+                                              const double* fixed, int64_t nfixed) {
+  if (!m || !params || !fixed) return fail(GB_ERR_BAD_ARG, "null argument");
+  if (kind == GB_TRANSFORM_AFFINE) {
+    if (nparams != 12 || nfixed != 3) return fail(GB_ERR_BAD_ARG, "affine transform takes 12 parameters and a 3-D centre");
+    m->nper = 0;
+  } else if (kind == GB_TRANSFORM_BSPLINE || kind == GB_TRANSFORM_COMPOSITE) {
+    if (nfixed != (kind == GB_TRANSFORM_BSPLINE ? 18 : 33))
+      return fail(GB_ERR_BAD_ARG, "B-spline fixed parameters: 18 (+15 for the initial affine of a composite)");
+    int64_t nper = 1;
+    for (int i = 0; i < 3; ++i) {
+      const double g = fixed[i];
+      if (!(g >= 4.0) || g != std::floor(g) || g > 4096.0)
+        return fail(GB_ERR_BAD_ARG, "B-spline grid size must be an integer >= 4 (mesh size >= 1)");
+      nper *= (int64_t)g;
+    }
+    if (nparams != 3 * nper) return fail(GB_ERR_BAD_ARG, "B-spline parameter count must be 3 * grid nodes");
+    if (nper > 65536) return fail(GB_ERR_UNSUPPORTED, "B-spline grids above 65536 nodes are not supported");
+    m->nper = nper;
+  } else {
+    return fail(GB_ERR_BAD_ARG, "unknown transform kind");
+  }
+  m->tkind = kind;
+  m->tparams.assign(params, params + nparams);
+  m->tfixed.assign(fixed, fixed + nfixed);
+  m->initialized = false;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_parameters(gb_metric* m, const double* params, int64_t nparams) {
+  if (!m || !params) return fail(GB_ERR_BAD_ARG, "null argument");
+  if (m->tkind < 0) return fail(GB_ERR_BAD_ARG, "no moving transform set");
+  if ((size_t)nparams != m->tparams.size()) return fail(GB_ERR_BAD_ARG, "parameter count mismatch");
+  std::copy(params, params + nparams, m->tparams.begin());
+  return GB_OK;
+}
+
+extern "C" int gb_metric_update_transform_parameters(gb_metric* m, const double* update, int64_t nparams,
+                                                     double factor) {
+  if (!m || !update) return fail(GB_ERR_BAD_ARG, "null argument");
+  if ((size_t)nparams != m->tparams.size())
+    return fail(GB_ERR_BAD_ARG, "Parameter update size must be same as transform parameter size");
+  if (factor == 1.0)
+    for (int64_t k = 0; k < nparams; ++k) m->tparams[k] += update[k];
+  else
+    for (int64_t k = 0; k < nparams; ++k) m->tparams[k] += update[k] * factor;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_get_parameters(gb_metric* m, double* params, int64_t nparams) {
+  if (!m || !params) return fail(GB_ERR_BAD_ARG, "null argument");
+  if ((size_t)nparams != m->tparams.size()) return fail(GB_ERR_BAD_ARG, "parameter count mismatch");
+  std::copy(m->tparams.begin(), m->tparams.end(), params);
+  return GB_OK;
+}
+
+extern "C" int gb_metric_get_number_of_parameters(gb_metric* m, int64_t* nparams) {
+  if (!m || !nparams) return fail(GB_ERR_BAD_ARG, "null argument");
+  *nparams = (int64_t)m->tparams.size();
+  return GB_OK;
+}
+
+// ===========================================================================
+// Initialize
+
+static size_t acc_layout_bytes(const gb_metric* m) {
+  const size_t P = m->tparams.size();
+  const size_t B = (size_t)m->bins;
+  // [value, deriv P] doubles | acc_n u64 | tickets 4 u32 | hist B*B doubles | fmarg B u64
+  return sizeof(double) * (1 + P) + 8 + 16 + sizeof(double) * B * B + 8 * B;
+}
+
+extern "C" int gb_metric_initialize(gb_metric* m) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  if (!m->fixed.set) return fail(GB_ERR_BAD_ARG, "FixedImage is not present");
+  if (!m->moving.set) return fail(GB_ERR_BAD_ARG, "MovingImage is not present");
+  if (m->tkind < 0) return fail(GB_ERR_BAD_ARG, "MovingTransform is not present");
+  if (m->grad_source == GB_GRADIENT_IMAGE && !m->grad_set)
+    return fail(GB_ERR_BAD_ARG, "gradient source is a gradient image but none was set");
+  if (m->grad_source == GB_GRADIENT_RECURSIVE_GAUSSIAN)
+    return fail(GB_ERR_UNSUPPORTED, "device recursive-Gaussian gradient is not available in this build");
+  if (m->tkind != GB_TRANSFORM_AFFINE) return fail(GB_ERR_UNSUPPORTED, "only the affine transform is available in this build");
+  GB_CUDA(cudaSetDevice(m->ctx->device));
+  m->initialized = false;
+  cudaStream_t st = m->stream;
+  if (!m->virt_user) m->virt = m->fixed;  // virtual domain from the fixed image, itkImageToImageMetricv4.hxx:98-112
+
+  const bool sampled = m->use_sampled;
+  if (sampled && m->h_points.empty()) return fail(GB_ERR_BAD_ARG, "VirtualSampledPointSet must have 1 or more points.");
+  const int64_t ncand = sampled ? (int64_t)(m->h_points.size() / 3) : m->virt.voxels();
+  if (ncand > (int64_t)0x7fffffff) return fail(GB_ERR_UNSUPPORTED, "more than 2^31-1 domain points");
+  m->ndomain = ncand;
+
+  DevBuf<float> d_pts;
+  if (sampled) {
+    GB_CUDA(d_pts.alloc(m->h_points.size()));
+    GB_CUDA(cudaMemcpyAsync(d_pts.p, m->h_points.data(), m->h_points.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+  }
+
+  // ---- Mattes ranges and bins (Mattes...v4.hxx:75-327)
+  const DGeom dfixed = to_dgeom(m->fixed), dvirt = to_dgeom(m->virt);
+  if (m->kind == GB_METRIC_MATTES) {
+    DevBuf<int> d_mm;
+    GB_CUDA(d_mm.alloc(4));
+    int init[4] = {float_to_ordered_host(FLT_MAX), float_to_ordered_host(-FLT_MAX), float_to_ordered_host(FLT_MAX),
+                   float_to_ordered_host(-FLT_MAX)};
+    GB_CUDA(cudaMemcpyAsync(d_mm.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    if (sampled) {
+      k_minmax_points<<<grid_for(m, ncand, 4), kBlock, 0, st>>>(d_pts.p, ncand, dfixed, m->d_fixed.p, d_mm.p);
+    } else {
+      k_minmax<<<grid_for(m, m->fixed.voxels(), 4), kBlock, 0, st>>>(m->d_fixed.p, m->fixed.voxels(), d_mm.p);
+    }
+    k_minmax<<<grid_for(m, m->moving.voxels(), 4), kBlock, 0, st>>>(m->d_moving.p, m->moving.voxels(), d_mm.p + 2);
+    GB_CUDA(cudaGetLastError());
+    int res[4];
+    GB_CUDA(cudaMemcpyAsync(res, d_mm.p, sizeof(res), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    const double fmin = (double)ordered_to_float_host(res[0]), fmax = (double)ordered_to_float_host(res[1]);
+    const double mmin = (double)ordered_to_float_host(res[2]), mmax = (double)ordered_to_float_host(res[3]);
+    const bool fempty = res[0] == float_to_ordered_host(FLT_MAX) && res[1] == float_to_ordered_host(-FLT_MAX);
+    m->mstate[0] = fmin;
+    m->mstate[1] = fmax;
+    m->mstate[2] = mmin;
+    m->mstate[3] = mmax;
+    if (fempty || fmax < fmin)
+      return fail(GB_ERR_FIXED_EMPTY,
+                  "No fixed-image samples were observed in the analysis region. Verify that the fixed image mask or "
+                  "sampled point set contains at least one valid pixel that overlaps the fixed image buffered region.");
+    if (fmax - fmin <= DBL_EPSILON)
+      return fail(GB_ERR_FIXED_CONSTANT,
+                  "All fixed-image samples in the analysis region have the same intensity value (" +
+                      std::to_string(fmin) +
+                      "). Mattes mutual information is undefined for a constant image: the marginal entropy is zero "
+                      "and no meaningful gradient can be computed.");
+    if (mmax < mmin)
+      return fail(GB_ERR_MOVING_EMPTY, "No moving-image samples were observed in the analysis region.");
+    if (mmax - mmin <= DBL_EPSILON)
+      return fail(GB_ERR_MOVING_CONSTANT,
+                  "All moving-image samples in the analysis region have the same intensity value (" +
+                      std::to_string(mmin) +
+                      "). Mattes mutual information is undefined for a constant image: the marginal entropy is zero "
+                      "and no meaningful gradient can be computed.");
+    const double padding = 2.0;
+    m->mstate[4] = (fmax - fmin) / (double)(m->bins - 2 * 2);
+    m->mstate[6] = fmin / m->mstate[4] - padding;
+    m->mstate[5] = (mmax - mmin) / (double)(m->bins - 2 * 2);
+    m->mstate[7] = mmin / m->mstate[5] - padding;
+  }
+
+  // ---- sample list: fixed values / bins in FP64, spatial sort
+  DevBuf<uint64_t> keys, keys_sorted;
+  DevBuf<uint32_t> vals, vals_sorted;
+  DevBuf<float4> recs;
+  DevBuf<unsigned long long> d_nvalid;
+  GB_CUDA(keys.alloc(ncand));
+  GB_CUDA(keys_sorted.alloc(ncand));
+  GB_CUDA(vals.alloc(ncand));
+  GB_CUDA(vals_sorted.alloc(ncand));
+  GB_CUDA(recs.alloc(ncand));
+  GB_CUDA(d_nvalid.alloc(1));
+  GB_CUDA(cudaMemsetAsync(d_nvalid.p, 0, sizeof(unsigned long long), st));
+  BuildArgs b{};
+  b.points = sampled ? d_pts.p : nullptr;
+  b.n = ncand;
+  b.points_virtual = m->points_virtual ? 1 : 0;
+  b.virt = dvirt;
+  b.fixed = dfixed;
+  b.fixed_img = m->d_fixed.p;
+  b.mattes = m->kind == GB_METRIC_MATTES;
+  b.bins = (int)m->bins;
+  b.f_bs = m->mstate[4];
+  b.f_normmin = m->mstate[6];
+  b.bspline = 0;
+  b.keys = keys.p;
+  b.vals = vals.p;
+  b.recs = recs.p;
+  b.bsp = nullptr;
+  b.bspf = nullptr;
+  b.nvalid = d_nvalid.p;
+  k_build_samples<<<(unsigned)((ncand + kBlock - 1) / kBlock), kBlock, 0, st>>>(b);
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(sort_pairs_u64(keys.p, keys_sorted.p, vals.p, vals_sorted.p, ncand, 64, st));
+  unsigned long long nvalid = 0;
+  GB_CUDA(cudaMemcpyAsync(&nvalid, d_nvalid.p, sizeof(nvalid), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  m->nsamples = (int64_t)nvalid;
+  m->d_samples.reset();
+  GB_CUDA(m->d_samples.alloc(std::max<int64_t>(1, m->nsamples)));
+  if (m->nsamples > 0)
+    k_gather_samples<<<(unsigned)((m->nsamples + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+        vals_sorted.p, m->nsamples, recs.p, m->d_samples.p, nullptr, nullptr, nullptr, nullptr);
+  GB_CUDA(cudaGetLastError());
+
+  // ---- moving image: packed (value, gradient) for the gradient-image path
+  if (m->grad_source == GB_GRADIENT_IMAGE) {
+    const int64_t nv = m->moving.voxels();
+    m->d_mov4.reset();
+    GB_CUDA(m->d_mov4.alloc(nv));
+    k_pack_moving<<<(unsigned)((nv + kBlock - 1) / kBlock), kBlock, 0, st>>>(m->d_moving.p, m->d_grad_in.p, nv,
+                                                                              m->d_mov4.p);
+    GB_CUDA(cudaGetLastError());
+  }
+
+  // ---- evaluation buffers
+  const size_t P = m->tparams.size();
+  m->acc_bytes = acc_layout_bytes(m);
+  m->d_acc.reset();
+  GB_CUDA(m->d_acc.alloc(m->acc_bytes));
+  GB_CUDA(m->d_params.alloc(P));
+  m->d_out.reset();
+  GB_CUDA(m->d_out.alloc(2 + P));
+  GB_CUDA(m->d_status.alloc(1));
+  if (m->kind == GB_METRIC_MATTES) {
+    m->d_pratio.reset();
+    GB_CUDA(m->d_pratio.alloc((size_t)(m->bins * m->bins)));
+    m->d_pdf.reset();
+    GB_CUDA(m->d_pdf.alloc((size_t)(m->bins * m->bins)));
+    GB_CUDA(cudaMemsetAsync(m->d_pdf.p, 0, sizeof(double) * m->bins * m->bins, st));
+    m->d_cache.reset();
+    GB_CUDA(m->d_cache.alloc(std::max<int64_t>(1, m->nsamples)));
+  }
+  if (m->h_params) cudaFreeHost(m->h_params);
+  if (m->h_out) cudaFreeHost(m->h_out);
+  m->h_params = nullptr;
+  m->h_out = nullptr;
+  GB_CUDA(cudaMallocHost(&m->h_params, sizeof(double) * std::max<size_t>(P, 1)));
+  GB_CUDA(cudaMallocHost(&m->h_out, sizeof(double) * (2 + P)));
+  GB_CUDA(cudaStreamSynchronize(st));
+  m->initialized = true;
+  return GB_OK;
+}
+
+// ===========================================================================
+// evaluation
+
+static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, double* d_out, bool deriv) {
+  memset(&a, 0, sizeof(a));
+  a.samples = m->d_samples.p;
+  a.n = m->nsamples;
+  a.mov4 = m->d_mov4.p;
+  a.mov1 = m->d_moving.p;
+  a.nx = (int)m->moving.size[0];
+  a.ny = (int)m->moving.size[1];
+  a.nz = (int)m->moving.size[2];
+  for (int i = 0; i < 9; ++i) a.m_p2i[i] = m->moving.p2i[i];
+  for (int i = 0; i < 3; ++i) a.m_origin[i] = m->moving.origin[i];
+  // central difference: +0.5 spacing along physical axis d, in index space
+  for (int d = 0; d < 3; ++d) {
+    const double off = 0.5 * m->moving.spacing[d];
+    for (int k = 0; k < 3; ++k) a.cd_off[3 * d + k] = (float)(m->moving.p2i[3 * k + d] * off);
+    a.cd_inv_delta[d] = (float)(1.0 / ((off) - (-off)));
+  }
+  a.params = d_params;
+  a.nparams = (int)m->tparams.size();
+  if (m->tkind == GB_TRANSFORM_AFFINE)
+    for (int i = 0; i < 3; ++i) a.center[i] = m->tfixed[i];
+  a.bins = (int)m->bins;
+  a.mmin = (float)m->mstate[2];
+  a.mmax = (float)m->mstate[3];
+  a.m_bs = m->mstate[5];
+  a.m_inv_bs = (float)(1.0 / m->mstate[5]);
+  unsigned char* base = m->d_acc.p;
+  const size_t P = m->tparams.size();
+  a.acc = reinterpret_cast<double*>(base);
+  a.acc_n = reinterpret_cast<unsigned long long*>(base + sizeof(double) * (1 + P));
+  a.tickets = reinterpret_cast<unsigned*>(base + sizeof(double) * (1 + P) + 8);
+  a.hist = reinterpret_cast<double*>(base + sizeof(double) * (1 + P) + 8 + 16);
+  a.fmarg = reinterpret_cast<unsigned long long*>(base + sizeof(double) * (1 + P) + 8 + 16 +
+                                                  sizeof(double) * m->bins * m->bins);
+  a.cache = m->d_cache.p;
+  a.pratio = m->d_pratio.p;
+  a.pdf_out = m->d_pdf.p;
+  a.out = d_out;
+  a.status = m->d_status.p;
+  a.with_derivative = deriv ? 1 : 0;
+}
+
+// Enqueues one evaluation; results land in d_out = [value, nvalid, derivative...].
+static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv) {
+  cudaStream_t st = m->stream;
+  EvalArgs a;
+  fill_eval_args(m, a, d_params, d_out, deriv);
+  GB_CUDA(cudaMemsetAsync(m->d_acc.p, 0, m->acc_bytes, st));
+  if (m->nsamples == 0) {
+    // no valid fixed sample at all: every point is invalid
+    const int code = GB_ERR_NO_VALID_POINTS;
+    GB_CUDA(cudaMemcpyAsync(m->d_status.p, &code, sizeof(int), cudaMemcpyHostToDevice, st));
+    const double v[2] = {m->kind == GB_METRIC_MEAN_SQUARES ? DBL_MAX : 0.0, 0.0};
+    GB_CUDA(cudaMemcpyAsync(d_out, v, sizeof(v), cudaMemcpyHostToDevice, st));
+    if (deriv && !m->tparams.empty()) GB_CUDA(cudaMemsetAsync(d_out + 2, 0, sizeof(double) * m->tparams.size(), st));
+    return GB_OK;
+  }
+  const bool cd = m->grad_source == GB_GRADIENT_CENTRAL_DIFFERENCE;
+  m->nevents = 0;
+  m->mark();
+  if (m->kind == GB_METRIC_MEAN_SQUARES) {
+    const int grid = grid_for(m, m->nsamples, 4);
+    if (cd) k_msq_affine<kGradCentralDifference><<<grid, kBlock, 0, st>>>(a);
+    else k_msq_affine<kGradImage><<<grid, kBlock, 0, st>>>(a);
+    GB_CUDA(cudaGetLastError());
+    m->mark();
+    return GB_OK;
+  }
+  // Mattes: pass 1, finalize, pass 2
+  const int B = (int)m->bins;
+  const size_t sh1 = sizeof(float) * B * B + sizeof(unsigned) * B;
+  const size_t sh2 = sizeof(float) * B * B;
+  if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > ~220)");
+  const int grid = grid_for(m, m->nsamples, 2);
+  if (cd) {
+    cudaFuncSetAttribute(k_mattes_pass1_affine<kGradCentralDifference>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sh1);
+    k_mattes_pass1_affine<kGradCentralDifference><<<grid, kBlock, sh1, st>>>(a);
+  } else {
+    cudaFuncSetAttribute(k_mattes_pass1_affine<kGradImage>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh1);
+    k_mattes_pass1_affine<kGradImage><<<grid, kBlock, sh1, st>>>(a);
+  }
+  GB_CUDA(cudaGetLastError());
+  m->mark();
+  k_mattes_finalize<<<B, 128, sizeof(double) * B, st>>>(a);
+  GB_CUDA(cudaGetLastError());
+  m->mark();
+  if (deriv) {
+    cudaFuncSetAttribute(k_mattes_pass2_affine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh2);
+    k_mattes_pass2_affine<<<grid_for(m, m->nsamples, 4), kBlock, sh2, st>>>(a);
+    GB_CUDA(cudaGetLastError());
+    m->mark();
+  }
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_profiling(gb_metric* m, int on) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  m->profiling = on != 0;
+  m->nevents = 0;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_get_kernel_times(gb_metric* m, double* ms, int max_kernels, int* count) {
+  if (!m || !count) return fail(GB_ERR_BAD_ARG, "null argument");
+  GB_CUDA(cudaSetDevice(m->ctx->device));
+  const int n = m->nevents > 1 ? m->nevents - 1 : 0;
+  *count = n;
+  if (n == 0) return GB_OK;
+  GB_CUDA(cudaEventSynchronize(m->events[m->nevents - 1]));
+  for (int i = 0; i < n && i < max_kernels; ++i) {
+    float t = 0.f;
+    GB_CUDA(cudaEventElapsedTime(&t, m->events[i], m->events[i + 1]));
+    if (ms) ms[i] = (double)t;
+  }
+  return GB_OK;
+}
+
+static int eval_host(gb_metric* m, double* value, double* derivative, int64_t nparams, bool deriv) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
+  const size_t P = m->tparams.size();
+  if (deriv && (size_t)nparams != P) return fail(GB_ERR_BAD_ARG, "derivative size must equal the number of parameters");
+  GB_CUDA(cudaSetDevice(m->ctx->device));
+  cudaStream_t st = m->stream;
+  std::copy(m->tparams.begin(), m->tparams.end(), m->h_params);
+  GB_CUDA(cudaMemcpyAsync(m->d_params.p, m->h_params, sizeof(double) * P, cudaMemcpyHostToDevice, st));
+  int rc = enqueue_eval(m, m->d_params.p, m->d_out.p, deriv);
+  if (rc) return rc;
+  GB_CUDA(cudaMemcpyAsync(m->h_out, m->d_out.p, sizeof(double) * (2 + (deriv ? P : 0)), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(m->h_status, m->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  const int status = *m->h_status;
+  m->last_status = status;
+  m->last_nvalid = (uint64_t)m->h_out[1];
+  if (value) *value = m->h_out[0];
+  if (deriv)
+    for (size_t p = 0; p < P; ++p) derivative[p] = m->h_out[2 + p];
+  if (status == GB_ERR_NO_VALID_POINTS) {
+    if (m->kind == GB_METRIC_MATTES)
+      return fail(status,
+                  "All samples map outside moving image buffer. The images do not sufficiently overlap. They need to "
+                  "be initialized to have more overlap before this metric will work. For instance, you can align the "
+                  "image centers by translation.");
+    return fail(status,
+                "No valid points were found during metric evaluation. For image metrics, verify that the images "
+                "overlap appropriately.");
+  }
+  if (status == GB_ERR_JOINT_PDF_SUM_ZERO) return fail(status, "Joint PDF summed to zero");
+  if (status != GB_OK) return fail(status, "metric evaluation failed");
+  return GB_OK;
+}
+
+extern "C" int gb_metric_get_value_and_derivative(gb_metric* m, double* value, double* derivative, int64_t nparams) {
+  if (!derivative || !value) return fail(GB_ERR_BAD_ARG, "null output");
+  return eval_host(m, value, derivative, nparams, true);
+}
+
+extern "C" int gb_metric_get_value(gb_metric* m, double* value) {
+  if (!value) return fail(GB_ERR_BAD_ARG, "null output");
+  return eval_host(m, value, nullptr, 0, false);
+}
+
+extern "C" int gb_metric_get_number_of_valid_points(gb_metric* m, uint64_t* nvalid) {
+  if (!m || !nvalid) return fail(GB_ERR_BAD_ARG, "null argument");
+  *nvalid = m->last_nvalid;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_get_number_of_domain_points(gb_metric* m, uint64_t* n) {
+  if (!m || !n) return fail(GB_ERR_BAD_ARG, "null argument");
+  *n = (uint64_t)m->ndomain;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_get_joint_pdf(gb_metric* m, double* out, int64_t n) {
+  if (!m || !out) return fail(GB_ERR_BAD_ARG, "null argument");
+  if (m->kind != GB_METRIC_MATTES) return fail(GB_ERR_BAD_ARG, "joint PDF exists for the Mattes metric only");
+  if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
+  if (n != m->bins * m->bins) return fail(GB_ERR_BAD_ARG, "joint PDF size must be bins*bins");
+  GB_CUDA(cudaSetDevice(m->ctx->device));
+  GB_CUDA(cudaMemcpyAsync(out, m->d_pdf.p, sizeof(double) * n, cudaMemcpyDeviceToHost, m->stream));
+  GB_CUDA(cudaStreamSynchronize(m->stream));
+  return GB_OK;
+}
+
+extern "C" int gb_metric_get_mattes_state(gb_metric* m, double out8[8]) {
+  if (!m || !out8) return fail(GB_ERR_BAD_ARG, "null argument");
+  if (m->kind != GB_METRIC_MATTES) return fail(GB_ERR_BAD_ARG, "Mattes metric only");
+  for (int i = 0; i < 8; ++i) out8[i] = m->mstate[i];
+  return GB_OK;
+}
+
+extern "C" int gb_metric_get_stream(gb_metric* m, uint64_t* stream) {
+  if (!m || !stream) return fail(GB_ERR_BAD_ARG, "null argument");
+  *stream = (uint64_t)(uintptr_t)m->stream;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_evaluate_device(gb_metric* m, const double* device_params, double* device_out,
+                                         int with_derivative) {
+  if (!m || !device_params || !device_out) return fail(GB_ERR_BAD_ARG, "null argument");
+  if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
+  GB_CUDA(cudaSetDevice(m->ctx->device));
+  return enqueue_eval(m, device_params, device_out, with_derivative != 0);
+}
+
+extern "C" int gb_metric_synchronize(gb_metric* m) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  GB_CUDA(cudaSetDevice(m->ctx->device));
+  GB_CUDA(cudaMemcpyAsync(m->h_status, m->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+  GB_CUDA(cudaStreamSynchronize(m->stream));
+  return *m->h_status;
+}

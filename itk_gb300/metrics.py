@@ -1,0 +1,275 @@
+"""Host-side mirror of ITK's v4 image metrics over the GB300 C ABI.
+
+Class and method names follow ``itk::MeanSquaresImageToImageMetricv4`` and
+``itk::MattesMutualInformationImageToImageMetricv4`` on ``Image<float,3>``
+(Registration/Metricsv4/include/itkImageToImageMetricv4.h,
+itkMattesMutualInformationImageToImageMetricv4.h) so code written against
+ITK reads the same: SetFixedImage / SetMovingImage / SetMovingTransform /
+Initialize / GetValueAndDerivative.  Every evaluation runs on the GPU; errors
+come back as ``ExceptionObject`` carrying the reference's message text.
+"""
+from __future__ import annotations
+
+import ctypes
+import warnings
+
+import numpy as np
+
+from . import _capi
+from ._capi import ExceptionObject, check, f64, i64, ptr
+from .image import GradientImage, Image
+
+_ctx_cache = {}
+
+
+def context(device: int = 0):
+    """One ``gb_ctx`` per device, created on first use."""
+    if device not in _ctx_cache:
+        L = _capi.lib()
+        h = ctypes.c_void_p()
+        check(L.gb_ctx_create(device, ctypes.byref(h)))
+        _ctx_cache[device] = h
+    return _ctx_cache[device]
+
+
+class ImageToImageMetricv4:
+    """Common part of the two metrics (itkImageToImageMetricv4.h)."""
+
+    _kind = None
+
+    def __init__(self, device: int = 0):
+        self._L = _capi.lib()
+        self._h = ctypes.c_void_p()
+        check(self._L.gb_metric_create(context(device), self._kind, ctypes.byref(self._h)))
+        self._fixed = None
+        self._moving = None
+        self._transform = None
+        self._gradient = None
+        self._use_moving_gradient_filter = True
+        self._use_sampled = False
+        self._points = None
+        self._points_virtual = True
+        self._virtual = None
+        self._value = np.finfo(np.float64).max
+        self._nparams = 0
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None) and self._h.value:
+                self._L.gb_metric_destroy(self._h)
+                self._h = ctypes.c_void_p()
+        except Exception:
+            pass
+
+    # ---- inputs
+    def SetFixedImage(self, image: Image):
+        self._fixed = image
+        self._set_image(_capi.GB_IMAGE_FIXED, image)
+
+    def SetMovingImage(self, image: Image):
+        self._moving = image
+        self._set_image(_capi.GB_IMAGE_MOVING, image)
+
+    def _set_image(self, which, image):
+        a = image.array
+        check(self._L.gb_metric_set_image(self._h, which, ptr(a), ptr(i64(image.GetSize())), ptr(f64(image.spacing)),
+                                          ptr(f64(image.origin)), ptr(f64(image.direction.reshape(9)))))
+
+    def GetFixedImage(self):
+        return self._fixed
+
+    def GetMovingImage(self):
+        return self._moving
+
+    def SetMovingTransform(self, transform):
+        self._transform = transform
+
+    def GetMovingTransform(self):
+        return self._transform
+
+    def SetUseMovingImageGradientFilter(self, on: bool):
+        """False selects CentralDifferenceImageFunction at each mapped point."""
+        self._use_moving_gradient_filter = bool(on)
+
+    def GetUseMovingImageGradientFilter(self):
+        return self._use_moving_gradient_filter
+
+    def SetMovingImageGradientImage(self, gradient):
+        """Supplies the gradient image the metric's gradient filter would compute."""
+        self._gradient = gradient if isinstance(gradient, GradientImage) else GradientImage(gradient)
+
+    def SetVirtualDomainFromImage(self, image: Image):
+        self._virtual = image
+        check(self._L.gb_metric_set_virtual_domain(self._h, ptr(i64(image.GetSize())), ptr(f64(image.spacing)),
+                                                   ptr(f64(image.origin)), ptr(f64(image.direction.reshape(9)))))
+
+    def SetFixedSampledPointSet(self, points):
+        self._points = np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 3))
+        self._points_virtual = False
+
+    def SetVirtualSampledPointSet(self, points):
+        self._points = np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 3))
+        self._points_virtual = True
+
+    def SetUseSampledPointSet(self, on: bool):
+        self._use_sampled = bool(on)
+
+    def UseSampledPointSetOn(self):
+        self.SetUseSampledPointSet(True)
+
+    def UseVirtualSampledPointSetOn(self):
+        self._points_virtual = True
+
+    # ---- set-up
+    def _push_transform(self):
+        kind, params, fixed = self._transform.flat()
+        params, fixed = f64(params), f64(fixed)
+        check(self._L.gb_metric_set_moving_transform(self._h, kind, ptr(params), params.size, ptr(fixed), fixed.size))
+        self._nparams = params.size
+
+    def Initialize(self):
+        if self._fixed is None:
+            raise ExceptionObject(_capi.GB_ERR_BAD_ARG, "FixedImage is not present")
+        if self._moving is None:
+            raise ExceptionObject(_capi.GB_ERR_BAD_ARG, "MovingImage is not present")
+        if self._transform is None:
+            raise ExceptionObject(_capi.GB_ERR_BAD_ARG, "MovingTransform is not present")
+        self._push_transform()
+        if self._use_moving_gradient_filter:
+            if self._gradient is not None:
+                check(self._L.gb_metric_set_gradient_source(self._h, _capi.GB_GRADIENT_IMAGE))
+                check(self._L.gb_metric_set_moving_gradient_image(self._h, ptr(self._gradient.array)))
+            else:
+                check(self._L.gb_metric_set_gradient_source(self._h, _capi.GB_GRADIENT_RECURSIVE_GAUSSIAN))
+        else:
+            check(self._L.gb_metric_set_gradient_source(self._h, _capi.GB_GRADIENT_CENTRAL_DIFFERENCE))
+        if self._use_sampled:
+            if self._points is None or len(self._points) == 0:
+                raise ExceptionObject(_capi.GB_ERR_BAD_ARG, "VirtualSampledPointSet must have 1 or more points.")
+            check(self._L.gb_metric_set_sampled_points(self._h, ptr(self._points), self._points.shape[0],
+                                                       int(self._points_virtual)))
+        check(self._L.gb_metric_use_sampled_point_set(self._h, int(self._use_sampled)))
+        self._pre_initialize()
+        check(self._L.gb_metric_initialize(self._h))
+
+    def _pre_initialize(self):
+        pass
+
+    # ---- evaluation
+    def _sync_params(self):
+        p = f64(self._transform.GetParameters())
+        if p.size != self._nparams:
+            raise ExceptionObject(_capi.GB_ERR_BAD_ARG, "transform parameter count changed; call Initialize()")
+        check(self._L.gb_metric_set_parameters(self._h, ptr(p), p.size))
+
+    def _handle_status(self, rc):
+        if rc == _capi.GB_OK:
+            return
+        if rc == _capi.GB_ERR_NO_VALID_POINTS and self._kind == _capi.GB_METRIC_MEAN_SQUARES:
+            warnings.warn(_capi.last_error())
+            return
+        raise ExceptionObject(rc, _capi.last_error())
+
+    def GetValueAndDerivative(self):
+        """Returns (value, derivative) like GetValueAndDerivative(value, derivative)."""
+        self._sync_params()
+        value = np.zeros(1)
+        deriv = np.zeros(self._nparams)
+        rc = self._L.gb_metric_get_value_and_derivative(self._h, ptr(value), ptr(deriv), self._nparams)
+        self._handle_status(rc)
+        self._value = float(value[0])
+        return self._value, deriv
+
+    def GetValue(self):
+        self._sync_params()
+        value = np.zeros(1)
+        rc = self._L.gb_metric_get_value(self._h, ptr(value))
+        self._handle_status(rc)
+        self._value = float(value[0])
+        return self._value
+
+    def GetDerivative(self):
+        return self.GetValueAndDerivative()[1]
+
+    def GetCurrentValue(self):
+        return self._value
+
+    def GetNumberOfValidPoints(self):
+        n = ctypes.c_uint64()
+        check(self._L.gb_metric_get_number_of_valid_points(self._h, ctypes.byref(n)))
+        return int(n.value)
+
+    def GetNumberOfDomainPoints(self):
+        n = ctypes.c_uint64()
+        check(self._L.gb_metric_get_number_of_domain_points(self._h, ctypes.byref(n)))
+        return int(n.value)
+
+    def GetNumberOfParameters(self):
+        return self._transform.GetNumberOfParameters()
+
+    def UpdateTransformParameters(self, update, factor=1.0):
+        self._transform.UpdateTransformParameters(update, factor)
+
+    # ---- device-resident form
+    @property
+    def handle(self):
+        return self._h
+
+    def stream(self) -> int:
+        s = ctypes.c_uint64()
+        check(self._L.gb_metric_get_stream(self._h, ctypes.byref(s)))
+        return int(s.value)
+
+    def evaluate_device(self, device_params_ptr: int, device_out_ptr: int, with_derivative: bool = True):
+        check(self._L.gb_metric_evaluate_device(self._h, ctypes.c_void_p(device_params_ptr),
+                                                ctypes.c_void_p(device_out_ptr), int(with_derivative)))
+
+    def synchronize(self) -> int:
+        return self._L.gb_metric_synchronize(self._h)
+
+    def set_profiling(self, on: bool = True):
+        check(self._L.gb_metric_set_profiling(self._h, int(on)))
+
+    def kernel_times_ms(self):
+        """Device milliseconds of each kernel of the last evaluation (profiling on)."""
+        buf = np.zeros(8)
+        n = ctypes.c_int()
+        check(self._L.gb_metric_get_kernel_times(self._h, ptr(buf), 8, ctypes.byref(n)))
+        return buf[:n.value].copy()
+
+
+class MeanSquaresImageToImageMetricv4(ImageToImageMetricv4):
+    """Mean of squared intensity differences; derivative 2 (f - m) J^T grad m / N."""
+
+    _kind = _capi.GB_METRIC_MEAN_SQUARES
+
+
+class MattesMutualInformationImageToImageMetricv4(ImageToImageMetricv4):
+    """Mattes mutual information with cubic B-spline Parzen windows (default 50 bins)."""
+
+    _kind = _capi.GB_METRIC_MATTES
+
+    def __init__(self, device: int = 0):
+        super().__init__(device)
+        self._bins = 50
+
+    def SetNumberOfHistogramBins(self, bins: int):
+        self._bins = max(int(bins), 5)  # itkSetClampMacro(..., 5, max)
+
+    def GetNumberOfHistogramBins(self):
+        return self._bins
+
+    def _pre_initialize(self):
+        check(self._L.gb_metric_set_number_of_histogram_bins(self._h, self._bins))
+
+    def GetJointPDF(self):
+        out = np.zeros((self._bins, self._bins))
+        check(self._L.gb_metric_get_joint_pdf(self._h, ptr(out), out.size))
+        return out
+
+    def GetHistogramState(self):
+        """(fixed min, fixed max, moving min, moving max, fixed bin size, moving bin size,
+        fixed normalized min, moving normalized min)."""
+        out = np.zeros(8)
+        check(self._L.gb_metric_get_mattes_state(self._h, ptr(out)))
+        return out

@@ -1,0 +1,216 @@
+"""ctypes front end of the FP64 CPU oracle (oracle/itk_oracle.c).
+
+TEST INFRASTRUCTURE ONLY.  The oracle is the checker for the GPU library:
+tests, ``__graft_entry__.smoke()`` and the CPU-baseline / reference legs of
+``bench.py`` use it.  Nothing in ``itk_gb300`` imports this module.
+
+Arrays follow ITK's memory order: a 3-D image is a numpy array of shape
+(nz, ny, nx), x fastest; a gradient image is (nz, ny, nx, 3) float64 like
+``Image<CovariantVector<double,3>,3>``; sample points are (n, 3) float32 like
+``PointSet<float,3>`` (Registration/RegistrationMethodsv4/include/
+itkImageRegistrationMethodv4.hxx:925-1003 stores them as float).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libitk_oracle.so")
+_lib = None
+
+TRANSFORM_AFFINE = 0
+TRANSFORM_BSPLINE = 1
+TRANSFORM_COMPOSITE = 2
+
+STATUS_NAMES = {
+    0: "OK",
+    1: "BAD_ARG",
+    2: "NO_VALID_POINTS",
+    3: "JOINT_PDF_SUM_ZERO",
+    4: "FIXED_CONSTANT",
+    5: "MOVING_CONSTANT",
+    6: "FIXED_EMPTY",
+    7: "MOVING_EMPTY",
+    8: "OOM",
+}
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (portable C, no ISA flags)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(os.path.join(_HERE, f))
+                                          for f in ("itk_oracle.c", "itk_oracle.h"))):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.c_void_p
+        i64 = ctypes.c_int64
+        L.orc_msq_flat.argtypes = [P, P, P, P, P, P, P, P, i64, ctypes.c_int, P, i64, P, i64,
+                                   ctypes.c_int, ctypes.c_int, P, P, P]
+        L.orc_mattes_flat.argtypes = [P, P, P, P, P, P, P, P, i64, ctypes.c_int, P, i64, P, i64,
+                                      i64, ctypes.c_int, ctypes.c_int, P, P, P, P, P]
+        L.orc_transform_point_flat.argtypes = [ctypes.c_int, P, i64, P, i64, P, i64, P]
+        L.orc_interpolate_flat.argtypes = [P, P, P, P, i64, P, P]
+        L.orc_central_difference_flat.argtypes = [P, P, P, P, i64, P]
+        L.orc_bspline_weights.argtypes = [P, P, P]
+        L.orc_bspline3.argtypes = [ctypes.c_double]
+        L.orc_bspline3.restype = ctypes.c_double
+        L.orc_bspline3_derivative.argtypes = [ctypes.c_double]
+        L.orc_bspline3_derivative.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+@dataclass
+class Geometry:
+    """Image geometry as ITK's ImageBase holds it (start index 0)."""
+    size: tuple          # (nx, ny, nz)
+    spacing: tuple = (1.0, 1.0, 1.0)
+    origin: tuple = (0.0, 0.0, 0.0)
+    direction: tuple = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
+
+    def flat(self):
+        return np.ascontiguousarray(np.array(list(self.spacing) + list(self.origin) + list(self.direction),
+                                             dtype=np.float64))
+
+    def size_array(self):
+        return np.ascontiguousarray(np.array(self.size, dtype=np.int64))
+
+
+@dataclass
+class Transform:
+    """Flat transform description (see itk_oracle.h for the encodings)."""
+    kind: int
+    params: np.ndarray
+    fixed: np.ndarray
+
+    @property
+    def nparams(self):
+        return int(self.params.size)
+
+
+def _img(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _grad(g):
+    return None if g is None else np.ascontiguousarray(g, dtype=np.float64)
+
+
+def _pts(p):
+    return None if p is None else np.ascontiguousarray(np.asarray(p, dtype=np.float32).reshape(-1, 3))
+
+
+def _threads(nthreads, pixel_double):
+    t = int(nthreads or os.cpu_count()) & 0xFFFF
+    return t | (0x10000 if pixel_double else 0)
+
+
+def mean_squares(fixed, fgeom, moving, mgeom, transform, moving_grad=None, points=None, nthreads=None,
+                 compute_derivative=True, pixel_double=False):
+    """Returns (status, value, derivative, nvalid)."""
+    L = lib()
+    fixed, moving = _img(fixed), _img(moving)
+    mg, pts = _grad(moving_grad), _pts(points)
+    tp = np.ascontiguousarray(transform.params, dtype=np.float64)
+    tf = np.ascontiguousarray(transform.fixed, dtype=np.float64)
+    value = np.zeros(1, np.float64)
+    deriv = np.zeros(tp.size, np.float64)
+    nvalid = np.zeros(1, np.uint64)
+    fs, fg, ms, mgeo = fgeom.size_array(), fgeom.flat(), mgeom.size_array(), mgeom.flat()
+    rc = L.orc_msq_flat(_p(fixed), _p(fs), _p(fg), _p(moving), _p(ms), _p(mgeo), _p(mg), _p(pts),
+                        0 if pts is None else pts.shape[0], transform.kind, _p(tp), tp.size, _p(tf), tf.size,
+                        _threads(nthreads, pixel_double), int(compute_derivative), _p(value), _p(deriv),
+                        _p(nvalid))
+    return rc, float(value[0]), deriv, int(nvalid[0])
+
+
+def mattes(fixed, fgeom, moving, mgeom, transform, bins=50, moving_grad=None, points=None, nthreads=None,
+           compute_derivative=True, pixel_double=False):
+    """Returns (status, value, derivative, nvalid, joint_pdf[bins,bins], state[8])."""
+    L = lib()
+    fixed, moving = _img(fixed), _img(moving)
+    mg, pts = _grad(moving_grad), _pts(points)
+    tp = np.ascontiguousarray(transform.params, dtype=np.float64)
+    tf = np.ascontiguousarray(transform.fixed, dtype=np.float64)
+    b = max(int(bins), 5)
+    value = np.zeros(1, np.float64)
+    deriv = np.zeros(tp.size, np.float64)
+    nvalid = np.zeros(1, np.uint64)
+    pdf = np.zeros((b, b), np.float64)
+    state = np.zeros(8, np.float64)
+    fs, fg, ms, mgeo = fgeom.size_array(), fgeom.flat(), mgeom.size_array(), mgeom.flat()
+    rc = L.orc_mattes_flat(_p(fixed), _p(fs), _p(fg), _p(moving), _p(ms), _p(mgeo), _p(mg), _p(pts),
+                           0 if pts is None else pts.shape[0], transform.kind, _p(tp), tp.size, _p(tf), tf.size,
+                           b, _threads(nthreads, pixel_double), int(compute_derivative), _p(value), _p(deriv),
+                           _p(nvalid), _p(pdf), _p(state))
+    return rc, float(value[0]), deriv, int(nvalid[0]), pdf, state
+
+
+def transform_points(transform, x):
+    L = lib()
+    x = np.ascontiguousarray(np.asarray(x, np.float64).reshape(-1, 3))
+    y = np.zeros_like(x)
+    tp = np.ascontiguousarray(transform.params, dtype=np.float64)
+    tf = np.ascontiguousarray(transform.fixed, dtype=np.float64)
+    rc = L.orc_transform_point_flat(transform.kind, _p(tp), tp.size, _p(tf), tf.size, _p(x), x.shape[0], _p(y))
+    if rc:
+        raise ValueError(f"oracle transform error {STATUS_NAMES.get(rc, rc)}")
+    return y
+
+
+def interpolate(img, geom, points):
+    L = lib()
+    img = _img(img)
+    pts = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1, 3))
+    vals = np.zeros(pts.shape[0], np.float64)
+    inside = np.zeros(pts.shape[0], np.int32)
+    rc = L.orc_interpolate_flat(_p(img), _p(geom.size_array()), _p(geom.flat()), _p(pts), pts.shape[0],
+                                _p(vals), _p(inside))
+    if rc:
+        raise ValueError(f"oracle interpolate error {STATUS_NAMES.get(rc, rc)}")
+    return vals, inside.astype(bool)
+
+
+def central_difference(img, geom, points):
+    L = lib()
+    img = _img(img)
+    pts = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1, 3))
+    g = np.zeros_like(pts)
+    rc = L.orc_central_difference_flat(_p(img), _p(geom.size_array()), _p(geom.flat()), _p(pts),
+                                       pts.shape[0], _p(g))
+    if rc:
+        raise ValueError(f"oracle central difference error {STATUS_NAMES.get(rc, rc)}")
+    return g
+
+
+def bspline_weights(cindex):
+    L = lib()
+    ci = np.ascontiguousarray(np.asarray(cindex, np.float64).reshape(3))
+    w = np.zeros(64, np.float64)
+    st = np.zeros(3, np.int64)
+    L.orc_bspline_weights(_p(ci), _p(w), _p(st))
+    return w, st
+
+
+def bspline3(u):
+    return lib().orc_bspline3(float(u))
+
+
+def bspline3_derivative(u):
+    return lib().orc_bspline3_derivative(float(u))
