@@ -126,9 +126,10 @@ __device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {
 
 // Trilinear gather of the packed (value, gx, gy, gz) moving image.
 __device__ __forceinline__ float4 gather4(const float4* __restrict__ img, const Stencil& s, int nx, int ny) {
-  const int64_t sy = nx, sz = (int64_t)nx * ny;
-  const int64_t r00 = s.z0 * sz + s.y0 * sy, r10 = s.z0 * sz + s.y1 * sy;
-  const int64_t r01 = s.z1 * sz + s.y0 * sy, r11 = s.z1 * sz + s.y1 * sy;
+  // 32-bit offsets: volumes are limited to 2^31 voxels at set-up
+  const unsigned sy = (unsigned)nx, sz = (unsigned)nx * (unsigned)ny;
+  const unsigned r00 = s.z0 * sz + s.y0 * sy, r10 = s.z0 * sz + s.y1 * sy;
+  const unsigned r01 = s.z1 * sz + s.y0 * sy, r11 = s.z1 * sz + s.y1 * sy;
   const float4 v000 = __ldg(img + r00 + s.x0), v100 = __ldg(img + r00 + s.x1);
   const float4 v010 = __ldg(img + r10 + s.x0), v110 = __ldg(img + r10 + s.x1);
   const float4 v001 = __ldg(img + r01 + s.x0), v101 = __ldg(img + r01 + s.x1);
@@ -141,9 +142,10 @@ __device__ __forceinline__ float4 gather4(const float4* __restrict__ img, const 
 
 // Trilinear gather of a scalar image.
 __device__ __forceinline__ float gather1(const float* __restrict__ img, const Stencil& s, int nx, int ny) {
-  const int64_t sy = nx, sz = (int64_t)nx * ny;
-  const int64_t r00 = s.z0 * sz + s.y0 * sy, r10 = s.z0 * sz + s.y1 * sy;
-  const int64_t r01 = s.z1 * sz + s.y0 * sy, r11 = s.z1 * sz + s.y1 * sy;
+  // 32-bit offsets: volumes are limited to 2^31 voxels at set-up
+  const unsigned sy = (unsigned)nx, sz = (unsigned)nx * (unsigned)ny;
+  const unsigned r00 = s.z0 * sz + s.y0 * sy, r10 = s.z0 * sz + s.y1 * sy;
+  const unsigned r01 = s.z1 * sz + s.y0 * sy, r11 = s.z1 * sz + s.y1 * sy;
   const float v000 = __ldg(img + r00 + s.x0), v100 = __ldg(img + r00 + s.x1);
   const float v010 = __ldg(img + r10 + s.x0), v110 = __ldg(img + r10 + s.x1);
   const float v001 = __ldg(img + r01 + s.x0), v101 = __ldg(img + r01 + s.x1);

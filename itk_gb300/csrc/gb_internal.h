@@ -103,6 +103,7 @@ struct gb_metric {
   gb::DevBuf<double> d_coeff_f;  // spare
   gb::DevBuf<unsigned char> d_acc;  // accumulators, cleared per evaluation
   size_t acc_bytes = 0;
+  gb::DevBuf<double> d_scratch;     // per-block / per-group partials, overwritten per evaluation
   gb::DevBuf<double> d_out;         // [value, nvalid, derivative...]
   gb::DevBuf<int> d_status;
   gb::DevBuf<float> d_pratio;       // bins*bins log(p/pm) table

@@ -26,6 +26,15 @@ enum { kGradImage = 0, kGradCentralDifference = 1 };
 enum { kXfAffine = 0, kXfBSpline = 1, kXfComposite = 2 };
 
 constexpr int kBlock = 256;
+constexpr int kMaxBlocks = 2048;          // grid cap of the evaluation kernels
+constexpr int kTicketMain = 0;            // grid_sums of the MeanSquares kernel: [0, 129]
+constexpr int kTicketFinalize = 160;      // last_block of the Mattes finalize
+constexpr int kTicketPass2 = 192;         // grid_sums of Mattes pass 2: [192, 321]
+constexpr int kTicketCount = 352;
+constexpr int kPartPass2 = 4096;          // offset of pass-2 partials (finalize rows use [0, bins))
+constexpr size_t kGroupOffset = kPartPass2 + (size_t)kMaxBlocks * 16;  // per-group partials: 128 groups x 16
+constexpr size_t kFinalOffset = kGroupOffset + 2048;
+constexpr size_t kScratchDoubles = kFinalOffset + 8;
 constexpr float kQScale = 67108864.f;  // 2^26 fixed-point scale for warp-aggregated histogram weights
 constexpr float kQInv = 1.f / 67108864.f;
 
@@ -56,12 +65,15 @@ struct EvalArgs {
   int bins;
   float mmin, mmax, m_inv_bs;
   double m_bs;
-  // accumulators / outputs
-  double* acc;                  // [value, derivative...]
+  // accumulators (cleared per evaluation)
   unsigned long long* acc_n;
-  unsigned* tickets;
-  double* hist;                 // bins*bins
+  unsigned* tickets;            // [kTicketCount]
+  unsigned long long* hist;     // bins*bins, 2^26 fixed point
   unsigned long long* fmarg;    // bins
+  // scratch (overwritten per evaluation)
+  double* part;                 // per-block partials
+  double* grp;                  // per-group partials
+  double* final_value;          // Mattes value handed from finalize to pass 2
   float4* cache;
   float* pratio;
   double* pdf_out;
@@ -152,38 +164,83 @@ __device__ __forceinline__ bool eval_moving(const EvalArgs& a, const CIdx& c, bo
 }
 
 // ---------------------------------------------------------------------------
-// block reduction: NV Kahan sums + a count, committed with FP64 atomics
+// deterministic reductions
+//
+// Within a block: per-thread Kahan FP32 sums, XOR-shuffle warp sums, then a
+// fixed-order FP64 sum over warps.  Across blocks: each block writes its FP64
+// partials; the last block of each group of 16 (atomic ticket) sums its group
+// in block order, and the last group sums the groups in group order.  The
+// result is bitwise reproducible for a given grid, so GetValue and
+// GetValueAndDerivative agree exactly.
+
+constexpr int kGroup = 16;
 
 template <int NV>
-__device__ __forceinline__ void block_commit(KahanF (&acc)[NV], unsigned nv, double* gacc, unsigned long long* gn,
-                                             double (*red)[NV + 1]) {
+__device__ __forceinline__ void block_sums(KahanF (&acc)[NV], double (*red)[NV], double* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float v[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = warp_sum(acc[k].value());
-  const unsigned n = warp_sum_u(nv);
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) red[warp][k] = (double)v[k];
-    red[warp][NV] = (double)n;
+  for (int k = 0; k < NV; ++k) {
+    const float v = warp_sum(acc[k].value());
+    if (lane == 0) red[warp][k] = (double)v;
   }
   __syncthreads();
   const int nwarps = blockDim.x >> 5;
-  if (threadIdx.x < NV) {
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) {
     double s = 0.0;
-    for (int w = 0; w < nwarps; ++w) s += red[w][threadIdx.x];
-    if (gacc) atomicAdd(&gacc[threadIdx.x], s);
-  } else if (threadIdx.x == NV && gn) {
+    for (int w = 0; w < nwarps; ++w) s += red[w][k];
+    out[k] = s;
+  }
+  __syncthreads();
+}
+
+// Returns true in exactly one block, which then holds the grid-wide sums in `fin`.
+template <int NV>
+__device__ __forceinline__ bool grid_sums(const double* blk, double* part, double* grp, unsigned* tick, double* fin) {
+  __shared__ unsigned t;
+  const int b = blockIdx.x, g = b / kGroup;
+  const int ng = (gridDim.x + kGroup - 1) / kGroup;
+  const int gsize = min(kGroup, (int)gridDim.x - g * kGroup);
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) part[b * NV + k] = blk[k];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) t = atomicAdd(&tick[g], 1u);
+  __syncthreads();
+  if (t != (unsigned)(gsize - 1)) return false;
+  __threadfence();
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) {
     double s = 0.0;
-    for (int w = 0; w < nwarps; ++w) s += red[w][NV];
-    atomicAdd(gn, (unsigned long long)s);
+    for (int j = g * kGroup; j < g * kGroup + gsize; ++j) s += __ldcg(&part[j * NV + k]);
+    grp[g * NV + k] = s;
   }
   __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) t = atomicAdd(&tick[ng], 1u);
+  __syncthreads();
+  if (t != (unsigned)(ng - 1)) return false;
+  __threadfence();
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < ng; ++j) s += __ldcg(&grp[j * NV + k]);
+    fin[k] = s;
+  }
+  __syncthreads();
+  return true;
+}
+
+__device__ __forceinline__ void block_count(unsigned nv, unsigned long long* gn) {
+  __shared__ unsigned sh;
+  if (threadIdx.x == 0) sh = 0u;
+  __syncthreads();
+  const unsigned w = warp_sum_u(nv);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(&sh, w);
+  __syncthreads();
+  if (threadIdx.x == 0 && sh) atomicAdd(gn, (unsigned long long)sh);
 }
 
 // true in exactly one block: the last to finish (threadFenceReduction pattern)
 __device__ __forceinline__ bool last_block(unsigned* ticket) {
   __shared__ bool is_last;
+  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
   __syncthreads();
@@ -197,7 +254,8 @@ __device__ __forceinline__ bool last_block(unsigned* ticket) {
 template <int GRAD>
 __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
   __shared__ AffConst K;
-  __shared__ double red[kBlock / 32][14];
+  __shared__ double red[kBlock / 32][13];
+  __shared__ double blk[13], fin[13];
   if (threadIdx.x == 0) affine_consts(a, K);
   __syncthreads();
   KahanF acc[13];
@@ -235,8 +293,9 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
       acc[10].add(t0); acc[11].add(t1); acc[12].add(t2);
     }
   }
-  block_commit<13>(acc, nv, a.acc, a.acc_n, red);
-  if (!last_block(a.tickets)) return;
+  block_count(nv, a.acc_n);
+  block_sums<13>(acc, red, blk);
+  if (!grid_sums<13>(blk, a.part, a.grp, a.tickets + kTicketMain, fin)) return;
   if (threadIdx.x == 0) {
     // AfterThreadedExecution + VerifyNumberOfValidPoints (ThreaderBase.hxx:116-172)
     const unsigned long long N = __ldcg(a.acc_n);
@@ -247,10 +306,9 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
       for (int p = 0; p < P; ++p) a.out[2 + p] = 0.0;
       *a.status = GB_ERR_NO_VALID_POINTS;
     } else {
-      const double inv = 1.0 / (double)N;
-      a.out[0] = __ldcg(&a.acc[0]) / (double)N;
+      a.out[0] = fin[0] / (double)N;
       a.out[1] = (double)N;
-      for (int p = 0; p < P; ++p) a.out[2 + p] = __ldcg(&a.acc[1 + p]) * inv;
+      for (int p = 0; p < P; ++p) a.out[2 + p] = fin[1 + p] / (double)N;
       *a.status = GB_OK;
     }
   }
@@ -259,6 +317,8 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
 // ---------------------------------------------------------------------------
 // Mattes pass 1, affine: joint histogram (Parzen: box on fixed, cubic B-spline
 // on moving), fixed marginal counts, valid count, per-sample cache.
+// Histogram weights are accumulated in 2^26 fixed point (integer adds are
+// associative, so the histogram does not depend on scheduling).
 
 __device__ __forceinline__ void parzen_weights(float term, int B, int& pdfm, float& arg, float w[4]) {
   int midx = (int)term;  // static_cast<OffsetValueType>, Mattes...Threader.hxx:249
@@ -272,10 +332,10 @@ __device__ __forceinline__ void parzen_weights(float term, int B, int& pdfm, flo
 }
 
 // Adds one sample's four Parzen weights into the block histogram.  Lanes with
-// the same (fixed bin, first moving bin) key are summed in 2^26 fixed point
-// with one redux per weight, and only the group leader issues the shared atomics.
-__device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, const float w[4], float* hist,
-                                                    unsigned* fm) {
+// the same (fixed bin, first moving bin) key are summed with one redux per
+// weight, and only the group leader issues the shared atomics.
+__device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, const float w[4],
+                                                    unsigned long long* hist, unsigned* fm) {
   const unsigned okmask = __ballot_sync(0xffffffffu, ok);
   if (!ok) return;
   const unsigned peers = __match_any_sync(okmask, key);
@@ -287,20 +347,19 @@ __device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, 
   if (lane == leader) {
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-      if (s[k]) atomicAdd(&hist[key + k], (float)s[k] * kQInv);
+      if (s[k]) atomicAdd(&hist[key + k], (unsigned long long)s[k]);
     atomicAdd(&fm[fidx], (unsigned)__popc(peers));
   }
 }
 
 template <int GRAD>
 __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
-  extern __shared__ float smem[];
+  extern __shared__ unsigned long long smem_u64[];
   const int B = a.bins;
-  float* hist = smem;
-  unsigned* fm = reinterpret_cast<unsigned*>(smem + B * B);
+  unsigned long long* hist = smem_u64;
+  unsigned* fm = reinterpret_cast<unsigned*>(smem_u64 + B * B);
   __shared__ AffConst K;
-  __shared__ double red[kBlock / 32][2];
-  for (int k = threadIdx.x; k < B * B; k += blockDim.x) hist[k] = 0.f;
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) hist[k] = 0ull;
   for (int k = threadIdx.x; k < B; k += blockDim.x) fm[k] = 0u;
   if (threadIdx.x == 0) affine_consts(a, K);
   __syncthreads();
@@ -340,21 +399,20 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
   }
   __syncthreads();
   for (int k = threadIdx.x; k < B * B; k += blockDim.x) {
-    const float h = hist[k];
-    if (h != 0.f) atomicAdd(&a.hist[k], (double)h);
+    const unsigned long long h = hist[k];
+    if (h) atomicAdd(&a.hist[k], h);
   }
   for (int k = threadIdx.x; k < B; k += blockDim.x) {
     const unsigned c = fm[k];
     if (c) atomicAdd(&a.fmarg[k], (unsigned long long)c);
   }
-  KahanF dummy[1];
-  dummy[0].zero();
-  block_commit<1>(dummy, nv, nullptr, a.acc_n, red);
+  block_count(nv, a.acc_n);
 }
 
 // Mattes finalize: one block per fixed bin.  FP64 normalization, marginals,
 // sum p (log(p/pm) - log pf), and the FP32 log(p/pm) table for pass 2
 // (ComputeResults, Mattes...v4.hxx:358-499; JointPDFSum .hxx:533-541).
+// Row partials of the sum are added in row order by the last block.
 __global__ void k_mattes_finalize(EvalArgs a) {
   extern __shared__ double colsum[];
   __shared__ double sh_total, sh_logpf;
@@ -362,9 +420,9 @@ __global__ void k_mattes_finalize(EvalArgs a) {
   const int B = a.bins;
   const int f = blockIdx.x;
   for (int m = threadIdx.x; m < B; m += blockDim.x) {
-    double s = 0.0;
+    unsigned long long s = 0ull;  // exact integer column sum
     for (int ff = 0; ff < B; ++ff) s += __ldcg(&a.hist[ff * B + m]);
-    colsum[m] = s;
+    colsum[m] = (double)s * (double)kQInv;
   }
   __syncthreads();
   const unsigned long long N = __ldcg(a.acc_n);
@@ -383,7 +441,7 @@ __global__ void k_mattes_finalize(EvalArgs a) {
     const double nf = 1.0 / total;
     const double pf = (double)__ldcg(&a.fmarg[f]) * nf;
     for (int m = threadIdx.x; m < B; m += blockDim.x) {
-      const double p = __ldcg(&a.hist[f * B + m]) * nf;
+      const double p = (double)__ldcg(&a.hist[f * B + m]) * (double)kQInv * nf;
       const double pm = colsum[m] * nf;
       a.pdf_out[f * B + m] = p;
       float pr = 0.f;
@@ -406,15 +464,18 @@ __global__ void k_mattes_finalize(EvalArgs a) {
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
-    if (s != 0.0) atomicAdd(&a.acc[0], s);
-    __threadfence();
+    a.part[f] = s;
   }
-  if (!last_block(a.tickets + 1)) return;
+  if (!last_block(a.tickets + kTicketFinalize)) return;
   if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int r = 0; r < B; ++r) s += __ldcg(&a.part[r]);
     const int st = N == 0 ? GB_ERR_NO_VALID_POINTS : (bad ? GB_ERR_JOINT_PDF_SUM_ZERO : GB_OK);
     *a.status = st;
+    const double value = st == GB_OK ? -1.0 * s : 0.0;  // metrics minimize: value = -MI
+    a.final_value[0] = value;
     if (!a.with_derivative) {
-      a.out[0] = st == GB_OK ? -1.0 * __ldcg(&a.acc[0]) : 0.0;  // metrics minimize: value = -MI
+      a.out[0] = value;
       a.out[1] = (double)N;
     }
   }
@@ -424,7 +485,8 @@ __global__ void k_mattes_finalize(EvalArgs a) {
 __global__ void __launch_bounds__(kBlock) k_mattes_pass2_affine(EvalArgs a) {
   extern __shared__ float pr[];
   __shared__ float c[3];
-  __shared__ double red[kBlock / 32][13];
+  __shared__ double red[kBlock / 32][12];
+  __shared__ double blk[12], fin[12];
   const int B = a.bins;
   for (int k = threadIdx.x; k < B * B; k += blockDim.x) pr[k] = __ldcg(&a.pratio[k]);
   if (threadIdx.x < 3) c[threadIdx.x] = (float)a.center[threadIdx.x];
@@ -437,12 +499,10 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass2_affine(EvalArgs a) {
     const float4 cc = __ldcs(a.cache + i);
     if (cc.x != cc.x) continue;  // rejected sample
     const float4 s = __ldcs(a.samples + i);
-    int pdfm;
-    float arg;
     int midx = (int)cc.x;
     midx = midx < 2 ? 2 : (midx > B - 3 ? B - 3 : midx);
-    pdfm = midx - 1;
-    arg = (float)pdfm - cc.x;
+    const int pdfm = midx - 1;
+    const float arg = (float)pdfm - cc.x;
     const float* row = pr + __float_as_int(s.w) * B + pdfm;
     const float w = row[0] * bspline3_deriv(arg) + row[1] * bspline3_deriv(arg + 1.f) +
                     row[2] * bspline3_deriv(arg + 2.f) + row[3] * bspline3_deriv(arg + 3.f);
@@ -453,8 +513,8 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass2_affine(EvalArgs a) {
     acc[6].add(t2 * vx); acc[7].add(t2 * vy); acc[8].add(t2 * vz);
     acc[9].add(t0); acc[10].add(t1); acc[11].add(t2);
   }
-  block_commit<12>(acc, 0u, a.acc + 1, nullptr, red);
-  if (!last_block(a.tickets + 2)) return;
+  block_sums<12>(acc, red, blk);
+  if (!grid_sums<12>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin)) return;
   if (threadIdx.x == 0) {
     const unsigned long long N = __ldcg(a.acc_n);
     const int st = __ldcg(a.status);
@@ -466,8 +526,8 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass2_affine(EvalArgs a) {
     }
     // nFactor = -1 / (MovingImageBinSize * N), Mattes...Threader.hxx:446-457
     const double nFactor = -1.0 / (a.m_bs * (double)N);
-    a.out[0] = -1.0 * __ldcg(&a.acc[0]);
-    for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = __ldcg(&a.acc[1 + p]) * nFactor;
+    a.out[0] = __ldcg(a.final_value);
+    for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = fin[p] * nFactor;
   }
 }
 

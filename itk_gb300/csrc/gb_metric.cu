@@ -99,7 +99,7 @@ static DGeom to_dgeom(const Geom& g) {
 
 static int grid_for(const gb_metric* m, int64_t n, int per_sm) {
   const int64_t want = (n + kBlock - 1) / kBlock;
-  const int64_t cap = (int64_t)m->ctx->sm_count * per_sm;
+  const int64_t cap = std::min<int64_t>((int64_t)m->ctx->sm_count * per_sm, kMaxBlocks);
   return (int)std::max<int64_t>(1, std::min(want, cap));
 }
 
@@ -196,6 +196,7 @@ static int set_image_common(gb_metric* m, int which, const float* src, bool devi
   Geom g;
   int rc = geom_init(g, size, spacing, origin, direction);
   if (rc) return rc;
+  if (g.voxels() > ((int64_t)1 << 31)) return fail(GB_ERR_UNSUPPORTED, "images above 2^31 voxels are not supported");
   DevBuf<float>& buf = which == GB_IMAGE_FIXED ? m->d_fixed : m->d_moving;
   const size_t n = (size_t)g.voxels();
   buf.reset();
@@ -338,11 +339,14 @@ extern "C" int gb_metric_get_number_of_parameters(gb_metric* m, int64_t* nparams
 // ===========================================================================
 // Initialize
 
+// Accumulators cleared before every evaluation:
+// acc_n u64 | tickets kTicketCount u32 | hist B*B u64 | fmarg B u64
+static size_t acc_offset_tickets() { return 8; }
+static size_t acc_offset_hist() { return 8 + (sizeof(unsigned) * kTicketCount + 7) / 8 * 8; }
+static size_t acc_offset_fmarg(int64_t B) { return acc_offset_hist() + 8 * (size_t)(B * B); }
 static size_t acc_layout_bytes(const gb_metric* m) {
-  const size_t P = m->tparams.size();
-  const size_t B = (size_t)m->bins;
-  // [value, deriv P] doubles | acc_n u64 | tickets 4 u32 | hist B*B doubles | fmarg B u64
-  return sizeof(double) * (1 + P) + 8 + 16 + sizeof(double) * B * B + 8 * B;
+  const int64_t B = m->kind == GB_METRIC_MATTES ? m->bins : 0;
+  return acc_offset_fmarg(B) + 8 * (size_t)B;
 }
 
 extern "C" int gb_metric_initialize(gb_metric* m) {
@@ -481,6 +485,7 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   m->acc_bytes = acc_layout_bytes(m);
   m->d_acc.reset();
   GB_CUDA(m->d_acc.alloc(m->acc_bytes));
+  GB_CUDA(m->d_scratch.alloc(kScratchDoubles));
   GB_CUDA(m->d_params.alloc(P));
   m->d_out.reset();
   GB_CUDA(m->d_out.alloc(2 + P));
@@ -535,13 +540,13 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.m_bs = m->mstate[5];
   a.m_inv_bs = (float)(1.0 / m->mstate[5]);
   unsigned char* base = m->d_acc.p;
-  const size_t P = m->tparams.size();
-  a.acc = reinterpret_cast<double*>(base);
-  a.acc_n = reinterpret_cast<unsigned long long*>(base + sizeof(double) * (1 + P));
-  a.tickets = reinterpret_cast<unsigned*>(base + sizeof(double) * (1 + P) + 8);
-  a.hist = reinterpret_cast<double*>(base + sizeof(double) * (1 + P) + 8 + 16);
-  a.fmarg = reinterpret_cast<unsigned long long*>(base + sizeof(double) * (1 + P) + 8 + 16 +
-                                                  sizeof(double) * m->bins * m->bins);
+  a.acc_n = reinterpret_cast<unsigned long long*>(base);
+  a.tickets = reinterpret_cast<unsigned*>(base + acc_offset_tickets());
+  a.hist = reinterpret_cast<unsigned long long*>(base + acc_offset_hist());
+  a.fmarg = reinterpret_cast<unsigned long long*>(base + acc_offset_fmarg(m->bins));
+  a.part = m->d_scratch.p;
+  a.grp = m->d_scratch.p + kGroupOffset;
+  a.final_value = m->d_scratch.p + kFinalOffset;
   a.cache = m->d_cache.p;
   a.pratio = m->d_pratio.p;
   a.pdf_out = m->d_pdf.p;
@@ -578,10 +583,10 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   }
   // Mattes: pass 1, finalize, pass 2
   const int B = (int)m->bins;
-  const size_t sh1 = sizeof(float) * B * B + sizeof(unsigned) * B;
+  const size_t sh1 = sizeof(unsigned long long) * B * B + sizeof(unsigned) * B;
   const size_t sh2 = sizeof(float) * B * B;
-  if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > ~220)");
-  const int grid = grid_for(m, m->nsamples, 2);
+  if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
+  const int grid = grid_for(m, m->nsamples, 4);
   if (cd) {
     cudaFuncSetAttribute(k_mattes_pass1_affine<kGradCentralDifference>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sh1);
