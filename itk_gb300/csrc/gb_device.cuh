@@ -1,12 +1,13 @@
 // gb_device.cuh -- device-side building blocks of the registration-metric kernels.
 //
-// Per-point arithmetic is FP32.  Positions are carried as an exact integer
-// voxel index plus an FP32 fraction: each warp anchors its 32 (spatially
-// sorted) samples on one of them, maps the anchor to moving-image index space
-// in FP64 once, and maps every other sample by its small offset from the
-// anchor in FP32.  The fraction inside the voxel is then accurate to ~1e-6
-// voxel instead of the ~2e-5 that a plain FP32 transform of a 256 mm
-// coordinate gives.
+// GB300 issues FP64 at a small fraction of its FP32 rate, so nothing in the
+// per-sample loops is FP64.  Positions are mapped in double-float arithmetic:
+// the per-evaluation affine map (virtual point -> moving continuous index) is
+// computed once in FP64 and split into FP32 hi/lo pairs; each sample's
+// (exactly representable, float) coordinates are multiplied with error-free
+// FMA products and summed with two-sum, giving the continuous index to ~1e-12
+// voxel, i.e. the reference's double arithmetic for every practical input,
+// including points that fall exactly on a buffer edge.
 #pragma once
 
 #include <cstdint>
@@ -23,9 +24,9 @@ struct KahanF {
   float s, c;
   __device__ __forceinline__ void zero() { s = 0.f; c = 0.f; }
   __device__ __forceinline__ void add(float x) {
-    const float y = x - c;
-    const float t = s + y;
-    c = __fsub_rn(__fsub_rn(t, s), y);  // _rn intrinsics keep nvcc from contracting this away
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);  // _rn intrinsics are never contracted or reassociated
     s = t;
   }
   __device__ __forceinline__ float value() const { return s - c; }
@@ -43,52 +44,53 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-__device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
-  return __reduce_add_sync(0xffffffffu, v);
+__device__ __forceinline__ unsigned warp_sum_u(unsigned v) { return __reduce_add_sync(0xffffffffu, v); }
+
+// ---------------------------------------------------------------------------
+// Cubic B-spline Parzen window (order 3).  With the window starting at bin
+// pdfm = midx - 1 and t = term - midx in [0, 1], the four arguments are
+// -1-t, -t, 1-t, 2-t; BSplineKernelFunction<3> (Core/Common/include/itkBSplineKernelFunction.h:152-169)
+// and BSplineDerivativeKernelFunction<3> (itkBSplineDerivativeKernelFunction.h:156-180)
+// evaluated there are the uniform cubic B-spline basis polynomials below.
+
+// 6 * beta3(arg_k), k = 0..3 (integer coefficients: no rounding of 1/6)
+__device__ __forceinline__ void parzen6(float t, float w6[4]) {
+  const float u = 1.f - t;
+  const float t2 = t * t, t3 = t2 * t;
+  w6[0] = u * u * u;
+  w6[1] = fmaf(3.f, t3, fmaf(-6.f, t2, 4.f));
+  w6[2] = fmaf(-3.f, t3, fmaf(3.f, t2, fmaf(3.f, t, 1.f)));
+  w6[3] = t3;
+}
+
+// beta3'(arg_k), k = 0..3
+__device__ __forceinline__ void parzen_deriv(float t, float d[4]) {
+  const float u = 1.f - t;
+  d[0] = 0.5f * u * u;
+  d[1] = t * fmaf(-1.5f, t, 2.f);
+  d[2] = u * fmaf(1.5f, u, -2.f);
+  d[3] = -0.5f * t * t;
 }
 
 // ---------------------------------------------------------------------------
-// Cubic B-spline Parzen kernels (order 3), as polynomials of |u|:
-// BSplineKernelFunction<3>, Core/Common/include/itkBSplineKernelFunction.h:152-169
-// BSplineDerivativeKernelFunction<3>, Core/Common/include/itkBSplineDerivativeKernelFunction.h:156-180
-__device__ __forceinline__ float bspline3(float u) {
-  const float a = fabsf(u);
-  if (a < 1.f) {
-    const float s = a * a;
-    return (4.f - 6.f * s + 3.f * s * a) * (1.f / 6.f);
-  }
-  if (a < 2.f) {
-    const float s = a * a;
-    return (8.f - 12.f * a + 6.f * s - s * a) * (1.f / 6.f);
-  }
-  return 0.f;
-}
-
-__device__ __forceinline__ float bspline3_deriv(float u) {
-  if (u >= 0.f && u < 1.f) return -2.f * u + 1.5f * u * u;
-  if (u > -1.f && u < 0.f) return -2.f * u - 1.5f * u * u;
-  if (u >= 1.f && u < 2.f) return -2.f + 2.f * u - 0.5f * u * u;
-  if (u > -2.f && u <= -1.f) return 2.f + 2.f * u + 0.5f * u * u;
-  return 0.f;
-}
-
-// ---------------------------------------------------------------------------
-// A continuous index as integer base + fraction in [0, 1).
+// A continuous index as integer base + fraction in [0, 1].
 struct CIdx {
   int b[3];
   float f[3];
 };
 
-// Buffer test of LinearInterpolateImageFunction / ImageFunction::IsInsideBuffer:
-// cindex in [-0.5, n - 0.5) per axis (Core/ImageFunction/include/itkImageFunction.h:157-169).
+// ImageFunction::IsInsideBuffer: cindex in [-0.5, n - 0.5) per axis, NaN outside
+// (Core/ImageFunction/include/itkImageFunction.h:157-169).
 __device__ __forceinline__ bool ci_inside(const CIdx& c, int nx, int ny, int nz) {
   const int n[3] = {nx, ny, nz};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int b = c.b[k];
+    const float f = c.f[k];
+    if (!(f >= 0.f)) return false;  // NaN position
     if (b >= 0 && b <= n[k] - 2) continue;
-    if (b == -1) { if (!(c.f[k] >= 0.5f)) return false; continue; }
-    if (b == n[k] - 1) { if (!(c.f[k] < 0.5f)) return false; continue; }
+    if (b == -1) { if (!(f >= 0.5f)) return false; continue; }
+    if (b == n[k] - 1) { if (!(f < 0.5f)) return false; continue; }
     return false;
   }
   return true;
@@ -102,19 +104,18 @@ struct Stencil {
   float dx, dy, dz;
 };
 
+__device__ __forceinline__ void stencil_axis(int b, float d, int n, int& i0, int& i1, float& w) {
+  if (b < 0) { b = 0; d = 0.f; }
+  i0 = b;
+  i1 = (b + 1 <= n - 1 && d > 0.f) ? b + 1 : b;
+  w = d > 0.f ? d : 0.f;
+}
+
 __device__ __forceinline__ Stencil make_stencil(const CIdx& c, int nx, int ny, int nz) {
   Stencil s;
-  int b;
-  float d;
-  b = c.b[0]; d = c.f[0];
-  if (b < 0) { b = 0; d = 0.f; }
-  s.x0 = b; s.x1 = (b + 1 <= nx - 1 && d > 0.f) ? b + 1 : b; s.dx = d > 0.f ? d : 0.f;
-  b = c.b[1]; d = c.f[1];
-  if (b < 0) { b = 0; d = 0.f; }
-  s.y0 = b; s.y1 = (b + 1 <= ny - 1 && d > 0.f) ? b + 1 : b; s.dy = d > 0.f ? d : 0.f;
-  b = c.b[2]; d = c.f[2];
-  if (b < 0) { b = 0; d = 0.f; }
-  s.z0 = b; s.z1 = (b + 1 <= nz - 1 && d > 0.f) ? b + 1 : b; s.dz = d > 0.f ? d : 0.f;
+  stencil_axis(c.b[0], c.f[0], nx, s.x0, s.x1, s.dx);
+  stencil_axis(c.b[1], c.f[1], ny, s.y0, s.y1, s.dy);
+  stencil_axis(c.b[2], c.f[2], nz, s.z0, s.z1, s.dz);
   return s;
 }
 
@@ -142,7 +143,6 @@ __device__ __forceinline__ float4 gather4(const float4* __restrict__ img, const 
 
 // Trilinear gather of a scalar image.
 __device__ __forceinline__ float gather1(const float* __restrict__ img, const Stencil& s, int nx, int ny) {
-  // 32-bit offsets: volumes are limited to 2^31 voxels at set-up
   const unsigned sy = (unsigned)nx, sz = (unsigned)nx * (unsigned)ny;
   const unsigned r00 = s.z0 * sz + s.y0 * sy, r10 = s.z0 * sz + s.y1 * sy;
   const unsigned r01 = s.z1 * sz + s.y0 * sy, r11 = s.z1 * sz + s.y1 * sy;
@@ -163,50 +163,49 @@ __device__ __forceinline__ void split_add(int base, float t, int& b, float& f) {
   f = t - fl;
 }
 
-// Warp anchor: integer + fractional moving-index position of the anchor sample.
-struct Anchor {
-  float ax, ay, az;   // anchor position (virtual space, float)
-  int ib[3];          // floor of the anchor's moving continuous index
-  float fb[3];        // fraction of the anchor's moving continuous index
+// ---------------------------------------------------------------------------
+// double-float helpers
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Affine map virtual point -> moving continuous index, as FP32 hi/lo pairs:
+// cidx_k = sum_j (Ahi + Alo)[k][j] x_j + (bhi + blo)[k].
+struct AffineDF {
+  float Ahi[9], Alo[9], bhi[3], blo[3];
 };
 
-// Moving continuous index of a sample at (x, y, z) from the warp anchor:
-// cidx = A (p - a) + cidx(a), A the 3x3 map virtual point -> moving index.
-__device__ __forceinline__ CIdx map_from_anchor(const Anchor& an, const float* A, float x, float y, float z) {
-  const float d0 = x - an.ax, d1 = y - an.ay, d2 = z - an.az;
+// cidx of one float point, to ~1e-12 voxel; floor and fraction of the pair.
+__device__ __forceinline__ CIdx map_df(const AffineDF& K, float x, float y, float z) {
+  const float xs[3] = {x, y, z};
   CIdx c;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float t = fmaf(A[3 * k + 0], d0, fmaf(A[3 * k + 1], d1, fmaf(A[3 * k + 2], d2, an.fb[k])));
-    split_add(an.ib[k], t, c.b[k], c.f[k]);
+    float s = K.bhi[k], err = K.blo[k];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float a = K.Ahi[3 * k + j];
+      const float p = __fmul_rn(a, xs[j]);
+      const float pe = __fmaf_rn(a, xs[j], -p);  // exact product error
+      float t, e;
+      two_sum(s, p, t, e);
+      s = t;
+      err = __fadd_rn(err, __fadd_rn(e, __fmaf_rn(K.Alo[3 * k + j], xs[j], pe)));
+    }
+    const float hi = __fadd_rn(s, err);
+    const float lo = __fsub_rn(err, __fsub_rn(hi, s));
+    float fl = floorf(hi);
+    if (hi == fl && lo < 0.f) fl -= 1.f;
+    c.b[k] = (int)fl;  // saturates for huge values: outside the buffer
+    c.f[k] = __fadd_rn(__fsub_rn(hi, fl), lo);
   }
   return c;
 }
 
-// Anchor from a moving-index position given in FP64.
-__device__ __forceinline__ void anchor_set(Anchor& an, float ax, float ay, float az, const double ci[3]) {
-  an.ax = ax; an.ay = ay; an.az = az;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const double fl = floor(ci[k]);
-    an.ib[k] = (int)fl;
-    an.fb[k] = (float)(ci[k] - fl);
-  }
-}
-
-__device__ __forceinline__ Anchor anchor_bcast(const Anchor& a, int src) {
-  Anchor r;
-  r.ax = __shfl_sync(0xffffffffu, a.ax, src);
-  r.ay = __shfl_sync(0xffffffffu, a.ay, src);
-  r.az = __shfl_sync(0xffffffffu, a.az, src);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    r.ib[k] = __shfl_sync(0xffffffffu, a.ib[k], src);
-    r.fb[k] = __shfl_sync(0xffffffffu, a.fb[k], src);
-  }
-  return r;
-}
-
+// ---------------------------------------------------------------------------
 // Ordered-int encodings of floats for atomic min/max.
 __device__ __forceinline__ int float_to_ordered(float f) {
   int i = __float_as_int(f);
@@ -216,7 +215,7 @@ __device__ __forceinline__ float ordered_to_float(int i) {
   return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff);
 }
 
-// 10-bit-per-axis Morton interleave (x fastest bit).
+// 21-bit-per-axis Morton interleave (x fastest bit).
 __device__ __forceinline__ uint64_t morton_spread(uint64_t v) {
   v &= 0x1fffff;
   v = (v | v << 32) & 0x1f00000000ffffULL;

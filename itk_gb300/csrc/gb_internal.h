@@ -11,6 +11,8 @@
 
 namespace gb {
 
+struct EvalConsts;  // per-evaluation transform constants (gb_kernels.cuh)
+
 // Image geometry (start index 0, x fastest), as ImageBase holds it.
 struct Geom {
   int64_t size[3] = {0, 0, 0};
@@ -108,6 +110,8 @@ struct gb_metric {
   gb::DevBuf<int> d_status;
   gb::DevBuf<float> d_pratio;       // bins*bins log(p/pm) table
   gb::DevBuf<double> d_pdf;         // normalized joint PDF of the last evaluation
+  gb::DevBuf<gb::EvalConsts> d_consts;  // per-evaluation transform constants
+  gb::EvalConsts* h_consts = nullptr;   // pinned staging of the constants
   double* h_params = nullptr;       // pinned staging
   double* h_out = nullptr;          // pinned staging, 2 + P doubles
   int* h_status = nullptr;

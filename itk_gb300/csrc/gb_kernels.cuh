@@ -18,25 +18,62 @@
 
 #include <cfloat>
 
+#include "../../include/itk_gb300.h"
 #include "gb_device.cuh"
 
 namespace gb {
 
 enum { kGradImage = 0, kGradCentralDifference = 1 };
-enum { kXfAffine = 0, kXfBSpline = 1, kXfComposite = 2 };
 
 constexpr int kBlock = 256;
 constexpr int kMaxBlocks = 2048;          // grid cap of the evaluation kernels
-constexpr int kTicketMain = 0;            // grid_sums of the MeanSquares kernel: [0, 129]
+constexpr int kTicketMain = 0;            // grid_sums of the MeanSquares kernel: [0, 128]
 constexpr int kTicketFinalize = 160;      // last_block of the Mattes finalize
-constexpr int kTicketPass2 = 192;         // grid_sums of Mattes pass 2: [192, 321]
+constexpr int kTicketPass2 = 192;         // grid_sums of Mattes pass 2: [192, 320]
 constexpr int kTicketCount = 352;
-constexpr int kPartPass2 = 4096;          // offset of pass-2 partials (finalize rows use [0, bins))
+constexpr int kPartPass2 = 4096;          // offset of pass-2 partials (finalize blocks use [0, 4096))
 constexpr size_t kGroupOffset = kPartPass2 + (size_t)kMaxBlocks * 16;  // per-group partials: 128 groups x 16
 constexpr size_t kFinalOffset = kGroupOffset + 2048;
 constexpr size_t kScratchDoubles = kFinalOffset + 8;
-constexpr float kQScale = 67108864.f;  // 2^26 fixed-point scale for warp-aggregated histogram weights
-constexpr float kQInv = 1.f / 67108864.f;
+constexpr int kFinalizeThreads = 32;
+constexpr float kQScale = 67108864.f;  // 2^26 fixed point of histogram weights
+constexpr double kQInv = 1.0 / 67108864.0;
+
+// Per-evaluation transform constants (computed in FP64 once per evaluation,
+// stored as FP32 / double-float).
+struct EvalConsts {
+  AffineDF map;  // virtual point -> moving continuous index
+  float c[3];    // affine centre (Jacobian)
+};
+
+// MatrixOffsetTransformBase::ComputeOffset (itkMatrixOffsetTransformBase.hxx:612-631)
+// composed with ImageBase::TransformPhysicalPointToContinuousIndex (itkImageBase.h:515-531).
+__host__ __device__ inline void split_df(double x, float& hi, float& lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+
+__host__ __device__ inline void affine_consts(const double* p, const double center[3], const double m_p2i[9],
+                                              const double m_origin[3], EvalConsts& K) {
+  double M[9], off[3];
+  for (int i = 0; i < 9; ++i) M[i] = p[i];
+  for (int i = 0; i < 3; ++i) {
+    double o = p[9 + i] + center[i];
+    for (int j = 0; j < 3; ++j) o -= M[i * 3 + j] * center[j];
+    off[i] = o;
+  }
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += m_p2i[r * 3 + k] * M[k * 3 + c];
+      split_df(s, K.map.Ahi[r * 3 + c], K.map.Alo[r * 3 + c]);
+    }
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) s += m_p2i[r * 3 + k] * (off[k] - m_origin[k]);
+    split_df(s, K.map.bhi[r], K.map.blo[r]);
+  }
+  for (int i = 0; i < 3; ++i) K.c[i] = (float)center[i];
+}
 
 struct EvalArgs {
   const float4* __restrict__ samples;
@@ -47,20 +84,12 @@ struct EvalArgs {
   double m_p2i[9];
   double m_origin[3];
   float cd_off[9];        // [3*d + k]: index-space offset along k of +0.5 spacing on physical axis d
-  float cd_inv_delta[3];  // 1 / (spacing[d])
+  float cd_inv_delta[3];  // 1 / spacing[d]
   // transform
-  const double* params;
+  const double* params;   // device parameters (device-resident path: k_prepare reads them)
+  const EvalConsts* consts;
   int nparams;
-  double center[3];  // affine centre
-  // B-spline / composite
-  const int4* __restrict__ bsp;    // per-sample support start (x, y, z), valid flag
-  const float4* __restrict__ bspf; // per-sample fractions inside the support cell
-  int gx, gy, gz;
-  int64_t nper;
-  double init_M[9];       // initial affine of a composite transform
-  double init_offset[3];
-  const int64_t* __restrict__ cell_chunks;
-  int64_t ncell_chunks;
+  double center[3];       // affine centre
   // Mattes
   int bins;
   float mmin, mmax, m_inv_bs;
@@ -70,6 +99,7 @@ struct EvalArgs {
   unsigned* tickets;            // [kTicketCount]
   unsigned long long* hist;     // bins*bins, 2^26 fixed point
   unsigned long long* fmarg;    // bins
+  unsigned long long* colsum;   // bins: moving marginal, 2^26 fixed point
   // scratch (overwritten per evaluation)
   double* part;                 // per-block partials
   double* grp;                  // per-group partials
@@ -82,45 +112,15 @@ struct EvalArgs {
   int with_derivative;
 };
 
-// ---------------------------------------------------------------------------
-// transform constants, computed once per block from the device parameters
-
-struct AffConst {
-  double Ad[9];  // virtual point -> moving continuous index: cidx = Ad x + bd
-  double bd[3];
-  float A[9];
-  float c[3];    // affine centre (Jacobian)
-};
-
-// MatrixOffsetTransformBase::ComputeOffset (itkMatrixOffsetTransformBase.hxx:612-631)
-// composed with ImageBase::TransformPhysicalPointToContinuousIndex (itkImageBase.h:515-531).
-__device__ __forceinline__ void affine_consts(const EvalArgs& a, AffConst& K) {
-  const double* p = a.params;
-  double M[9], off[3];
-  for (int i = 0; i < 9; ++i) M[i] = p[i];
-  for (int i = 0; i < 3; ++i) {
-    double o = p[9 + i] + a.center[i];
-    for (int j = 0; j < 3; ++j) o -= M[i * 3 + j] * a.center[j];
-    off[i] = o;
-  }
-  for (int r = 0; r < 3; ++r) {
-    for (int c = 0; c < 3; ++c) {
-      double s = 0.0;
-      for (int k = 0; k < 3; ++k) s += a.m_p2i[r * 3 + k] * M[k * 3 + c];
-      K.Ad[r * 3 + c] = s;
-      K.A[r * 3 + c] = (float)s;
-    }
-    double s = 0.0;
-    for (int k = 0; k < 3; ++k) s += a.m_p2i[r * 3 + k] * (off[k] - a.m_origin[k]);
-    K.bd[r] = s;
-  }
-  for (int i = 0; i < 3; ++i) K.c[i] = (float)a.center[i];
+// Device twin of the host constant computation (parameters already in HBM).
+__global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) affine_consts(a.params, a.center, a.m_p2i, a.m_origin, *out);
 }
 
-__device__ __forceinline__ void affine_map_d(const AffConst& K, float x, float y, float z, double ci[3]) {
-  const double X = x, Y = y, Z = z;
-#pragma unroll
-  for (int r = 0; r < 3; ++r) ci[r] = K.Ad[3 * r] * X + K.Ad[3 * r + 1] * Y + K.Ad[3 * r + 2] * Z + K.bd[r];
+__device__ __forceinline__ void load_consts(const EvalConsts* g, EvalConsts& s) {
+  const float* src = reinterpret_cast<const float*>(g);
+  float* dst = reinterpret_cast<float*>(&s);
+  for (int k = threadIdx.x; k < (int)(sizeof(EvalConsts) / 4); k += blockDim.x) dst[k] = __ldg(src + k);
 }
 
 // ---------------------------------------------------------------------------
@@ -253,32 +253,21 @@ __device__ __forceinline__ bool last_block(unsigned* ticket) {
 
 template <int GRAD>
 __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
-  __shared__ AffConst K;
+  __shared__ EvalConsts K;
   __shared__ double red[kBlock / 32][13];
   __shared__ double blk[13], fin[13];
-  if (threadIdx.x == 0) affine_consts(a, K);
+  load_consts(a.consts, K);
   __syncthreads();
   KahanF acc[13];
 #pragma unroll
   for (int k = 0; k < 13; ++k) acc[k].zero();
   unsigned nv = 0;
-  const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < a.n; base += stride) {
-    const int64_t i = base + lane;
-    const bool live = i < a.n;
-    const float4 s = live ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-    Anchor an;
-    if (lane == 0) {
-      double ci[3];
-      affine_map_d(K, s.x, s.y, s.z, ci);
-      anchor_set(an, s.x, s.y, s.z, ci);
-    }
-    an = anchor_bcast(an, 0);
-    if (!live) continue;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 s = __ldcs(a.samples + i);
     float m;
     float3 g;
-    const CIdx c = map_from_anchor(an, K.A, s.x, s.y, s.z);
+    const CIdx c = map_df(K.map, s.x, s.y, s.z);
     if (!eval_moving<GRAD>(a, c, a.with_derivative != 0, m, g)) continue;
     const float diff = s.w - m;  // FixedImagePixelType diff, MeanSquares...Threader.hxx:46
     acc[0].add(diff * diff);
@@ -316,25 +305,23 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
 
 // ---------------------------------------------------------------------------
 // Mattes pass 1, affine: joint histogram (Parzen: box on fixed, cubic B-spline
-// on moving), fixed marginal counts, valid count, per-sample cache.
-// Histogram weights are accumulated in 2^26 fixed point (integer adds are
-// associative, so the histogram does not depend on scheduling).
+// on moving), fixed marginal counts, moving marginal, valid count, per-sample
+// cache.  Histogram weights are 2^26 fixed point: integer adds are
+// associative, so the histogram does not depend on scheduling.
 
-__device__ __forceinline__ void parzen_weights(float term, int B, int& pdfm, float& arg, float w[4]) {
-  int midx = (int)term;  // static_cast<OffsetValueType>, Mattes...Threader.hxx:249
+// Moving Parzen window of one sample: first bin and the position t in [0, 1]
+// (Mattes...Threader.hxx:248-264).
+__device__ __forceinline__ void parzen_window(float term, int B, int& pdfm, float& t) {
+  int midx = (int)term;  // static_cast<OffsetValueType>
   midx = midx < 2 ? 2 : (midx > B - 3 ? B - 3 : midx);
   pdfm = midx - 1;
-  arg = (float)pdfm - term;
-  w[0] = bspline3(arg);
-  w[1] = bspline3(arg + 1.f);
-  w[2] = bspline3(arg + 2.f);
-  w[3] = bspline3(arg + 3.f);
+  t = term - (float)midx;
 }
 
 // Adds one sample's four Parzen weights into the block histogram.  Lanes with
 // the same (fixed bin, first moving bin) key are summed with one redux per
 // weight, and only the group leader issues the shared atomics.
-__device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, const float w[4],
+__device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, const unsigned q[4],
                                                     unsigned long long* hist, unsigned* fm) {
   const unsigned okmask = __ballot_sync(0xffffffffu, ok);
   if (!ok) return;
@@ -343,7 +330,7 @@ __device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, 
   const int lane = threadIdx.x & 31;
   unsigned s[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) s[k] = __reduce_add_sync(peers, __float2uint_rn(w[k] * kQScale));
+  for (int k = 0; k < 4; ++k) s[k] = __reduce_add_sync(peers, q[k]);
   if (lane == leader) {
 #pragma unroll
     for (int k = 0; k < 4; ++k)
@@ -358,10 +345,10 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
   const int B = a.bins;
   unsigned long long* hist = smem_u64;
   unsigned* fm = reinterpret_cast<unsigned*>(smem_u64 + B * B);
-  __shared__ AffConst K;
+  __shared__ EvalConsts K;
   for (int k = threadIdx.x; k < B * B; k += blockDim.x) hist[k] = 0ull;
   for (int k = threadIdx.x; k < B; k += blockDim.x) fm[k] = 0u;
-  if (threadIdx.x == 0) affine_consts(a, K);
+  load_consts(a.consts, K);
   __syncthreads();
   unsigned nv = 0;
   const int lane = threadIdx.x & 31;
@@ -370,18 +357,11 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
     const int64_t i = base + lane;
     const bool live = i < a.n;
     const float4 s = live ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-    Anchor an;
-    if (lane == 0) {
-      double ci[3];
-      affine_map_d(K, s.x, s.y, s.z, ci);
-      anchor_set(an, s.x, s.y, s.z, ci);
-    }
-    an = anchor_bcast(an, 0);
     float m = 0.f;
     float3 g = make_float3(0.f, 0.f, 0.f);
     bool ok = false;
     if (live) {
-      const CIdx c = map_from_anchor(an, K.A, s.x, s.y, s.z);
+      const CIdx c = map_df(K.map, s.x, s.y, s.z);
       ok = eval_moving<GRAD>(a, c, a.with_derivative != 0, m, g);
       // reject moving values outside [MovingImageTrueMin, MovingImageTrueMax], Mattes...Threader.hxx:238-245
       ok = ok && !(m < a.mmin) && !(m > a.mmax);
@@ -391,10 +371,16 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
     if (a.with_derivative && live)
       __stcs(a.cache + i, ok ? make_float4(term, g.x, g.y, g.z) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f));
     int pdfm = 0;
-    float arg, w[4] = {0.f, 0.f, 0.f, 0.f};
+    unsigned q[4] = {0u, 0u, 0u, 0u};
     const int fidx = __float_as_int(s.w);
-    if (ok) parzen_weights(term, B, pdfm, arg, w);
-    hist_add_aggregated(ok, fidx * B + pdfm, fidx, w, hist, fm);
+    if (ok) {
+      float t, w6[4];
+      parzen_window(term, B, pdfm, t);
+      parzen6(t, w6);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) q[k] = (__float2uint_rn(w6[k] * kQScale) + 3u) / 6u;  // unbiased 1/6
+    }
+    hist_add_aggregated(ok, fidx * B + pdfm, fidx, q, hist, fm);
     nv += ok ? 1u : 0u;
   }
   __syncthreads();
@@ -405,71 +391,66 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
   for (int k = threadIdx.x; k < B; k += blockDim.x) {
     const unsigned c = fm[k];
     if (c) atomicAdd(&a.fmarg[k], (unsigned long long)c);
+    unsigned long long cs = 0ull;
+    for (int f = 0; f < B; ++f) cs += hist[f * B + k];
+    if (cs) atomicAdd(&a.colsum[k], cs);
   }
   block_count(nv, a.acc_n);
 }
 
-// Mattes finalize: one block per fixed bin.  FP64 normalization, marginals,
-// sum p (log(p/pm) - log pf), and the FP32 log(p/pm) table for pass 2
+// Mattes finalize: one thread per joint-histogram bin.  FP64 normalization,
+// marginals, p (log(p/pm) - log pf), the FP32 log(p/pm) table for pass 2
 // (ComputeResults, Mattes...v4.hxx:358-499; JointPDFSum .hxx:533-541).
-// Row partials of the sum are added in row order by the last block.
-__global__ void k_mattes_finalize(EvalArgs a) {
-  extern __shared__ double colsum[];
-  __shared__ double sh_total, sh_logpf;
-  __shared__ double red[32];
+// Block partials of the sum are added in block order by the last block.
+__global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a) {
+  __shared__ double logpf[kFinalizeThreads + 2];
   const int B = a.bins;
-  const int f = blockIdx.x;
-  for (int m = threadIdx.x; m < B; m += blockDim.x) {
-    unsigned long long s = 0ull;  // exact integer column sum
-    for (int ff = 0; ff < B; ++ff) s += __ldcg(&a.hist[ff * B + m]);
-    colsum[m] = (double)s * (double)kQInv;
-  }
-  __syncthreads();
+  const int lane = threadIdx.x;
+  const int f_first = (blockIdx.x * kFinalizeThreads) / B;
+  // JointPDFSum: exact integer total of the moving marginal
+  unsigned long long tot = 0ull;
+  for (int m = lane; m < B; m += kFinalizeThreads) tot += __ldcg(&a.colsum[m]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  const double total = (double)tot * kQInv;
   const unsigned long long N = __ldcg(a.acc_n);
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int m = 0; m < B; ++m) t += colsum[m];
-    sh_total = t;
-    const double pf = (t > 0.0) ? (double)__ldcg(&a.fmarg[f]) / t : 0.0;
-    sh_logpf = pf > DBL_EPSILON ? log(pf) : 0.0;
+  const bool bad = (N == 0) || !(total >= DBL_EPSILON);
+  {
+    // log of the fixed marginal of the (at most kFinalizeThreads + 2) rows this block covers
+    const int f_last = min(B - 1, (int)((blockIdx.x * kFinalizeThreads + kFinalizeThreads - 1) / B));
+    const int f = f_first + lane;
+    if (f <= f_last && !bad) {
+      const double pf = (double)__ldcg(&a.fmarg[f]) / total;
+      logpf[lane] = pf > DBL_EPSILON ? log(pf) : 0.0;
+    }
   }
   __syncthreads();
-  const double total = sh_total;
-  const bool bad = (N == 0) || !(total >= DBL_EPSILON);
+  const int bin = blockIdx.x * kFinalizeThreads + lane;
   double part = 0.0;
-  if (!bad) {
-    const double nf = 1.0 / total;
-    const double pf = (double)__ldcg(&a.fmarg[f]) * nf;
-    for (int m = threadIdx.x; m < B; m += blockDim.x) {
-      const double p = (double)__ldcg(&a.hist[f * B + m]) * (double)kQInv * nf;
-      const double pm = colsum[m] * nf;
-      a.pdf_out[f * B + m] = p;
-      float pr = 0.f;
+  if (bin < B * B) {
+    const int f = bin / B, m = bin - f * B;
+    float pr = 0.f;
+    double p = 0.0;
+    if (!bad) {
+      const double nf = 1.0 / total;
+      p = (double)__ldcg(&a.hist[bin]) * kQInv * nf;
+      const double pm = (double)__ldcg(&a.colsum[m]) * kQInv * nf;
+      const double pf = (double)__ldcg(&a.fmarg[f]) * nf;
       if (pf > DBL_EPSILON && pm > DBL_EPSILON && p > DBL_EPSILON) {
         const double lr = log(p / pm);
-        part += p * (lr - sh_logpf);
+        part = p * (lr - logpf[f - f_first]);
         pr = (float)lr;
       }
-      a.pratio[f * B + m] = pr;
     }
-  } else {
-    for (int m = threadIdx.x; m < B; m += blockDim.x) {
-      a.pratio[f * B + m] = 0.f;
-      a.pdf_out[f * B + m] = 0.0;
-    }
+    a.pdf_out[bin] = p;
+    a.pratio[bin] = pr;
   }
   part = warp_sum_d(part);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
-    a.part[f] = s;
-  }
+  if (lane == 0) a.part[blockIdx.x] = part;
   if (!last_block(a.tickets + kTicketFinalize)) return;
-  if (threadIdx.x == 0) {
+  if (lane == 0) {
     double s = 0.0;
-    for (int r = 0; r < B; ++r) s += __ldcg(&a.part[r]);
+    for (int r = 0; r < (int)gridDim.x; ++r) s += __ldcg(&a.part[r]);
     const int st = N == 0 ? GB_ERR_NO_VALID_POINTS : (bad ? GB_ERR_JOINT_PDF_SUM_ZERO : GB_OK);
     *a.status = st;
     const double value = st == GB_OK ? -1.0 * s : 0.0;  // metrics minimize: value = -MI
@@ -499,13 +480,12 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass2_affine(EvalArgs a) {
     const float4 cc = __ldcs(a.cache + i);
     if (cc.x != cc.x) continue;  // rejected sample
     const float4 s = __ldcs(a.samples + i);
-    int midx = (int)cc.x;
-    midx = midx < 2 ? 2 : (midx > B - 3 ? B - 3 : midx);
-    const int pdfm = midx - 1;
-    const float arg = (float)pdfm - cc.x;
+    int pdfm;
+    float t, d[4];
+    parzen_window(cc.x, B, pdfm, t);
+    parzen_deriv(t, d);
     const float* row = pr + __float_as_int(s.w) * B + pdfm;
-    const float w = row[0] * bspline3_deriv(arg) + row[1] * bspline3_deriv(arg + 1.f) +
-                    row[2] * bspline3_deriv(arg + 2.f) + row[3] * bspline3_deriv(arg + 3.f);
+    const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
     const float vx = s.x - c[0], vy = s.y - c[1], vz = s.z - c[2];
     const float t0 = w * cc.y, t1 = w * cc.z, t2 = w * cc.w;
     acc[0].add(t0 * vx); acc[1].add(t0 * vy); acc[2].add(t0 * vz);

@@ -172,6 +172,7 @@ extern "C" int gb_metric_destroy(gb_metric* m) {
   if (m->h_params) cudaFreeHost(m->h_params);
   if (m->h_out) cudaFreeHost(m->h_out);
   if (m->h_status) cudaFreeHost(m->h_status);
+  if (m->h_consts) cudaFreeHost(m->h_consts);
   for (int i = 0; i < gb_metric::kMaxEvents; ++i)
     if (m->events[i]) cudaEventDestroy(m->events[i]);
   if (m->stream) cudaStreamDestroy(m->stream);
@@ -340,13 +341,14 @@ extern "C" int gb_metric_get_number_of_parameters(gb_metric* m, int64_t* nparams
 // Initialize
 
 // Accumulators cleared before every evaluation:
-// acc_n u64 | tickets kTicketCount u32 | hist B*B u64 | fmarg B u64
+// acc_n u64 | tickets kTicketCount u32 | hist B*B u64 | fmarg B u64 | colsum B u64
 static size_t acc_offset_tickets() { return 8; }
 static size_t acc_offset_hist() { return 8 + (sizeof(unsigned) * kTicketCount + 7) / 8 * 8; }
 static size_t acc_offset_fmarg(int64_t B) { return acc_offset_hist() + 8 * (size_t)(B * B); }
+static size_t acc_offset_colsum(int64_t B) { return acc_offset_fmarg(B) + 8 * (size_t)B; }
 static size_t acc_layout_bytes(const gb_metric* m) {
   const int64_t B = m->kind == GB_METRIC_MATTES ? m->bins : 0;
-  return acc_offset_fmarg(B) + 8 * (size_t)B;
+  return acc_offset_colsum(B) + 8 * (size_t)B;
 }
 
 extern "C" int gb_metric_initialize(gb_metric* m) {
@@ -505,6 +507,8 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   m->h_out = nullptr;
   GB_CUDA(cudaMallocHost(&m->h_params, sizeof(double) * std::max<size_t>(P, 1)));
   GB_CUDA(cudaMallocHost(&m->h_out, sizeof(double) * (2 + P)));
+  GB_CUDA(m->d_consts.alloc(1));
+  if (!m->h_consts) GB_CUDA(cudaMallocHost(&m->h_consts, sizeof(EvalConsts)));
   GB_CUDA(cudaStreamSynchronize(st));
   m->initialized = true;
   return GB_OK;
@@ -544,6 +548,8 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.tickets = reinterpret_cast<unsigned*>(base + acc_offset_tickets());
   a.hist = reinterpret_cast<unsigned long long*>(base + acc_offset_hist());
   a.fmarg = reinterpret_cast<unsigned long long*>(base + acc_offset_fmarg(m->bins));
+  a.colsum = reinterpret_cast<unsigned long long*>(base + acc_offset_colsum(m->bins));
+  a.consts = m->d_consts.p;
   a.part = m->d_scratch.p;
   a.grp = m->d_scratch.p + kGroupOffset;
   a.final_value = m->d_scratch.p + kFinalOffset;
@@ -597,7 +603,7 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   }
   GB_CUDA(cudaGetLastError());
   m->mark();
-  k_mattes_finalize<<<B, 128, sizeof(double) * B, st>>>(a);
+  k_mattes_finalize<<<(B * B + kFinalizeThreads - 1) / kFinalizeThreads, kFinalizeThreads, 0, st>>>(a);
   GB_CUDA(cudaGetLastError());
   m->mark();
   if (deriv) {
@@ -638,9 +644,10 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
   if (deriv && (size_t)nparams != P) return fail(GB_ERR_BAD_ARG, "derivative size must equal the number of parameters");
   GB_CUDA(cudaSetDevice(m->ctx->device));
   cudaStream_t st = m->stream;
-  std::copy(m->tparams.begin(), m->tparams.end(), m->h_params);
-  GB_CUDA(cudaMemcpyAsync(m->d_params.p, m->h_params, sizeof(double) * P, cudaMemcpyHostToDevice, st));
-  int rc = enqueue_eval(m, m->d_params.p, m->d_out.p, deriv);
+  // per-evaluation constants in FP64 on the host, uploaded with the parameters
+  affine_consts(m->tparams.data(), m->tfixed.data(), m->moving.p2i, m->moving.origin, *m->h_consts);
+  GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
+  int rc = enqueue_eval(m, nullptr, m->d_out.p, deriv);
   if (rc) return rc;
   GB_CUDA(cudaMemcpyAsync(m->h_out, m->d_out.p, sizeof(double) * (2 + (deriv ? P : 0)), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaMemcpyAsync(m->h_status, m->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -717,6 +724,10 @@ extern "C" int gb_metric_evaluate_device(gb_metric* m, const double* device_para
   if (!m || !device_params || !device_out) return fail(GB_ERR_BAD_ARG, "null argument");
   if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
   GB_CUDA(cudaSetDevice(m->ctx->device));
+  EvalArgs a;
+  fill_eval_args(m, a, device_params, device_out, with_derivative != 0);
+  k_prepare_affine<<<1, 1, 0, m->stream>>>(a, m->d_consts.p);
+  GB_CUDA(cudaGetLastError());
   return enqueue_eval(m, device_params, device_out, with_derivative != 0);
 }
 
