@@ -73,42 +73,41 @@ __device__ __forceinline__ void parzen_deriv(float t, float d[4]) {
 }
 
 // ---------------------------------------------------------------------------
-// A continuous index as integer base + fraction in [0, 1].
+// A continuous index as its nearest integer b = floor(cidx + 0.5) and the
+// centred remainder f = cidx - b in [-0.5, 0.5).  Positions close to a voxel
+// centre keep full relative precision in f, and the buffer test becomes exact.
 struct CIdx {
   int b[3];
   float f[3];
 };
 
-// ImageFunction::IsInsideBuffer: cindex in [-0.5, n - 0.5) per axis, NaN outside
-// (Core/ImageFunction/include/itkImageFunction.h:157-169).
+// ImageFunction::IsInsideBuffer: cidx in [-0.5, n - 0.5) per axis, NaN outside
+// (Core/ImageFunction/include/itkImageFunction.h:157-169).  With b the
+// round-half-up index, cidx >= -0.5 <=> b >= 0 and cidx < n - 0.5 <=> b <= n - 1.
 __device__ __forceinline__ bool ci_inside(const CIdx& c, int nx, int ny, int nz) {
   const int n[3] = {nx, ny, nz};
+  bool in = true;
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const int b = c.b[k];
-    const float f = c.f[k];
-    if (!(f >= 0.f)) return false;  // NaN position
-    if (b >= 0 && b <= n[k] - 2) continue;
-    if (b == -1) { if (!(f >= 0.5f)) return false; continue; }
-    if (b == n[k] - 1) { if (!(f < 0.5f)) return false; continue; }
-    return false;
-  }
-  return true;
+  for (int k = 0; k < 3; ++k) in = in && (c.f[k] == c.f[k]) && c.b[k] >= 0 && c.b[k] <= n[k] - 1;
+  return in;
 }
 
 // Corner indices and weights of LinearInterpolateImageFunction's 3-D path
 // (Core/ImageFunction/include/itkLinearInterpolateImageFunction.h:227-470):
-// base clamped to 0, distance clamped to >= 0, neighbour clamped to the end.
+// trilinear interpolation with neighbours clamped to the buffer, an axis with
+// distance <= 0 below the start contributing the start voxel only.  Measured
+// from the nearest voxel b, the second corner is b + sign(f) with weight |f|.
 struct Stencil {
   int x0, x1, y0, y1, z0, z1;
   float dx, dy, dz;
 };
 
-__device__ __forceinline__ void stencil_axis(int b, float d, int n, int& i0, int& i1, float& w) {
-  if (b < 0) { b = 0; d = 0.f; }
+__device__ __forceinline__ void stencil_axis(int b, float f, int n, int& i0, int& i1, float& w) {
   i0 = b;
-  i1 = (b + 1 <= n - 1 && d > 0.f) ? b + 1 : b;
-  w = d > 0.f ? d : 0.f;
+  int j = f > 0.f ? b + 1 : (f < 0.f ? b - 1 : b);
+  j = j < 0 ? 0 : (j > n - 1 ? n - 1 : j);
+  i1 = j;
+  w = fabsf(f);
 }
 
 __device__ __forceinline__ Stencil make_stencil(const CIdx& c, int nx, int ny, int nz) {
@@ -156,13 +155,6 @@ __device__ __forceinline__ float gather1(const float* __restrict__ img, const St
   return lerp(xx0, xx1, s.dz);
 }
 
-// Split a small FP32 offset t (relative to an integer base) into base + fraction.
-__device__ __forceinline__ void split_add(int base, float t, int& b, float& f) {
-  const float fl = floorf(t);
-  b = base + (int)fl;
-  f = t - fl;
-}
-
 // ---------------------------------------------------------------------------
 // double-float helpers
 
@@ -172,16 +164,22 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// A position as unevaluated sums hi + lo per axis (|lo| <= ulp(hi) / 2).
+struct DFPos {
+  float hi[3], lo[3];
+};
+
 // Affine map virtual point -> moving continuous index, as FP32 hi/lo pairs:
 // cidx_k = sum_j (Ahi + Alo)[k][j] x_j + (bhi + blo)[k].
 struct AffineDF {
   float Ahi[9], Alo[9], bhi[3], blo[3];
 };
 
-// cidx of one float point, to ~1e-12 voxel; floor and fraction of the pair.
-__device__ __forceinline__ CIdx map_df(const AffineDF& K, float x, float y, float z) {
+// Continuous index of one float point to ~1e-12 voxel: products by FMA error
+// terms, sums by two-sum.
+__device__ __forceinline__ DFPos map_pos(const AffineDF& K, float x, float y, float z) {
   const float xs[3] = {x, y, z};
-  CIdx c;
+  DFPos r;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     float s = K.bhi[k], err = K.blo[k];
@@ -195,14 +193,50 @@ __device__ __forceinline__ CIdx map_df(const AffineDF& K, float x, float y, floa
       s = t;
       err = __fadd_rn(err, __fadd_rn(e, __fmaf_rn(K.Alo[3 * k + j], xs[j], pe)));
     }
-    const float hi = __fadd_rn(s, err);
-    const float lo = __fsub_rn(err, __fsub_rn(hi, s));
-    float fl = floorf(hi);
-    if (hi == fl && lo < 0.f) fl -= 1.f;
-    c.b[k] = (int)fl;  // saturates for huge values: outside the buffer
-    c.f[k] = __fadd_rn(__fsub_rn(hi, fl), lo);
+    r.hi[k] = __fadd_rn(s, err);
+    r.lo[k] = __fsub_rn(err, __fsub_rn(r.hi[k], s));
   }
+  return r;
+}
+
+// Nearest integer b = floor(hi + lo + 0.5) and the remainder hi + lo - b.
+__device__ __forceinline__ void split_nearest(float hi, float lo, int& b, float& f) {
+  float s, e;
+  two_sum(hi, 0.5f, s, e);
+  const float e2 = __fadd_rn(e, lo);
+  float fl = floorf(s);
+  if (s == fl) {
+    if (e2 < 0.f) fl -= 1.f;
+  } else if (e2 >= __fsub_rn(fl + 1.f, s)) {
+    fl += 1.f;
+  }
+  b = (int)fl;  // saturates for huge values: outside any buffer
+  f = __fadd_rn(__fsub_rn(hi, fl), lo);
+}
+
+__device__ __forceinline__ CIdx to_cidx(const DFPos& p) {
+  CIdx c;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) split_nearest(p.hi[k], p.lo[k], c.b[k], c.f[k]);
   return c;
+}
+
+__device__ __forceinline__ CIdx map_df(const AffineDF& K, float x, float y, float z) {
+  return to_cidx(map_pos(K, x, y, z));
+}
+
+// p + (dhi + dlo) per axis, renormalized.
+__device__ __forceinline__ DFPos df_offset(const DFPos& p, const float* dhi, const float* dlo, float sign) {
+  DFPos r;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float s, e;
+    two_sum(p.hi[k], sign * dhi[k], s, e);
+    e = __fadd_rn(e, __fadd_rn(p.lo[k], sign * dlo[k]));
+    r.hi[k] = __fadd_rn(s, e);
+    r.lo[k] = __fsub_rn(e, __fsub_rn(r.hi[k], s));
+  }
+  return r;
 }
 
 // ---------------------------------------------------------------------------

@@ -83,8 +83,8 @@ struct EvalArgs {
   int nx, ny, nz;
   double m_p2i[9];
   double m_origin[3];
-  float cd_off[9];        // [3*d + k]: index-space offset along k of +0.5 spacing on physical axis d
-  float cd_inv_delta[3];  // 1 / spacing[d]
+  float cd_hi[9], cd_lo[9];  // [3*d + k]: index-space offset along k of +0.5 spacing on physical axis d
+  float cd_inv_delta[3];     // 1 / spacing[d]
   // transform
   const double* params;   // device parameters (device-resident path: k_prepare reads them)
   const EvalConsts* consts;
@@ -128,16 +128,13 @@ __device__ __forceinline__ void load_consts(const EvalConsts* g, EvalConsts& s) 
 
 // CentralDifferenceImageFunction::EvaluateSpecialized (point form, image direction on),
 // Core/ImageFunction/include/itkCentralDifferenceImageFunction.hxx:256-316
-__device__ __forceinline__ float3 central_difference(const EvalArgs& a, const CIdx& c) {
+__device__ __forceinline__ float3 central_difference(const EvalArgs& a, const DFPos& p) {
   float g[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    CIdx n1, n2;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) split_add(c.b[k], c.f[k] - a.cd_off[3 * d + k], n1.b[k], n1.f[k]);
+    const CIdx n1 = to_cidx(df_offset(p, a.cd_hi + 3 * d, a.cd_lo + 3 * d, -1.f));
     if (!ci_inside(n1, a.nx, a.ny, a.nz)) { g[d] = 0.f; continue; }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) split_add(c.b[k], c.f[k] + a.cd_off[3 * d + k], n2.b[k], n2.f[k]);
+    const CIdx n2 = to_cidx(df_offset(p, a.cd_hi + 3 * d, a.cd_lo + 3 * d, 1.f));
     if (!ci_inside(n2, a.nx, a.ny, a.nz)) { g[d] = 0.f; continue; }
     const float v1 = gather1(a.mov1, make_stencil(n1, a.nx, a.ny, a.nz), a.nx, a.ny);
     const float v2 = gather1(a.mov1, make_stencil(n2, a.nx, a.ny, a.nz), a.nx, a.ny);
@@ -149,7 +146,8 @@ __device__ __forceinline__ float3 central_difference(const EvalArgs& a, const CI
 // TransformAndEvaluateMovingPoint + ComputeMovingImageGradientAtPoint
 // (itkImageToImageMetricv4.hxx:331-425): buffer test, trilinear value, gradient.
 template <int GRAD>
-__device__ __forceinline__ bool eval_moving(const EvalArgs& a, const CIdx& c, bool need_grad, float& m, float3& g) {
+__device__ __forceinline__ bool eval_moving(const EvalArgs& a, const DFPos& p, bool need_grad, float& m, float3& g) {
+  const CIdx c = to_cidx(p);
   if (!ci_inside(c, a.nx, a.ny, a.nz)) return false;
   const Stencil st = make_stencil(c, a.nx, a.ny, a.nz);
   if (GRAD == kGradImage) {
@@ -158,7 +156,7 @@ __device__ __forceinline__ bool eval_moving(const EvalArgs& a, const CIdx& c, bo
     g = make_float3(v.y, v.z, v.w);
   } else {
     m = gather1(a.mov1, st, a.nx, a.ny);
-    g = need_grad ? central_difference(a, c) : make_float3(0.f, 0.f, 0.f);
+    g = need_grad ? central_difference(a, p) : make_float3(0.f, 0.f, 0.f);
   }
   return true;
 }
@@ -193,6 +191,20 @@ __device__ __forceinline__ void block_sums(KahanF (&acc)[NV], double (*red)[NV],
   __syncthreads();
 }
 
+// dst[k] = sum_{j < cnt} src[j * NV + k] for k < NV, one warp per k: lane l loads
+// entries l, l + 32, ... (independent loads in flight together), then a fixed
+// XOR-shuffle tree -- the same order on every call.
+template <int NV>
+__device__ __forceinline__ void strided_sums(const double* src, int cnt, double* dst) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int k = warp; k < NV; k += nwarps) {
+    double s = 0.0;
+    for (int j = lane; j < cnt; j += 32) s += __ldcg(&src[j * NV + k]);
+    s = warp_sum_d(s);
+    if (lane == 0) dst[k] = s;
+  }
+}
+
 // Returns true in exactly one block, which then holds the grid-wide sums in `fin`.
 template <int NV>
 __device__ __forceinline__ bool grid_sums(const double* blk, double* part, double* grp, unsigned* tick, double* fin) {
@@ -207,22 +219,17 @@ __device__ __forceinline__ bool grid_sums(const double* blk, double* part, doubl
   __syncthreads();
   if (t != (unsigned)(gsize - 1)) return false;
   __threadfence();
-  for (int k = threadIdx.x; k < NV; k += blockDim.x) {
-    double s = 0.0;
-    for (int j = g * kGroup; j < g * kGroup + gsize; ++j) s += __ldcg(&part[j * NV + k]);
-    grp[g * NV + k] = s;
-  }
+  strided_sums<NV>(part + g * kGroup * NV, gsize, grp + g * NV);
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) t = atomicAdd(&tick[ng], 1u);
   __syncthreads();
   if (t != (unsigned)(ng - 1)) return false;
   __threadfence();
-  for (int k = threadIdx.x; k < NV; k += blockDim.x) {
-    double s = 0.0;
-    for (int j = 0; j < ng; ++j) s += __ldcg(&grp[j * NV + k]);
-    fin[k] = s;
-  }
+  __shared__ double fin_s[NV];
+  strided_sums<NV>(grp, ng, fin_s);
+  __syncthreads();
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) fin[k] = fin_s[k];
   __syncthreads();
   return true;
 }
@@ -263,12 +270,15 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
   for (int k = 0; k < 13; ++k) acc[k].zero();
   unsigned nv = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-    const float4 s = __ldcs(a.samples + i);
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float4 s_next = i < a.n ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  for (; i < a.n; i += stride) {
+    const float4 s = s_next;
+    s_next = i + stride < a.n ? __ldcs(a.samples + i + stride) : make_float4(0.f, 0.f, 0.f, 0.f);
     float m;
     float3 g;
-    const CIdx c = map_df(K.map, s.x, s.y, s.z);
-    if (!eval_moving<GRAD>(a, c, a.with_derivative != 0, m, g)) continue;
+    const DFPos p = map_pos(K.map, s.x, s.y, s.z);
+    if (!eval_moving<GRAD>(a, p, a.with_derivative != 0, m, g)) continue;
     const float diff = s.w - m;  // FixedImagePixelType diff, MeanSquares...Threader.hxx:46
     acc[0].add(diff * diff);
     ++nv;
@@ -353,16 +363,20 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
   unsigned nv = 0;
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < a.n; base += stride) {
+  int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  float4 s_next = base + lane < a.n ? __ldcs(a.samples + base + lane) : make_float4(0.f, 0.f, 0.f, 0.f);
+  for (; base < a.n; base += stride) {
     const int64_t i = base + lane;
     const bool live = i < a.n;
-    const float4 s = live ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 s = s_next;
+    // prefetch the next record so its latency overlaps this iteration's gathers
+    s_next = i + stride < a.n ? __ldcs(a.samples + i + stride) : make_float4(0.f, 0.f, 0.f, 0.f);
     float m = 0.f;
     float3 g = make_float3(0.f, 0.f, 0.f);
     bool ok = false;
     if (live) {
-      const CIdx c = map_df(K.map, s.x, s.y, s.z);
-      ok = eval_moving<GRAD>(a, c, a.with_derivative != 0, m, g);
+      const DFPos p = map_pos(K.map, s.x, s.y, s.z);
+      ok = eval_moving<GRAD>(a, p, a.with_derivative != 0, m, g);
       // reject moving values outside [MovingImageTrueMin, MovingImageTrueMax], Mattes...Threader.hxx:238-245
       ok = ok && !(m < a.mmin) && !(m > a.mmax);
     }
@@ -448,9 +462,10 @@ __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a
   part = warp_sum_d(part);
   if (lane == 0) a.part[blockIdx.x] = part;
   if (!last_block(a.tickets + kTicketFinalize)) return;
+  double s = 0.0;
+  for (int r = lane; r < (int)gridDim.x; r += 32) s += __ldcg(&a.part[r]);
+  s = warp_sum_d(s);
   if (lane == 0) {
-    double s = 0.0;
-    for (int r = 0; r < (int)gridDim.x; ++r) s += __ldcg(&a.part[r]);
     const int st = N == 0 ? GB_ERR_NO_VALID_POINTS : (bad ? GB_ERR_JOINT_PDF_SUM_ZERO : GB_OK);
     *a.status = st;
     const double value = st == GB_OK ? -1.0 * s : 0.0;  // metrics minimize: value = -MI
@@ -476,22 +491,31 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass2_affine(EvalArgs a) {
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k].zero();
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-    const float4 cc = __ldcs(a.cache + i);
-    if (cc.x != cc.x) continue;  // rejected sample
-    const float4 s = __ldcs(a.samples + i);
-    int pdfm;
-    float t, d[4];
-    parzen_window(cc.x, B, pdfm, t);
-    parzen_deriv(t, d);
-    const float* row = pr + __float_as_int(s.w) * B + pdfm;
-    const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
-    const float vx = s.x - c[0], vy = s.y - c[1], vz = s.z - c[2];
-    const float t0 = w * cc.y, t1 = w * cc.z, t2 = w * cc.w;
-    acc[0].add(t0 * vx); acc[1].add(t0 * vy); acc[2].add(t0 * vz);
-    acc[3].add(t1 * vx); acc[4].add(t1 * vy); acc[5].add(t1 * vz);
-    acc[6].add(t2 * vx); acc[7].add(t2 * vy); acc[8].add(t2 * vz);
-    acc[9].add(t0); acc[10].add(t1); acc[11].add(t2);
+  constexpr int kUnroll = 4;  // independent loads in flight per thread
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < a.n; i0 += kUnroll * stride) {
+    float4 cc[kUnroll], s[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const int64_t i = i0 + u * stride;
+      cc[u] = i < a.n ? __ldcs(a.cache + i) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+      s[u] = i < a.n ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      if (cc[u].x != cc[u].x) continue;  // rejected sample
+      int pdfm;
+      float t, d[4];
+      parzen_window(cc[u].x, B, pdfm, t);
+      parzen_deriv(t, d);
+      const float* row = pr + __float_as_int(s[u].w) * B + pdfm;
+      const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
+      const float vx = s[u].x - c[0], vy = s[u].y - c[1], vz = s[u].z - c[2];
+      const float t0 = w * cc[u].y, t1 = w * cc[u].z, t2 = w * cc[u].w;
+      acc[0].add(t0 * vx); acc[1].add(t0 * vy); acc[2].add(t0 * vz);
+      acc[3].add(t1 * vx); acc[4].add(t1 * vy); acc[5].add(t1 * vz);
+      acc[6].add(t2 * vx); acc[7].add(t2 * vy); acc[8].add(t2 * vz);
+      acc[9].add(t0); acc[10].add(t1); acc[11].add(t2);
+    }
   }
   block_sums<12>(acc, red, blk);
   if (!grid_sums<12>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin)) return;

@@ -103,6 +103,15 @@ static int grid_for(const gb_metric* m, int64_t n, int per_sm) {
   return (int)std::max<int64_t>(1, std::min(want, cap));
 }
 
+// One full wave of resident blocks (grid-stride kernels), from the occupancy calculator.
+template <typename K>
+static int full_wave(const gb_metric* m, K kernel, size_t smem, int64_t n) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 2;
+  return grid_for(m, n, per_sm);
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -531,7 +540,7 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   // central difference: +0.5 spacing along physical axis d, in index space
   for (int d = 0; d < 3; ++d) {
     const double off = 0.5 * m->moving.spacing[d];
-    for (int k = 0; k < 3; ++k) a.cd_off[3 * d + k] = (float)(m->moving.p2i[3 * k + d] * off);
+    for (int k = 0; k < 3; ++k) split_df(m->moving.p2i[3 * k + d] * off, a.cd_hi[3 * d + k], a.cd_lo[3 * d + k]);
     a.cd_inv_delta[d] = (float)(1.0 / ((off) - (-off)));
   }
   a.params = d_params;
@@ -580,9 +589,12 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   m->nevents = 0;
   m->mark();
   if (m->kind == GB_METRIC_MEAN_SQUARES) {
-    const int grid = grid_for(m, m->nsamples, 4);
-    if (cd) k_msq_affine<kGradCentralDifference><<<grid, kBlock, 0, st>>>(a);
-    else k_msq_affine<kGradImage><<<grid, kBlock, 0, st>>>(a);
+    if (cd) {
+      k_msq_affine<kGradCentralDifference>
+          <<<full_wave(m, k_msq_affine<kGradCentralDifference>, 0, m->nsamples), kBlock, 0, st>>>(a);
+    } else {
+      k_msq_affine<kGradImage><<<full_wave(m, k_msq_affine<kGradImage>, 0, m->nsamples), kBlock, 0, st>>>(a);
+    }
     GB_CUDA(cudaGetLastError());
     m->mark();
     return GB_OK;
@@ -592,14 +604,15 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   const size_t sh1 = sizeof(unsigned long long) * B * B + sizeof(unsigned) * B;
   const size_t sh2 = sizeof(float) * B * B;
   if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
-  const int grid = grid_for(m, m->nsamples, 4);
   if (cd) {
     cudaFuncSetAttribute(k_mattes_pass1_affine<kGradCentralDifference>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sh1);
-    k_mattes_pass1_affine<kGradCentralDifference><<<grid, kBlock, sh1, st>>>(a);
+    k_mattes_pass1_affine<kGradCentralDifference>
+        <<<full_wave(m, k_mattes_pass1_affine<kGradCentralDifference>, sh1, m->nsamples), kBlock, sh1, st>>>(a);
   } else {
     cudaFuncSetAttribute(k_mattes_pass1_affine<kGradImage>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh1);
-    k_mattes_pass1_affine<kGradImage><<<grid, kBlock, sh1, st>>>(a);
+    k_mattes_pass1_affine<kGradImage>
+        <<<full_wave(m, k_mattes_pass1_affine<kGradImage>, sh1, m->nsamples), kBlock, sh1, st>>>(a);
   }
   GB_CUDA(cudaGetLastError());
   m->mark();
@@ -608,7 +621,7 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   m->mark();
   if (deriv) {
     cudaFuncSetAttribute(k_mattes_pass2_affine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh2);
-    k_mattes_pass2_affine<<<grid_for(m, m->nsamples, 4), kBlock, sh2, st>>>(a);
+    k_mattes_pass2_affine<<<full_wave(m, k_mattes_pass2_affine, sh2, m->nsamples), kBlock, sh2, st>>>(a);
     GB_CUDA(cudaGetLastError());
     m->mark();
   }

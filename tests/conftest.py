@@ -39,12 +39,15 @@ def pytest_collection_modifyitems(config, items):
 # within 1e-4 relative (relative to the derivative's largest magnitude component)
 VALUE_RTOL = 1e-5
 DERIV_RTOL = 1e-4
+# Mattes MI can be ~0 (e.g. 5 bins leave one central bin): there a relative bound is
+# meaningless, so the value also passes within 1e-8 absolute (entropies are O(1) nats)
+MATTES_VALUE_ATOL = 1e-8
 
 
-def assert_value_close(got, want, rtol=VALUE_RTOL, what="value"):
-    denom = max(abs(want), 1e-300)
-    err = abs(got - want) / denom
-    assert err <= rtol, f"{what}: got {got!r} want {want!r} rel err {err:.3e} > {rtol:.1e}"
+def assert_value_close(got, want, rtol=VALUE_RTOL, what="value", atol=0.0):
+    err = abs(got - want)
+    assert err <= rtol * abs(want) + atol, \
+        f"{what}: got {got!r} want {want!r} abs err {err:.3e} > {rtol:.1e} * |want| + {atol:.1e}"
 
 
 def assert_deriv_close(got, want, rtol=DERIV_RTOL, what="derivative"):
