@@ -200,7 +200,10 @@ __global__ void k_build_samples(BuildArgs b) {
   }
   b.keys[i] = key;
   b.vals[i] = (uint32_t)i;
-  b.recs[i] = make_float4((float)vp[0], (float)vp[1], (float)vp[2], aux);
+  // domain coordinates: the point for a point set, the exact grid index for the dense domain
+  if (b.points) b.recs[i] = make_float4((float)vp[0], (float)vp[1], (float)vp[2], aux);
+  else b.recs[i] = make_float4((float)(i % b.virt.n[0]), (float)((i / b.virt.n[0]) % b.virt.n[1]),
+                               (float)(i / (b.virt.n[0] * b.virt.n[1])), aux);
   if (b.bsp) {
     b.bsp[i] = sup;
     b.bspf[i] = fr;

@@ -30,21 +30,36 @@ constexpr int kMaxBlocks = 2048;          // grid cap of the evaluation kernels
 constexpr int kTicketMain = 0;            // grid_sums of the MeanSquares kernel: [0, 128]
 constexpr int kTicketFinalize = 160;      // last_block of the Mattes finalize
 constexpr int kTicketPass2 = 192;         // grid_sums of Mattes pass 2: [192, 320]
+constexpr int kTicketPass1 = 176;         // last_block of Mattes pass 1
 constexpr int kTicketCount = 352;
 constexpr int kPartPass2 = 4096;          // offset of pass-2 partials (finalize blocks use [0, 4096))
 constexpr size_t kGroupOffset = kPartPass2 + (size_t)kMaxBlocks * 16;  // per-group partials: 128 groups x 16
 constexpr size_t kFinalOffset = kGroupOffset + 2048;
-constexpr size_t kScratchDoubles = kFinalOffset + 8;
+constexpr size_t kMargOffset = kFinalOffset + 8;        // [T, 1/T]
+constexpr size_t kLogColOffset = kMargOffset + 8;       // bins doubles
+constexpr size_t kLogRowOffset = kLogColOffset + 4096;  // bins doubles
+constexpr size_t kScratchDoubles = kLogRowOffset + 4096;
 constexpr int kFinalizeThreads = 32;
 constexpr float kQScale = 67108864.f;  // 2^26 fixed point of histogram weights
 constexpr double kQInv = 1.0 / 67108864.0;
 
 // Per-evaluation transform constants (computed in FP64 once per evaluation,
-// stored as FP32 / double-float).
+// stored as FP32 / double-float).  Sample records hold "domain coordinates":
+// the physical point for a sampled point set, the integer grid index for the
+// dense virtual domain (so dense points are exact).  `map` takes domain
+// coordinates to the moving continuous index; U, joff give the affine
+// Jacobian's x - c = U u + joff.
 struct EvalConsts {
-  AffineDF map;  // virtual point -> moving continuous index
-  float c[3];    // affine centre (Jacobian)
+  AffineDF map;
+  float U[9];
+  float joff[3];
 };
+
+__device__ __forceinline__ float3 jac_vec(const EvalConsts& K, float x, float y, float z) {
+  return make_float3(fmaf(K.U[0], x, fmaf(K.U[1], y, fmaf(K.U[2], z, K.joff[0]))),
+                     fmaf(K.U[3], x, fmaf(K.U[4], y, fmaf(K.U[5], z, K.joff[1]))),
+                     fmaf(K.U[6], x, fmaf(K.U[7], y, fmaf(K.U[8], z, K.joff[2]))));
+}
 
 // MatrixOffsetTransformBase::ComputeOffset (itkMatrixOffsetTransformBase.hxx:612-631)
 // composed with ImageBase::TransformPhysicalPointToContinuousIndex (itkImageBase.h:515-531).
@@ -53,26 +68,51 @@ __host__ __device__ inline void split_df(double x, float& hi, float& lo) {
   lo = (float)(x - (double)hi);
 }
 
-__host__ __device__ inline void affine_consts(const double* p, const double center[3], const double m_p2i[9],
-                                              const double m_origin[3], EvalConsts& K) {
-  double M[9], off[3];
-  for (int i = 0; i < 9; ++i) M[i] = p[i];
-  for (int i = 0; i < 3; ++i) {
-    double o = p[9 + i] + center[i];
-    for (int j = 0; j < 3; ++j) o -= M[i * 3 + j] * center[j];
-    off[i] = o;
+// dom2phys / dom_origin: domain coordinates -> physical point (the virtual
+// grid's index-to-physical map for dense sampling; null for a point set).
+// One output of the constants: e in [0, 9) the map's matrix entry (r, c) = (e / 3, e % 3),
+// e in [9, 12) its offset row e - 9, e == 12 the Jacobian terms.  Rows of the
+// physical-point -> moving-index map: A = P2I M, b = P2I (offset - origin_m),
+// offset = t + c - M c.
+__host__ __device__ inline void affine_const_entry(int e, const double* p, const double center[3],
+                                                   const double m_p2i[9], const double m_origin[3],
+                                                   const double* dom2phys, const double* dom_origin, EvalConsts& K) {
+  const double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, Z[3] = {0, 0, 0};
+  const double* U = dom2phys ? dom2phys : I;
+  const double* u0 = dom2phys ? dom_origin : Z;
+  if (e == 12) {
+    for (int i = 0; i < 9; ++i) K.U[i] = (float)U[i];
+    for (int i = 0; i < 3; ++i) K.joff[i] = (float)(u0[i] - center[i]);
+    return;
   }
-  for (int r = 0; r < 3; ++r) {
-    for (int c = 0; c < 3; ++c) {
-      double s = 0.0;
-      for (int k = 0; k < 3; ++k) s += m_p2i[r * 3 + k] * M[k * 3 + c];
-      split_df(s, K.map.Ahi[r * 3 + c], K.map.Alo[r * 3 + c]);
-    }
+  const int r = e < 9 ? e / 3 : e - 9;
+  double Ar[3];
+  for (int c = 0; c < 3; ++c) {
     double s = 0.0;
-    for (int k = 0; k < 3; ++k) s += m_p2i[r * 3 + k] * (off[k] - m_origin[k]);
-    split_df(s, K.map.bhi[r], K.map.blo[r]);
+    for (int k = 0; k < 3; ++k) s += m_p2i[r * 3 + k] * p[k * 3 + c];
+    Ar[c] = s;
   }
-  for (int i = 0; i < 3; ++i) K.c[i] = (float)center[i];
+  if (e < 9) {
+    const int c = e % 3;
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) s += Ar[k] * U[k * 3 + c];
+    split_df(s, K.map.Ahi[e], K.map.Alo[e]);
+    return;
+  }
+  double br = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    double o = p[9 + k] + center[k];
+    for (int j = 0; j < 3; ++j) o -= p[k * 3 + j] * center[j];
+    br += m_p2i[r * 3 + k] * (o - m_origin[k]);
+  }
+  for (int k = 0; k < 3; ++k) br += Ar[k] * u0[k];
+  split_df(br, K.map.bhi[r], K.map.blo[r]);
+}
+
+__host__ __device__ inline void affine_consts(const double* p, const double center[3], const double m_p2i[9],
+                                              const double m_origin[3], const double* dom2phys,
+                                              const double* dom_origin, EvalConsts& K) {
+  for (int e = 0; e < 13; ++e) affine_const_entry(e, p, center, m_p2i, m_origin, dom2phys, dom_origin, K);
 }
 
 struct EvalArgs {
@@ -90,6 +130,9 @@ struct EvalArgs {
   const EvalConsts* consts;
   int nparams;
   double center[3];       // affine centre
+  int dense;              // sample records hold virtual grid indices
+  double v_i2p[9];        // virtual grid index -> physical point (dense)
+  double v_origin[3];
   // Mattes
   int bins;
   float mmin, mmax, m_inv_bs;
@@ -104,6 +147,9 @@ struct EvalArgs {
   double* part;                 // per-block partials
   double* grp;                  // per-group partials
   double* final_value;          // Mattes value handed from finalize to pass 2
+  double* logcol;               // bins: log of the fixed-point moving marginal
+  double* logrow;               // bins: log pf
+  double* marg;                 // [fixed-point total T, 1 / T]
   float4* cache;
   float* pratio;
   double* pdf_out;
@@ -113,8 +159,11 @@ struct EvalArgs {
 };
 
 // Device twin of the host constant computation (parameters already in HBM).
+// 13 threads, one output each, so the FP64 dependency chains run side by side.
 __global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) affine_consts(a.params, a.center, a.m_p2i, a.m_origin, *out);
+  if (threadIdx.x < 13)
+    affine_const_entry(threadIdx.x, a.params, a.center, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin,
+                       *out);
 }
 
 __device__ __forceinline__ void load_consts(const EvalConsts* g, EvalConsts& s) {
@@ -174,19 +223,20 @@ __device__ __forceinline__ bool eval_moving(const EvalArgs& a, const DFPos& p, b
 constexpr int kGroup = 16;
 
 template <int NV>
-__device__ __forceinline__ void block_sums(KahanF (&acc)[NV], double (*red)[NV], double* out) {
+__device__ __forceinline__ void block_sums(KahanF (&acc)[NV], float (*red)[NV], double* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
     const float v = warp_sum(acc[k].value());
-    if (lane == 0) red[warp][k] = (double)v;
+    if (lane == 0) red[warp][k] = v;
   }
   __syncthreads();
   const int nwarps = blockDim.x >> 5;
   for (int k = threadIdx.x; k < NV; k += blockDim.x) {
-    double s = 0.0;
-    for (int w = 0; w < nwarps; ++w) s += red[w][k];
-    out[k] = s;
+    KahanF s;
+    s.zero();
+    for (int w = 0; w < nwarps; ++w) s.add(red[w][k]);
+    out[k] = (double)s.value();  // FP32 compensated inside the block, FP64 across blocks
   }
   __syncthreads();
 }
@@ -261,7 +311,7 @@ __device__ __forceinline__ bool last_block(unsigned* ticket) {
 template <int GRAD>
 __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
   __shared__ EvalConsts K;
-  __shared__ double red[kBlock / 32][13];
+  __shared__ float red[kBlock / 32][13];
   __shared__ double blk[13], fin[13];
   load_consts(a.consts, K);
   __syncthreads();
@@ -284,7 +334,8 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
     ++nv;
     if (a.with_derivative) {
       const float t = 2.f * diff;
-      const float vx = s.x - K.c[0], vy = s.y - K.c[1], vz = s.z - K.c[2];
+      const float3 v = jac_vec(K, s.x, s.y, s.z);
+      const float vx = v.x, vy = v.y, vz = v.z;
       const float t0 = t * g.x, t1 = t * g.y, t2 = t * g.z;
       acc[1].add(t0 * vx); acc[2].add(t0 * vy); acc[3].add(t0 * vz);
       acc[4].add(t1 * vx); acc[5].add(t1 * vy); acc[6].add(t1 * vz);
@@ -354,10 +405,14 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
   extern __shared__ unsigned long long smem_u64[];
   const int B = a.bins;
   unsigned long long* hist = smem_u64;
-  unsigned* fm = reinterpret_cast<unsigned*>(smem_u64 + B * B);
+  unsigned long long* cs = smem_u64 + B * B;
+  unsigned* fm = reinterpret_cast<unsigned*>(smem_u64 + B * B + B);
   __shared__ EvalConsts K;
   for (int k = threadIdx.x; k < B * B; k += blockDim.x) hist[k] = 0ull;
-  for (int k = threadIdx.x; k < B; k += blockDim.x) fm[k] = 0u;
+  for (int k = threadIdx.x; k < B; k += blockDim.x) {
+    fm[k] = 0u;
+    cs[k] = 0ull;
+  }
   load_consts(a.consts, K);
   __syncthreads();
   unsigned nv = 0;
@@ -398,47 +453,60 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
     nv += ok ? 1u : 0u;
   }
   __syncthreads();
+  // flush the nonzero bins; the block's column sums ride along as shared atomics
   for (int k = threadIdx.x; k < B * B; k += blockDim.x) {
     const unsigned long long h = hist[k];
-    if (h) atomicAdd(&a.hist[k], h);
-  }
-  for (int k = threadIdx.x; k < B; k += blockDim.x) {
-    const unsigned c = fm[k];
-    if (c) atomicAdd(&a.fmarg[k], (unsigned long long)c);
-    unsigned long long cs = 0ull;
-    for (int f = 0; f < B; ++f) cs += hist[f * B + k];
-    if (cs) atomicAdd(&a.colsum[k], cs);
-  }
-  block_count(nv, a.acc_n);
-}
-
-// Mattes finalize: one thread per joint-histogram bin.  FP64 normalization,
-// marginals, p (log(p/pm) - log pf), the FP32 log(p/pm) table for pass 2
-// (ComputeResults, Mattes...v4.hxx:358-499; JointPDFSum .hxx:533-541).
-// Block partials of the sum are added in block order by the last block.
-__global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a) {
-  __shared__ double logpf[kFinalizeThreads + 2];
-  const int B = a.bins;
-  const int lane = threadIdx.x;
-  const int f_first = (blockIdx.x * kFinalizeThreads) / B;
-  // JointPDFSum: exact integer total of the moving marginal
-  unsigned long long tot = 0ull;
-  for (int m = lane; m < B; m += kFinalizeThreads) tot += __ldcg(&a.colsum[m]);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-  const double total = (double)tot * kQInv;
-  const unsigned long long N = __ldcg(a.acc_n);
-  const bool bad = (N == 0) || !(total >= DBL_EPSILON);
-  {
-    // log of the fixed marginal of the (at most kFinalizeThreads + 2) rows this block covers
-    const int f_last = min(B - 1, (int)((blockIdx.x * kFinalizeThreads + kFinalizeThreads - 1) / B));
-    const int f = f_first + lane;
-    if (f <= f_last && !bad) {
-      const double pf = (double)__ldcg(&a.fmarg[f]) / total;
-      logpf[lane] = pf > DBL_EPSILON ? log(pf) : 0.0;
+    if (h) {
+      atomicAdd(&a.hist[k], h);
+      atomicAdd(&cs[k % B], h);
     }
   }
   __syncthreads();
+  for (int k = threadIdx.x; k < B; k += blockDim.x) {
+    const unsigned c = fm[k];
+    if (c) atomicAdd(&a.fmarg[k], (unsigned long long)c);
+    if (cs[k]) atomicAdd(&a.colsum[k], cs[k]);
+  }
+  block_count(nv, a.acc_n);
+  if (!last_block(a.tickets + kTicketPass1)) return;
+  // Last block: marginal logs once, in FP64, for the finalize.  With T the
+  // (fixed-point) joint-histogram total, p = h / T, pm = colsum / T and
+  // pf = count 2^26 / T, so log(p / pm) = log h - log colsum and
+  // log pf = log count + 26 ln 2 - log T.
+  __shared__ unsigned long long tot_sh;
+  if (threadIdx.x == 0) tot_sh = 0ull;
+  __syncthreads();
+  unsigned long long t = 0ull;
+  for (int k = threadIdx.x; k < B; k += blockDim.x) t += __ldcg(&a.colsum[k]);
+  atomicAdd(&tot_sh, t);
+  __syncthreads();
+  const double T = (double)tot_sh;
+  const double logT = T > 0.0 ? log(T) : 0.0;
+  for (int k = threadIdx.x; k < B; k += blockDim.x) {
+    const double c = (double)__ldcg(&a.colsum[k]);
+    a.logcol[k] = c > 0.0 ? log(c) : 0.0;
+    const double n = (double)__ldcg(&a.fmarg[k]);
+    a.logrow[k] = n > 0.0 ? log(n) + 26.0 * 0.69314718055994530942 - logT : 0.0;
+  }
+  if (threadIdx.x == 0) {
+    a.marg[0] = T;                         // fixed-point total
+    a.marg[1] = T > 0.0 ? 1.0 / T : 0.0;   // normalization factor (of the fixed-point histogram)
+  }
+}
+
+// Mattes finalize: one thread per joint-histogram bin.  FP64 normalization and
+// p (log(p/pm) - log pf), with the marginal logs from pass 1's last block, and
+// the FP32 log(p/pm) table for pass 2 (ComputeResults, Mattes...v4.hxx:358-499;
+// JointPDFSum .hxx:533-541).  Block partials are added in block order by the
+// last block.
+__global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a) {
+  const int B = a.bins;
+  const int lane = threadIdx.x;
+  const double T = __ldcg(&a.marg[0]);
+  const double invT = __ldcg(&a.marg[1]);
+  const double total = T * kQInv;  // JointPDFSum
+  const unsigned long long N = __ldcg(a.acc_n);
+  const bool bad = (N == 0) || !(total >= DBL_EPSILON);
   const int bin = blockIdx.x * kFinalizeThreads + lane;
   double part = 0.0;
   if (bin < B * B) {
@@ -446,13 +514,13 @@ __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a
     float pr = 0.f;
     double p = 0.0;
     if (!bad) {
-      const double nf = 1.0 / total;
-      p = (double)__ldcg(&a.hist[bin]) * kQInv * nf;
-      const double pm = (double)__ldcg(&a.colsum[m]) * kQInv * nf;
-      const double pf = (double)__ldcg(&a.fmarg[f]) * nf;
+      const double h = (double)__ldcg(&a.hist[bin]);
+      p = h * invT;
+      const double pm = (double)__ldcg(&a.colsum[m]) * invT;
+      const double pf = (double)__ldcg(&a.fmarg[f]) * (invT * 67108864.0);
       if (pf > DBL_EPSILON && pm > DBL_EPSILON && p > DBL_EPSILON) {
-        const double lr = log(p / pm);
-        part = p * (lr - logpf[f - f_first]);
+        const double lr = log(h) - __ldcg(&a.logcol[m]);  // log(p / pm)
+        part = p * (lr - __ldcg(&a.logrow[f]));
         pr = (float)lr;
       }
     }
@@ -478,20 +546,20 @@ __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a
 }
 
 // Mattes pass 2, affine: derivative from the cached Parzen terms and gradients.
-__global__ void __launch_bounds__(kBlock) k_mattes_pass2_affine(EvalArgs a) {
+__global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
   extern __shared__ float pr[];
-  __shared__ float c[3];
-  __shared__ double red[kBlock / 32][12];
+  __shared__ EvalConsts K;
+  __shared__ float red[kBlock / 32][12];
   __shared__ double blk[12], fin[12];
   const int B = a.bins;
   for (int k = threadIdx.x; k < B * B; k += blockDim.x) pr[k] = __ldcg(&a.pratio[k]);
-  if (threadIdx.x < 3) c[threadIdx.x] = (float)a.center[threadIdx.x];
+  load_consts(a.consts, K);
   __syncthreads();
   KahanF acc[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k].zero();
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  constexpr int kUnroll = 4;  // independent loads in flight per thread
+  constexpr int kUnroll = 2;  // independent loads in flight per thread
   for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < a.n; i0 += kUnroll * stride) {
     float4 cc[kUnroll], s[kUnroll];
 #pragma unroll
@@ -509,7 +577,8 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass2_affine(EvalArgs a) {
       parzen_deriv(t, d);
       const float* row = pr + __float_as_int(s[u].w) * B + pdfm;
       const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
-      const float vx = s[u].x - c[0], vy = s[u].y - c[1], vz = s[u].z - c[2];
+      const float3 v = jac_vec(K, s[u].x, s[u].y, s[u].z);
+      const float vx = v.x, vy = v.y, vz = v.z;
       const float t0 = w * cc[u].y, t1 = w * cc[u].z, t2 = w * cc[u].w;
       acc[0].add(t0 * vx); acc[1].add(t0 * vy); acc[2].add(t0 * vz);
       acc[3].add(t1 * vx); acc[4].add(t1 * vy); acc[5].add(t1 * vz);

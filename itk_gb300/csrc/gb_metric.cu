@@ -547,6 +547,9 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.nparams = (int)m->tparams.size();
   if (m->tkind == GB_TRANSFORM_AFFINE)
     for (int i = 0; i < 3; ++i) a.center[i] = m->tfixed[i];
+  a.dense = m->use_sampled ? 0 : 1;
+  for (int i = 0; i < 9; ++i) a.v_i2p[i] = m->virt.i2p[i];
+  for (int i = 0; i < 3; ++i) a.v_origin[i] = m->virt.origin[i];
   a.bins = (int)m->bins;
   a.mmin = (float)m->mstate[2];
   a.mmax = (float)m->mstate[3];
@@ -562,6 +565,9 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.part = m->d_scratch.p;
   a.grp = m->d_scratch.p + kGroupOffset;
   a.final_value = m->d_scratch.p + kFinalOffset;
+  a.marg = m->d_scratch.p + kMargOffset;
+  a.logcol = m->d_scratch.p + kLogColOffset;
+  a.logrow = m->d_scratch.p + kLogRowOffset;
   a.cache = m->d_cache.p;
   a.pratio = m->d_pratio.p;
   a.pdf_out = m->d_pdf.p;
@@ -601,7 +607,7 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   }
   // Mattes: pass 1, finalize, pass 2
   const int B = (int)m->bins;
-  const size_t sh1 = sizeof(unsigned long long) * B * B + sizeof(unsigned) * B;
+  const size_t sh1 = sizeof(unsigned long long) * (B * B + B) + sizeof(unsigned) * B;
   const size_t sh2 = sizeof(float) * B * B;
   if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
   if (cd) {
@@ -658,7 +664,9 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
   GB_CUDA(cudaSetDevice(m->ctx->device));
   cudaStream_t st = m->stream;
   // per-evaluation constants in FP64 on the host, uploaded with the parameters
-  affine_consts(m->tparams.data(), m->tfixed.data(), m->moving.p2i, m->moving.origin, *m->h_consts);
+  const bool dense = !m->use_sampled;
+  affine_consts(m->tparams.data(), m->tfixed.data(), m->moving.p2i, m->moving.origin, dense ? m->virt.i2p : nullptr,
+                m->virt.origin, *m->h_consts);
   GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
   int rc = enqueue_eval(m, nullptr, m->d_out.p, deriv);
   if (rc) return rc;
@@ -739,7 +747,7 @@ extern "C" int gb_metric_evaluate_device(gb_metric* m, const double* device_para
   GB_CUDA(cudaSetDevice(m->ctx->device));
   EvalArgs a;
   fill_eval_args(m, a, device_params, device_out, with_derivative != 0);
-  k_prepare_affine<<<1, 1, 0, m->stream>>>(a, m->d_consts.p);
+  k_prepare_affine<<<1, 32, 0, m->stream>>>(a, m->d_consts.p);
   GB_CUDA(cudaGetLastError());
   return enqueue_eval(m, device_params, device_out, with_derivative != 0);
 }
