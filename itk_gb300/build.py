@@ -19,7 +19,10 @@ OBJ_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(OUT_DIR, "libitk_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no FMA contraction (aarch64 g++ contracts a*b+c by default), so host-side
+# FP64 geometry and transform constants round like the reference on every host ISA
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 

@@ -17,6 +17,25 @@ namespace gb {
 
 constexpr int kWarp = 32;
 
+// FP64 multiply / add that are never fused into an FMA: positions computed in
+// FP64 must round exactly like the reference's separate operations (a fused
+// product-sum turns an exact cancellation into a 1e-20 residue, which moves
+// points off exact buffer-edge ties).  Host code is built with -ffp-contract=off.
+__host__ __device__ __forceinline__ double dmul(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+__host__ __device__ __forceinline__ double dadd(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // Kahan-compensated FP32 accumulator (the reference's CompensatedSummation,
 // Core/Common/include/itkCompensatedSummation.hxx:38-48, at FP32).

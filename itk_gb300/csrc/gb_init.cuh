@@ -33,13 +33,16 @@ __device__ __forceinline__ double interp_d(const float* __restrict__ img, const 
   const double v011 = GBPIX(b0[0], b1[1], b1[2]), v111 = GBPIX(b1[0], b1[1], b1[2]);
 #undef GBPIX
   if (d[0] <= 0.0 && d[1] <= 0.0 && d[2] <= 0.0) return v000;
-  const double x00 = v000 + (v100 - v000) * d[0];
-  const double x10 = v010 + (v110 - v010) * d[0];
-  const double x01 = v001 + (v101 - v001) * d[0];
-  const double x11 = v011 + (v111 - v011) * d[0];
-  const double xx0 = x00 + (x10 - x00) * d[1];
-  const double xx1 = x01 + (x11 - x01) * d[1];
-  return xx0 + (xx1 - xx0) * d[2];
+  // a + (b - a) d with separate roundings, as the reference computes it
+#define GBLERP(a, b, t) dadd((a), dmul(dadd((b), -(a)), (t)))
+  const double x00 = GBLERP(v000, v100, d[0]);
+  const double x10 = GBLERP(v010, v110, d[0]);
+  const double x01 = GBLERP(v001, v101, d[0]);
+  const double x11 = GBLERP(v011, v111, d[0]);
+  const double xx0 = GBLERP(x00, x10, d[1]);
+  const double xx1 = GBLERP(x01, x11, d[1]);
+  return GBLERP(xx0, xx1, d[2]);
+#undef GBLERP
 }
 
 struct DGeom {
@@ -52,9 +55,13 @@ struct DGeom {
 __device__ __forceinline__ void d_point_to_cindex(const DGeom& g, const double p[3], double ci[3]) {
   double v[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) v[k] = p[k] - g.origin[k];
+  for (int k = 0; k < 3; ++k) v[k] = dadd(p[k], -g.origin[k]);
 #pragma unroll
-  for (int i = 0; i < 3; ++i) ci[i] = g.p2i[3 * i] * v[0] + g.p2i[3 * i + 1] * v[1] + g.p2i[3 * i + 2] * v[2];
+  for (int i = 0; i < 3; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < 3; ++j) s = dadd(s, dmul(g.p2i[3 * i + j], v[j]));
+    ci[i] = s;
+  }
 }
 
 __device__ __forceinline__ bool d_inside(const DGeom& g, const double ci[3]) {
@@ -70,8 +77,8 @@ __device__ __forceinline__ bool d_nearest_index(const DGeom& g, const double p[3
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     double s = 0.0;
-    for (int j = 0; j < 3; ++j) s += g.p2i[3 * i + j] * (p[j] - g.origin[j]);
-    idx[i] = (int64_t)floor(s + 0.5);
+    for (int j = 0; j < 3; ++j) s = dadd(s, dmul(g.p2i[3 * i + j], dadd(p[j], -g.origin[j])));
+    idx[i] = (int64_t)floor(dadd(s, 0.5));
     if (idx[i] < 0 || idx[i] >= g.n[i]) inside = false;
   }
   return inside;
@@ -148,7 +155,7 @@ __global__ void k_build_samples(BuildArgs b) {
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
       double p = b.virt.origin[r];
-      for (int c = 0; c < 3; ++c) p += b.virt.i2p[3 * r + c] * idx[c];
+      for (int c = 0; c < 3; ++c) p = dadd(p, dmul(b.virt.i2p[3 * r + c], idx[c]));
       vp[r] = p;
     }
   }

@@ -65,7 +65,7 @@ __device__ __forceinline__ float3 jac_vec(const EvalConsts& K, float x, float y,
 // composed with ImageBase::TransformPhysicalPointToContinuousIndex (itkImageBase.h:515-531).
 __host__ __device__ inline void split_df(double x, float& hi, float& lo) {
   hi = (float)x;
-  lo = (float)(x - (double)hi);
+  lo = (float)dadd(x, -(double)hi);
 }
 
 // dom2phys / dom_origin: domain coordinates -> physical point (the virtual
@@ -89,23 +89,23 @@ __host__ __device__ inline void affine_const_entry(int e, const double* p, const
   double Ar[3];
   for (int c = 0; c < 3; ++c) {
     double s = 0.0;
-    for (int k = 0; k < 3; ++k) s += m_p2i[r * 3 + k] * p[k * 3 + c];
+    for (int k = 0; k < 3; ++k) s = dadd(s, dmul(m_p2i[r * 3 + k], p[k * 3 + c]));
     Ar[c] = s;
   }
   if (e < 9) {
     const int c = e % 3;
     double s = 0.0;
-    for (int k = 0; k < 3; ++k) s += Ar[k] * U[k * 3 + c];
+    for (int k = 0; k < 3; ++k) s = dadd(s, dmul(Ar[k], U[k * 3 + c]));
     split_df(s, K.map.Ahi[e], K.map.Alo[e]);
     return;
   }
   double br = 0.0;
   for (int k = 0; k < 3; ++k) {
-    double o = p[9 + k] + center[k];
-    for (int j = 0; j < 3; ++j) o -= p[k * 3 + j] * center[j];
-    br += m_p2i[r * 3 + k] * (o - m_origin[k]);
+    double o = dadd(p[9 + k], center[k]);
+    for (int j = 0; j < 3; ++j) o = dadd(o, -dmul(p[k * 3 + j], center[j]));
+    br = dadd(br, dmul(m_p2i[r * 3 + k], dadd(o, -m_origin[k])));
   }
-  for (int k = 0; k < 3; ++k) br += Ar[k] * u0[k];
+  for (int k = 0; k < 3; ++k) br = dadd(br, dmul(Ar[k], u0[k]));
   split_df(br, K.map.bhi[r], K.map.blo[r]);
 }
 
