@@ -304,9 +304,12 @@ def run_gb300(args):
     peak, peak_src = measured_peak()
     achieved = kbytes / (ktime / 1e3) / 1e9
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(tf):
-        traffic = json.load(open(tf)).get(kname, {}).get("bytes_per_launch")
+    tf = os.path.join(ROOT, "profiles", "traffic.txt")
+    if os.path.exists(tf) and args.size == "256,256,200" and abs(args.fraction - 0.2) < 1e-9:
+        for line in open(tf):
+            parts = line.split()
+            if len(parts) == 2 and parts[0] == kname:
+                traffic = int(parts[1])
     b_alg = roofline.evaluation_bytes(n, v_touched)
     eval_ms = dev_ms / args.steps
     line = {
