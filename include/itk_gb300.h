@@ -173,6 +173,39 @@ int gb_metric_evaluate_device(gb_metric *m, const double *device_params, double 
 /* Synchronize the handle's stream and return the status of the last enqueued evaluation. */
 int gb_metric_synchronize(gb_metric *m);
 
+/* ---- allocation-free MeanSquares --------------------------------------- */
+/* No counterpart in the reference: an extra entry point of this library.
+ *
+ * For callers that cannot call cudaMalloc -- code running inside another
+ * framework's memory pool or arena, real-time loops that forbid allocation
+ * after start-up, hosts that account for every device allocation -- this
+ * evaluates MeanSquares value and derivative under an affine transform
+ * without allocating anything.  The caller passes device pointers to:
+ *   samples  n float4 records (x, y, z, fixed value): virtual-space points
+ *            and the fixed image's value there, 16-byte aligned;
+ *   moving   one float4 per moving voxel (value, gx, gy, gz), x fastest,
+ *            16-byte aligned;
+ *   out      14 doubles: value, number of valid points, derivative[12].
+ * Geometry, the 12 affine parameters and the centre are host arrays.  The
+ * call is asynchronous on `stream` (a cudaStream_t, 0 for the default
+ * stream); when no sample maps inside the moving image, out = [DBL_MAX, 0,
+ * 0...] as VerifyNumberOfValidPoints leaves it.
+ * Scratch: one static device array of GB_NOALLOC_SCRATCH_BYTES bytes that
+ * every GPU loading this library holds until the process exits.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current, so make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other host threads) race; serialize them.
+ * Limits: n <= GB_NOALLOC_MAX_SAMPLES, moving voxels <= GB_NOALLOC_MAX_VOXELS;
+ * larger sizes are rejected with GB_ERR_BAD_ARG. */
+#define GB_NOALLOC_SCRATCH_BYTES 114176
+#define GB_NOALLOC_MAX_SAMPLES 2147483647LL
+#define GB_NOALLOC_MAX_VOXELS 2147483648LL
+int gb_msq_affine_noalloc(const void *device_samples, int64_t n, const void *device_moving,
+                          const int64_t moving_size[3], const double moving_spacing[3],
+                          const double moving_origin[3], const double moving_direction[9],
+                          const double params[12], const double center[3], double *device_out, uint64_t stream);
+
 /* ---- observability ----------------------------------------------------- */
 /* Per-kernel CUDA-event timing of evaluations (the reference's TimeProbe,
  * Core/Common/include/itkTimeProbe.h:44, at kernel granularity).  When on,

@@ -78,6 +78,7 @@ SIGNATURES = {
     "gb_metric_get_stream": [_P, _P],
     "gb_metric_evaluate_device": [_P, _P, _P, _I],
     "gb_metric_synchronize": [_P],
+    "gb_msq_affine_noalloc": [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _U64],
     "gb_metric_set_profiling": [_P, _I],
     "gb_metric_get_kernel_times": [_P, _P, _I, _P],
 }

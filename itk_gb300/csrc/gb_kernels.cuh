@@ -158,6 +158,7 @@ struct EvalArgs {
   int with_derivative;
 };
 
+#ifndef GB_KERNELS_HELPERS_ONLY
 // Device twin of the host constant computation (parameters already in HBM).
 // 13 threads, one output each, so the FP64 dependency chains run side by side.
 __global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
@@ -165,6 +166,8 @@ __global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
     affine_const_entry(threadIdx.x, a.params, a.center, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin,
                        *out);
 }
+
+#endif  // GB_KERNELS_HELPERS_ONLY
 
 __device__ __forceinline__ void load_consts(const EvalConsts* g, EvalConsts& s) {
   const float* src = reinterpret_cast<const float*>(g);
@@ -494,6 +497,7 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
   }
 }
 
+#ifndef GB_KERNELS_HELPERS_ONLY
 // Mattes finalize: one thread per joint-histogram bin.  FP64 normalization and
 // p (log(p/pm) - log pf), with the marginal logs from pass 1's last block, and
 // the FP32 log(p/pm) table for pass 2 (ComputeResults, Mattes...v4.hxx:358-499;
@@ -545,6 +549,9 @@ __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a
   }
 }
 
+#endif  // GB_KERNELS_HELPERS_ONLY
+
+#ifndef GB_KERNELS_HELPERS_ONLY
 // Mattes pass 2, affine: derivative from the cached Parzen terms and gradients.
 __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
   extern __shared__ float pr[];
@@ -603,5 +610,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
     for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = fin[p] * nFactor;
   }
 }
+
+#endif  // GB_KERNELS_HELPERS_ONLY
 
 }  // namespace gb
