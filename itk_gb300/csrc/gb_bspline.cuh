@@ -1,0 +1,327 @@
+// gb_bspline.cuh -- B-spline (order 3) and [affine, B-spline] composite moving transforms.
+//
+// Reference semantics (paths relative to ITK's Modules/):
+//   BSplineTransform::TransformPoint / Jacobian   Core/Transform/include/itkBSplineTransform.hxx:478-652
+//   BSplineInterpolationWeightFunction::Evaluate  Core/Common/include/itkBSplineInterpolationWeightFunction.hxx:43-93
+//   CompositeTransform point and chain rule        Core/Transform/include/itkCompositeTransform.hxx:60-70,466-580
+//
+// Each sample's support (first node, in-cell fractions, valid-region flag) is
+// fixed by its virtual point, so Initialize computes it once in FP64 with the
+// reference's InsideValidRegion rules.  Per evaluation a sample needs the 64
+// tensor weights and the displacement sum over the coefficients (staged in
+// shared memory when they fit).  The Jacobian has 192 nonzeros per sample,
+//   (J^T g)[n_k + d * nper] = W_k (M^T g)_d,
+// M the composite's initial affine (identity for a plain B-spline).  Samples
+// are sorted by B-spline cell; a chunk kernel sums W_k a_s over each run of
+// same-cell samples (one thread per support node), and a gather kernel adds,
+// for every parameter, the chunk sums of the cells whose support holds its
+// node -- in a fixed order, with no atomics.
+#pragma once
+
+#include "gb_kernels.cuh"
+
+namespace gb {
+
+constexpr int kChunkLen = 256;     // samples per chunk (at most)
+constexpr int kChunkThreads = 64;  // one thread per support node
+constexpr int kParamsBlock = 256;  // 8 parameters per block in k_bspline_params
+
+__device__ __forceinline__ void unpack_support(float w, int& sx, int& sy, int& sz, bool& valid) {
+  const unsigned u = __float_as_uint(w);
+  sx = (int)(u & 1023u);
+  sy = (int)((u >> 10) & 1023u);
+  sz = (int)((u >> 20) & 1023u);
+  valid = ((u >> 30) & 1u) != 0u;
+}
+
+// Weights of the 4 nodes along one axis at in-cell position t in [0, 1]:
+// BSplineKernelFunction<3> at t+1, t, t-1, t-2; 1/6 applied as hi + lo parts.
+__device__ __forceinline__ void bspline_basis(float t, float* w) {
+  constexpr float c_hi = 0.16666667163372039795f;  // nearest float to 1/6
+  constexpr float c_lo = -4.96705373e-09f;         // 1/6 - c_hi
+  float w6[4];
+  parzen6(t, w6);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) w[k] = fmaf(w6[k], c_hi, w6[k] * c_lo);
+}
+
+#ifndef GB_KERNELS_HELPERS_ONLY
+// Converts the coefficients to float4 nodes (c_x, c_y, c_z, 0) and writes the
+// transform constants of the initial affine (block 0).
+__global__ void k_prepare_bspline(EvalArgs a, EvalConsts* out) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n < a.nper)
+    a.nodes[n] = make_float4((float)a.params[n], (float)a.params[a.nper + n], (float)a.params[2 * a.nper + n], 0.f);
+  if (blockIdx.x == 0 && threadIdx.x < 13)
+    affine_const_entry(threadIdx.x, a.init_p, a.init_c, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin,
+                       *out);
+}
+#endif  // GB_KERNELS_HELPERS_ONLY
+
+// Shared-memory copy of the nodes when they fit, else the global array.
+__device__ __forceinline__ const float4* stage_nodes(const EvalArgs& a, float4* sh) {
+  if (!a.nodes_smem) return a.nodes;
+  for (int k = threadIdx.x; k < a.nper; k += blockDim.x) sh[k] = __ldcg(a.nodes + k);
+  return sh;
+}
+
+// Moving continuous index of one sample under the B-spline (+ initial affine):
+// cidx = A x + b + P2I M u, A x + b in double-float, the displacement u in FP32.
+// has_jac: inside the B-spline valid region (else the transform is the identity
+// there and its Jacobian is zero, itkBSplineTransform.hxx:519-523,610-616).
+__device__ __forceinline__ DFPos bspline_position(const EvalConsts& K, const float4* nodes, const EvalArgs& a,
+                                                  const float4& s, const float4& su, bool& has_jac) {
+  DFPos p = map_pos(K.map, s.x, s.y, s.z);
+  int sx, sy, sz;
+  bool valid;
+  unpack_support(su.w, sx, sy, sz, valid);
+  has_jac = valid;
+  if (!valid) return p;
+  float wx[4], wy[4], wz[4];
+  bspline_basis(su.x, wx);
+  bspline_basis(su.y, wy);
+  bspline_basis(su.z, wz);
+  float u0 = 0.f, u1 = 0.f, u2 = 0.f;
+#pragma unroll
+  for (int kz = 0; kz < 4; ++kz)
+#pragma unroll
+    for (int ky = 0; ky < 4; ++ky) {
+      const float4* row = nodes + (sx + a.gx * ((sy + ky) + a.gy * (sz + kz)));
+      const float wyz = wy[ky] * wz[kz];
+#pragma unroll
+      for (int kx = 0; kx < 4; ++kx) {
+        const float W = wx[kx] * wyz;
+        const float4 c = row[kx];
+        u0 = fmaf(W, c.x, u0);
+        u1 = fmaf(W, c.y, u1);
+        u2 = fmaf(W, c.z, u2);
+      }
+    }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float corr = fmaf(K.Pm[3 * k], u0, fmaf(K.Pm[3 * k + 1], u1, K.Pm[3 * k + 2] * u2));
+    float hs, he;
+    two_sum(p.hi[k], corr, hs, he);
+    he = __fadd_rn(he, p.lo[k]);
+    p.hi[k] = __fadd_rn(hs, he);
+    p.lo[k] = __fsub_rn(he, __fsub_rn(p.hi[k], hs));
+  }
+  return p;
+}
+
+__device__ __forceinline__ float3 grad_map(const EvalConsts& K, float3 g) {
+  return make_float3(fmaf(K.Mg[0], g.x, fmaf(K.Mg[1], g.y, K.Mg[2] * g.z)),
+                     fmaf(K.Mg[3], g.x, fmaf(K.Mg[4], g.y, K.Mg[5] * g.z)),
+                     fmaf(K.Mg[6], g.x, fmaf(K.Mg[7], g.y, K.Mg[8] * g.z)));
+}
+
+#ifndef GB_KERNELS_HELPERS_ONLY
+// MeanSquares, B-spline: value sum and count; per sample a = 2 (f - m) M^T g in the cache.
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock) k_msq_bspline(EvalArgs a) {
+  extern __shared__ float4 nodes_sh[];
+  __shared__ EvalConsts K;
+  __shared__ float red[kBlock / 32][1];
+  __shared__ double blk[1], fin[1];
+  load_consts(a.consts, K);
+  const float4* nodes = stage_nodes(a, nodes_sh);
+  __syncthreads();
+  KahanF acc[1];
+  acc[0].zero();
+  unsigned nv = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 s = __ldcs(a.samples + i);
+    const float4 su = __ldcs(a.sup + i);
+    bool has_jac;
+    const DFPos p = bspline_position(K, nodes, a, s, su, has_jac);
+    float m;
+    float3 g;
+    float4 cache = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (eval_moving<GRAD>(a, p, a.with_derivative != 0 && has_jac, m, g)) {
+      const float diff = s.w - m;  // MeanSquares...Threader.hxx:46
+      acc[0].add(diff * diff);
+      ++nv;
+      if (has_jac) {
+        const float3 gm = grad_map(K, g);
+        const float t = 2.f * diff;
+        cache = make_float4(t * gm.x, t * gm.y, t * gm.z, 1.f);
+      }
+    }
+    if (a.with_derivative) __stcs(a.cache + i, cache);
+  }
+  block_count(nv, a.acc_n);
+  block_sums<1>(acc, red, blk);
+  if (!grid_sums<1>(blk, a.part, a.grp, a.tickets + kTicketMain, fin)) return;
+  if (threadIdx.x == 0) {
+    const unsigned long long N = __ldcg(a.acc_n);
+    a.out[1] = (double)N;
+    if (N == 0) {
+      a.out[0] = DBL_MAX;
+      *a.status = GB_ERR_NO_VALID_POINTS;
+    } else {
+      a.out[0] = fin[0] / (double)N;
+      *a.status = GB_OK;
+    }
+  }
+}
+
+// Dynamic shared memory of the B-spline Mattes pass 1: histogram, column sums,
+// fixed counts, then (16-byte aligned) the nodes.
+__host__ __device__ inline size_t mattes_bspline_node_offset(int B) {
+  return ((size_t)8 * (B * B + B) + 4 * (size_t)B + 15) / 16 * 16;
+}
+
+// Mattes pass 1, B-spline: as k_mattes_pass1_affine, caching (term, M^T g).
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock) k_mattes_pass1_bspline(EvalArgs a) {
+  extern __shared__ unsigned long long smem_u64[];
+  const int B = a.bins;
+  unsigned long long* hist = smem_u64;
+  unsigned long long* cs = smem_u64 + B * B;
+  unsigned* fm = reinterpret_cast<unsigned*>(smem_u64 + B * B + B);
+  float4* nodes_sh = reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(smem_u64) + mattes_bspline_node_offset(B));
+  __shared__ EvalConsts K;
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) hist[k] = 0ull;
+  for (int k = threadIdx.x; k < B; k += blockDim.x) {
+    fm[k] = 0u;
+    cs[k] = 0ull;
+  }
+  load_consts(a.consts, K);
+  const float4* nodes = stage_nodes(a, nodes_sh);
+  __syncthreads();
+  unsigned nv = 0;
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < a.n; base += stride) {
+    const int64_t i = base + lane;
+    const bool live = i < a.n;
+    const float4 s = live ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    float m = 0.f;
+    float3 g = make_float3(0.f, 0.f, 0.f);
+    bool ok = false, has_jac = false;
+    if (live) {
+      const float4 su = __ldcs(a.sup + i);
+      const DFPos p = bspline_position(K, nodes, a, s, su, has_jac);
+      ok = eval_moving<GRAD>(a, p, a.with_derivative != 0 && has_jac, m, g);
+      ok = ok && !(m < a.mmin) && !(m > a.mmax);  // Mattes...Threader.hxx:238-245
+    }
+    const float term = fmaf(m - a.mmin, a.m_inv_bs, 2.f);
+    if (a.with_derivative && live) {
+      const float3 gm = has_jac ? grad_map(K, g) : make_float3(0.f, 0.f, 0.f);
+      __stcs(a.cache + i, ok ? make_float4(term, gm.x, gm.y, gm.z)
+                             : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f));
+    }
+    int pdfm = 0;
+    unsigned q[4] = {0u, 0u, 0u, 0u};
+    const int fidx = __float_as_int(s.w);
+    if (ok) {
+      float t, w6[4];
+      parzen_window(term, B, pdfm, t);
+      parzen6(t, w6);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) q[k] = (__float2uint_rn(w6[k] * kQScale) + 3u) / 6u;
+    }
+    hist_add_aggregated(ok, fidx * B + pdfm, fidx, q, hist, fm);
+    nv += ok ? 1u : 0u;
+  }
+  mattes_pass1_epilogue(a, nv, hist, cs, fm);
+}
+
+// One block per chunk of same-cell samples; thread t = support node
+// (kx, ky, kz) = (t & 3, (t >> 2) & 3, t >> 4) sums over the chunk
+// W_t(s) a_s, a_s = 2 (f - m) M^T g (MeanSquares) or w(term) M^T g (Mattes,
+// w = sum_k log(p/pm)[f][m_k] beta3'(m_k - term)); compensated FP32.
+template <bool MATTES>
+__global__ void __launch_bounds__(kChunkThreads) k_bspline_chunks(EvalArgs a) {
+  __shared__ float W1[kChunkLen][12];
+  __shared__ float4 AV[kChunkLen];
+  const int4 ch = a.chunks[blockIdx.x];
+  const int len = ch.y - ch.x;
+  const int B = a.bins;
+  for (int j = threadIdx.x; j < len; j += kChunkThreads) {
+    const int64_t i = (int64_t)ch.x + j;
+    const float4 su = __ldg(a.sup + i);
+    const float4 c = __ldcg(a.cache + i);
+    float4 av = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (MATTES) {
+      if (c.x == c.x) {
+        int pdfm;
+        float t, d[4];
+        parzen_window(c.x, B, pdfm, t);
+        parzen_deriv(t, d);
+        const float* row = a.pratio + __float_as_int(__ldg(&a.samples[i].w)) * B + pdfm;
+        const float w = __ldcg(row) * d[0] + __ldcg(row + 1) * d[1] + __ldcg(row + 2) * d[2] + __ldcg(row + 3) * d[3];
+        av = make_float4(w * c.y, w * c.z, w * c.w, 0.f);
+      }
+    } else {
+      av = make_float4(c.x, c.y, c.z, 0.f);
+    }
+    bspline_basis(su.x, &W1[j][0]);
+    bspline_basis(su.y, &W1[j][4]);
+    bspline_basis(su.z, &W1[j][8]);
+    AV[j] = av;
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int kx = t & 3, ky = (t >> 2) & 3, kz = t >> 4;
+  KahanF s0, s1, s2;
+  s0.zero();
+  s1.zero();
+  s2.zero();
+  for (int j = 0; j < len; ++j) {
+    const float W = W1[j][kx] * W1[j][4 + ky] * W1[j][8 + kz];
+    const float4 v = AV[j];
+    s0.add(W * v.x);
+    s1.add(W * v.y);
+    s2.add(W * v.z);
+  }
+  float* out = a.chunk_part + (size_t)blockIdx.x * 192;
+  out[t] = s0.value();
+  out[64 + t] = s1.value();
+  out[128 + t] = s2.value();
+}
+
+// One warp per parameter (node n, dimension d): FP64 sum, in a fixed order, of
+// the chunk sums of every cell whose 4x4x4 support holds node n; then the
+// metric's scale (1/N for MeanSquares, -1/(binsize N) for Mattes,
+// MeanSquares...Threader.hxx:71-79, Mattes...Threader.hxx:446-457).
+template <bool MATTES>
+__global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long N = __ldcg(a.acc_n);
+  const int st = __ldcg(a.status);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.out[1] = (double)N;
+    if (MATTES) a.out[0] = st == GB_OK ? __ldcg(a.final_value) : 0.0;
+  }
+  if (gw >= 3 * a.nper) return;
+  const int d = gw / a.nper, n = gw - d * a.nper;
+  const int ix = n % a.gx, iy = (n / a.gx) % a.gy, iz = n / (a.gx * a.gy);
+  // cells (first support node) c with c <= i <= c + 3 and 0 <= c <= g - 4
+  const int cx0 = max(0, ix - 3), cx1 = min(ix, a.gx - 4);
+  const int cy0 = max(0, iy - 3), cy1 = min(iy, a.gy - 4);
+  const int cz0 = max(0, iz - 3), cz1 = min(iz, a.gz - 4);
+  const int ncx = cx1 - cx0 + 1, ncy = cy1 - cy0 + 1, ncz = cz1 - cz0 + 1;
+  double s = 0.0;
+  if (ncx > 0 && ncy > 0 && ncz > 0) {
+    for (int c = lane; c < ncx * ncy * ncz; c += 32) {
+      const int cx = cx0 + c % ncx, cy = cy0 + (c / ncx) % ncy, cz = cz0 + c / (ncx * ncy);
+      const int cell = 1 + cx + a.gx * (cy + a.gy * cz);
+      const int k = (ix - cx) + 4 * (iy - cy) + 16 * (iz - cz);
+      const int q1 = __ldg(a.cell_first + cell + 1);
+      for (int q = __ldg(a.cell_first + cell); q < q1; ++q)
+        s += (double)__ldcg(a.chunk_part + (size_t)q * 192 + d * 64 + k);
+    }
+  }
+  s = warp_sum_d(s);
+  if (lane == 0) {
+    double scale = 0.0;
+    if (st == GB_OK && N > 0) scale = MATTES ? -1.0 / (a.m_bs * (double)N) : 1.0 / (double)N;
+    a.out[2 + gw] = s * scale;
+  }
+}
+#endif  // GB_KERNELS_HELPERS_ONLY
+
+}  // namespace gb

@@ -101,8 +101,7 @@ struct BuildArgs {
   uint64_t* keys;
   uint32_t* vals;
   float4* recs;
-  int4* bsp;
-  float4* bspf;
+  float4* sup;  // B-spline support record per candidate (null without a B-spline)
   unsigned long long* nvalid;
 };
 
@@ -174,24 +173,32 @@ __global__ void k_build_samples(BuildArgs b) {
     else if (p > b.bins - 3) p = b.bins - 3;
     aux = __int_as_float((int)p);
   }
-  // B-spline support of the virtual point: start index, cell and fractions
-  int4 sup = make_int4(0, 0, 0, 0);
-  float4 fr = make_float4(0.f, 0.f, 0.f, 0.f);
+  // B-spline support of the virtual point (BSplineTransform::TransformPoint,
+  // itkBSplineTransform.hxx:510-591): in-cell positions t = ci - start - 1 in
+  // [0, 1] and the start node packed as sx | sy << 10 | sz << 20 | valid << 30;
+  // cell = 1 + start's linear node index (0: outside the valid region).
+  float4 sup = make_float4(0.f, 0.f, 0.f, 0.f);
   uint64_t cell = 0;
   if (ok && b.bspline) {
     double ci[3], v[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) v[k] = vp[k] - b.g_origin[k];
+    for (int k = 0; k < 3; ++k) v[k] = dadd(vp[k], -b.g_origin[k]);
 #pragma unroll
-    for (int r = 0; r < 3; ++r) ci[r] = b.g_p2i[3 * r] * v[0] + b.g_p2i[3 * r + 1] * v[1] + b.g_p2i[3 * r + 2] * v[2];
+    for (int r = 0; r < 3; ++r) {
+      double s = 0.0;
+      for (int j = 0; j < 3; ++j) s = dadd(s, dmul(b.g_p2i[3 * r + j], v[j]));
+      ci[r] = s;
+    }
     if (d_bspline_inside(b.grid, ci)) {
       int st[3];
+      float t[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        st[k] = (int)floor(ci[k] + 0.5 - 1.5);  // BSplineInterpolationWeightFunction start index
+        st[k] = (int)floor(dadd(dadd(ci[k], 0.5), -1.5));  // BSplineInterpolationWeightFunction start index
+        t[k] = (float)dadd(dadd(ci[k], -(double)st[k]), -1.0);
       }
-      sup = make_int4(st[0], st[1], st[2], 1);
-      fr = make_float4((float)(ci[0] - st[0]), (float)(ci[1] - st[1]), (float)(ci[2] - st[2]), 1.f);
+      const unsigned packed = (unsigned)st[0] | ((unsigned)st[1] << 10) | ((unsigned)st[2] << 20) | (1u << 30);
+      sup = make_float4(t[0], t[1], t[2], __uint_as_float(packed));
       cell = 1 + (uint64_t)st[0] + (uint64_t)b.grid[0] * ((uint64_t)st[1] + (uint64_t)b.grid[1] * (uint64_t)st[2]);
     }
   }
@@ -211,23 +218,17 @@ __global__ void k_build_samples(BuildArgs b) {
   if (b.points) b.recs[i] = make_float4((float)vp[0], (float)vp[1], (float)vp[2], aux);
   else b.recs[i] = make_float4((float)(i % b.virt.n[0]), (float)((i / b.virt.n[0]) % b.virt.n[1]),
                                (float)(i / (b.virt.n[0] * b.virt.n[1])), aux);
-  if (b.bsp) {
-    b.bsp[i] = sup;
-    b.bspf[i] = fr;
-  }
+  if (b.sup) b.sup[i] = sup;
 }
 
 __global__ void k_gather_samples(const uint32_t* __restrict__ perm, int64_t n, const float4* __restrict__ recs,
-                                 float4* __restrict__ out, const int4* __restrict__ bsp_in, int4* __restrict__ bsp_out,
-                                 const float4* __restrict__ bspf_in, float4* __restrict__ bspf_out) {
+                                 float4* __restrict__ out, const float4* __restrict__ sup_in,
+                                 float4* __restrict__ sup_out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t j = perm[i];
   out[i] = recs[j];
-  if (bsp_out) {
-    bsp_out[i] = bsp_in[j];
-    bspf_out[i] = bspf_in[j];
-  }
+  if (sup_out) sup_out[i] = sup_in[j];
 }
 
 // min / max over a float buffer (ordered-int atomics): out[0] = min, out[1] = max

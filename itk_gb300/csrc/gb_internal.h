@@ -94,15 +94,17 @@ struct gb_metric {
   gb::DevBuf<float4> d_mov4;     // packed moving image: (value, gx, gy, gz)
   gb::DevBuf<float4> d_samples;  // (x, y, z, fixed value | fixed Parzen bin)
   gb::DevBuf<float4> d_cache;    // per-sample pass-1 result for the derivative pass
-  gb::DevBuf<int4> d_bsp;        // per-sample B-spline support: start index, cell
-  gb::DevBuf<float4> d_bspf;     // per-sample B-spline fractions (fx, fy, fz, valid)
-  gb::DevBuf<int64_t> d_cell_chunks;  // [chunk] -> begin sample of a same-cell chunk
-  int64_t ncell_chunks = 0;
+  gb::DevBuf<float4> d_sup;      // per-sample B-spline support (tx, ty, tz, packed start | valid)
+  gb::DevBuf<int4> d_chunks;     // (first sample, end sample, cell, 0) of same-cell sample runs
+  gb::DevBuf<int> d_cell_first;  // first chunk of each B-spline cell, cells 0 .. nper + 1
+  gb::DevBuf<float> d_chunk_part;  // nchunks x 192 Jacobian partial sums
+  gb::DevBuf<float4> d_nodes;    // B-spline coefficients as float4 nodes
+  int64_t nchunks = 0;
+  int grid[3] = {0, 0, 0};       // B-spline control grid
   double mstate[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
   // evaluation buffers
   gb::DevBuf<double> d_params;
-  gb::DevBuf<double> d_coeff_f;  // spare
   gb::DevBuf<unsigned char> d_acc;  // accumulators, cleared per evaluation
   size_t acc_bytes = 0;
   gb::DevBuf<double> d_scratch;     // per-block / per-group partials, overwritten per evaluation

@@ -53,6 +53,8 @@ struct EvalConsts {
   AffineDF map;
   float U[9];
   float joff[3];
+  float Mg[9];  // B-spline paths: gradient -> (M^T g), M the initial affine of a composite (identity otherwise)
+  float Pm[9];  // B-spline paths: physical displacement -> moving index offset, P2I M
 };
 
 __device__ __forceinline__ float3 jac_vec(const EvalConsts& K, float x, float y, float z) {
@@ -83,6 +85,13 @@ __host__ __device__ inline void affine_const_entry(int e, const double* p, const
   if (e == 12) {
     for (int i = 0; i < 9; ++i) K.U[i] = (float)U[i];
     for (int i = 0; i < 3; ++i) K.joff[i] = (float)(u0[i] - center[i]);
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) {
+        K.Mg[r * 3 + c] = (float)p[c * 3 + r];  // M^T
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s = dadd(s, dmul(m_p2i[r * 3 + k], p[k * 3 + c]));
+        K.Pm[r * 3 + c] = (float)s;
+      }
     return;
   }
   const int r = e < 9 ? e / 3 : e - 9;
@@ -156,6 +165,17 @@ struct EvalArgs {
   double* out;                  // [value, nvalid, derivative...]
   int* status;
   int with_derivative;
+  // B-spline / composite transforms
+  const float4* __restrict__ sup;    // per sample: (tx, ty, tz, packed support start | valid << 30)
+  float4* nodes;                     // coefficient nodes (cx, cy, cz, 0), written by k_prepare_bspline
+  int gx, gy, gz, nper;
+  int nodes_smem;                    // evaluation kernels stage the nodes in shared memory
+  double init_p[12];                 // initial affine of a composite (identity for a plain B-spline)
+  double init_c[3];
+  const int4* __restrict__ chunks;   // (first sample, end sample, cell id, 0) of same-cell sample runs
+  int nchunks;
+  const int* __restrict__ cell_first;  // first chunk of each cell id; cell ids 1 .. gx*gy*gz
+  float* chunk_part;                 // nchunks x 192 per-chunk Jacobian partial sums
 };
 
 #ifndef GB_KERNELS_HELPERS_ONLY
@@ -403,6 +423,53 @@ __device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, 
   }
 }
 
+// End of Mattes pass 1 (any transform): flush the block histogram, marginals and
+// count; the last block computes the marginal logs.
+__device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigned nv, unsigned long long* hist,
+                                                      unsigned long long* cs, unsigned* fm) {
+  const int B = a.bins;
+  __syncthreads();
+  // flush the nonzero bins; the block's column sums ride along as shared atomics
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) {
+    const unsigned long long h = hist[k];
+    if (h) {
+      atomicAdd(&a.hist[k], h);
+      atomicAdd(&cs[k % B], h);
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < B; k += blockDim.x) {
+    const unsigned c = fm[k];
+    if (c) atomicAdd(&a.fmarg[k], (unsigned long long)c);
+    if (cs[k]) atomicAdd(&a.colsum[k], cs[k]);
+  }
+  block_count(nv, a.acc_n);
+  if (!last_block(a.tickets + kTicketPass1)) return;
+  // Last block: marginal logs once, in FP64, for the finalize.  With T the
+  // (fixed-point) joint-histogram total, p = h / T, pm = colsum / T and
+  // pf = count 2^26 / T, so log(p / pm) = log h - log colsum and
+  // log pf = log count + 26 ln 2 - log T.
+  __shared__ unsigned long long tot_sh;
+  if (threadIdx.x == 0) tot_sh = 0ull;
+  __syncthreads();
+  unsigned long long t = 0ull;
+  for (int k = threadIdx.x; k < B; k += blockDim.x) t += __ldcg(&a.colsum[k]);
+  atomicAdd(&tot_sh, t);
+  __syncthreads();
+  const double T = (double)tot_sh;
+  const double logT = T > 0.0 ? log(T) : 0.0;
+  for (int k = threadIdx.x; k < B; k += blockDim.x) {
+    const double c = (double)__ldcg(&a.colsum[k]);
+    a.logcol[k] = c > 0.0 ? log(c) : 0.0;
+    const double n = (double)__ldcg(&a.fmarg[k]);
+    a.logrow[k] = n > 0.0 ? log(n) + 26.0 * 0.69314718055994530942 - logT : 0.0;
+  }
+  if (threadIdx.x == 0) {
+    a.marg[0] = T;                         // fixed-point total
+    a.marg[1] = T > 0.0 ? 1.0 / T : 0.0;   // normalization factor (of the fixed-point histogram)
+  }
+}
+
 template <int GRAD>
 __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
   extern __shared__ unsigned long long smem_u64[];
@@ -455,46 +522,7 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
     hist_add_aggregated(ok, fidx * B + pdfm, fidx, q, hist, fm);
     nv += ok ? 1u : 0u;
   }
-  __syncthreads();
-  // flush the nonzero bins; the block's column sums ride along as shared atomics
-  for (int k = threadIdx.x; k < B * B; k += blockDim.x) {
-    const unsigned long long h = hist[k];
-    if (h) {
-      atomicAdd(&a.hist[k], h);
-      atomicAdd(&cs[k % B], h);
-    }
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < B; k += blockDim.x) {
-    const unsigned c = fm[k];
-    if (c) atomicAdd(&a.fmarg[k], (unsigned long long)c);
-    if (cs[k]) atomicAdd(&a.colsum[k], cs[k]);
-  }
-  block_count(nv, a.acc_n);
-  if (!last_block(a.tickets + kTicketPass1)) return;
-  // Last block: marginal logs once, in FP64, for the finalize.  With T the
-  // (fixed-point) joint-histogram total, p = h / T, pm = colsum / T and
-  // pf = count 2^26 / T, so log(p / pm) = log h - log colsum and
-  // log pf = log count + 26 ln 2 - log T.
-  __shared__ unsigned long long tot_sh;
-  if (threadIdx.x == 0) tot_sh = 0ull;
-  __syncthreads();
-  unsigned long long t = 0ull;
-  for (int k = threadIdx.x; k < B; k += blockDim.x) t += __ldcg(&a.colsum[k]);
-  atomicAdd(&tot_sh, t);
-  __syncthreads();
-  const double T = (double)tot_sh;
-  const double logT = T > 0.0 ? log(T) : 0.0;
-  for (int k = threadIdx.x; k < B; k += blockDim.x) {
-    const double c = (double)__ldcg(&a.colsum[k]);
-    a.logcol[k] = c > 0.0 ? log(c) : 0.0;
-    const double n = (double)__ldcg(&a.fmarg[k]);
-    a.logrow[k] = n > 0.0 ? log(n) + 26.0 * 0.69314718055994530942 - logT : 0.0;
-  }
-  if (threadIdx.x == 0) {
-    a.marg[0] = T;                         // fixed-point total
-    a.marg[1] = T > 0.0 ? 1.0 / T : 0.0;   // normalization factor (of the fixed-point histogram)
-  }
+  mattes_pass1_epilogue(a, nv, hist, cs, fm);
 }
 
 #ifndef GB_KERNELS_HELPERS_ONLY

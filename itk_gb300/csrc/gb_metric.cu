@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "gb_bspline.cuh"
 #include "gb_init.cuh"
 #include "gb_internal.h"
 #include "gb_kernels.cuh"
@@ -110,6 +111,18 @@ static int full_wave(const gb_metric* m, K kernel, size_t smem, int64_t n) {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, smem) != cudaSuccess || per_sm < 1)
     per_sm = 2;
   return grid_for(m, n, per_sm);
+}
+
+static bool is_bspline(const gb_metric* m) {
+  return m->tkind == GB_TRANSFORM_BSPLINE || m->tkind == GB_TRANSFORM_COMPOSITE;
+}
+
+// Dynamic shared memory of the evaluation kernels' B-spline nodes: staged when
+// they leave room for at least two resident blocks per SM, else read from HBM/L2.
+static size_t bspline_node_bytes(const gb_metric* m) { return (size_t)m->nper * sizeof(float4); }
+static bool nodes_in_smem(const gb_metric* m) {
+  const size_t base = m->kind == GB_METRIC_MATTES ? mattes_bspline_node_offset((int)m->bins) : 0;
+  return base + bspline_node_bytes(m) <= 96 * 1024;
 }
 
 }  // namespace gb
@@ -369,7 +382,20 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     return fail(GB_ERR_BAD_ARG, "gradient source is a gradient image but none was set");
   if (m->grad_source == GB_GRADIENT_RECURSIVE_GAUSSIAN)
     return fail(GB_ERR_UNSUPPORTED, "device recursive-Gaussian gradient is not available in this build");
-  if (m->tkind != GB_TRANSFORM_AFFINE) return fail(GB_ERR_UNSUPPORTED, "only the affine transform is available in this build");
+  const bool bspline = is_bspline(m);
+  double g_p2i[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (bspline) {
+    // BSplineTransform fixed parameters: grid size, origin, spacing, direction (itkBSplineTransform.hxx:243-283)
+    const double* f = m->tfixed.data();
+    double i2p[9];
+    for (int i = 0; i < 3; ++i) {
+      if (f[i] > 1024.0) return fail(GB_ERR_UNSUPPORTED, "B-spline grids above 1024 nodes per axis are not supported");
+      m->grid[i] = (int)f[i];
+    }
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) i2p[r * 3 + c] = f[9 + r * 3 + c] * f[6 + c];
+    if (inv3(i2p, g_p2i) != GB_OK) return fail(GB_ERR_BAD_ARG, "B-spline grid direction * spacing is singular");
+  }
   GB_CUDA(cudaSetDevice(m->ctx->device));
   m->initialized = false;
   cudaStream_t st = m->stream;
@@ -460,12 +486,20 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   b.bins = (int)m->bins;
   b.f_bs = m->mstate[4];
   b.f_normmin = m->mstate[6];
-  b.bspline = 0;
+  b.bspline = bspline ? 1 : 0;
+  DevBuf<float4> sup;
+  if (bspline) {
+    GB_CUDA(sup.alloc(ncand));
+    for (int i = 0; i < 3; ++i) {
+      b.grid[i] = m->grid[i];
+      b.g_origin[i] = m->tfixed[3 + i];
+    }
+    for (int i = 0; i < 9; ++i) b.g_p2i[i] = g_p2i[i];
+  }
   b.keys = keys.p;
   b.vals = vals.p;
   b.recs = recs.p;
-  b.bsp = nullptr;
-  b.bspf = nullptr;
+  b.sup = bspline ? sup.p : nullptr;
   b.nvalid = d_nvalid.p;
   k_build_samples<<<(unsigned)((ncand + kBlock - 1) / kBlock), kBlock, 0, st>>>(b);
   GB_CUDA(cudaGetLastError());
@@ -476,10 +510,50 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   m->nsamples = (int64_t)nvalid;
   m->d_samples.reset();
   GB_CUDA(m->d_samples.alloc(std::max<int64_t>(1, m->nsamples)));
+  m->d_sup.reset();
+  if (bspline) GB_CUDA(m->d_sup.alloc(std::max<int64_t>(1, m->nsamples)));
   if (m->nsamples > 0)
     k_gather_samples<<<(unsigned)((m->nsamples + kBlock - 1) / kBlock), kBlock, 0, st>>>(
-        vals_sorted.p, m->nsamples, recs.p, m->d_samples.p, nullptr, nullptr, nullptr, nullptr);
+        vals_sorted.p, m->nsamples, recs.p, m->d_samples.p, bspline ? sup.p : nullptr,
+        bspline ? m->d_sup.p : nullptr);
   GB_CUDA(cudaGetLastError());
+
+  // ---- B-spline: runs of same-cell samples (at most kChunkLen each) for the
+  // derivative's per-cell reduction, and each cell's first run
+  m->nchunks = 0;
+  if (bspline) {
+    std::vector<uint64_t> hk((size_t)m->nsamples);
+    if (m->nsamples > 0)
+      GB_CUDA(cudaMemcpyAsync(hk.data(), keys_sorted.p, sizeof(uint64_t) * m->nsamples, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    std::vector<int4> chunks;
+    std::vector<int> cell_first((size_t)m->nper + 2, 0);
+    for (int64_t i = 0; i < m->nsamples;) {
+      const uint64_t cell = hk[i] >> 36;
+      int64_t j = i + 1;
+      while (j < m->nsamples && (hk[j] >> 36) == cell && j - i < kChunkLen) ++j;
+      if (cell > 0) {
+        chunks.push_back(make_int4((int)i, (int)j, (int)cell, 0));
+        ++cell_first[cell + 1];
+      }
+      i = j;
+    }
+    for (size_t c = 1; c < cell_first.size(); ++c) cell_first[c] += cell_first[c - 1];
+    m->nchunks = (int64_t)chunks.size();
+    m->d_chunks.reset();
+    m->d_cell_first.reset();
+    m->d_chunk_part.reset();
+    GB_CUDA(m->d_chunks.alloc(std::max<size_t>(1, chunks.size())));
+    GB_CUDA(m->d_cell_first.alloc(cell_first.size()));
+    GB_CUDA(m->d_chunk_part.alloc(std::max<size_t>(1, chunks.size()) * 192));
+    if (!chunks.empty())
+      GB_CUDA(cudaMemcpyAsync(m->d_chunks.p, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(m->d_cell_first.p, cell_first.data(), sizeof(int) * cell_first.size(),
+                            cudaMemcpyHostToDevice, st));
+    m->d_nodes.reset();
+    GB_CUDA(m->d_nodes.alloc((size_t)m->nper));
+    GB_CUDA(cudaStreamSynchronize(st));  // the host vectors die here
+  }
 
   // ---- moving image: packed (value, gradient) for the gradient-image path
   if (m->grad_source == GB_GRADIENT_IMAGE) {
@@ -507,9 +581,9 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     m->d_pdf.reset();
     GB_CUDA(m->d_pdf.alloc((size_t)(m->bins * m->bins)));
     GB_CUDA(cudaMemsetAsync(m->d_pdf.p, 0, sizeof(double) * m->bins * m->bins, st));
-    m->d_cache.reset();
-    GB_CUDA(m->d_cache.alloc(std::max<int64_t>(1, m->nsamples)));
   }
+  m->d_cache.reset();
+  if (m->kind == GB_METRIC_MATTES || bspline) GB_CUDA(m->d_cache.alloc(std::max<int64_t>(1, m->nsamples)));
   if (m->h_params) cudaFreeHost(m->h_params);
   if (m->h_out) cudaFreeHost(m->h_out);
   m->h_params = nullptr;
@@ -574,6 +648,75 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.out = d_out;
   a.status = m->d_status.p;
   a.with_derivative = deriv ? 1 : 0;
+  if (is_bspline(m)) {
+    a.sup = m->d_sup.p;
+    a.nodes = m->d_nodes.p;
+    a.gx = m->grid[0];
+    a.gy = m->grid[1];
+    a.gz = m->grid[2];
+    a.nper = (int)m->nper;
+    a.nodes_smem = nodes_in_smem(m) ? 1 : 0;
+    // initial affine of the composite ([affine, B-spline] queue: B-spline applied first), else identity
+    const double I[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+    const bool comp = m->tkind == GB_TRANSFORM_COMPOSITE;
+    for (int i = 0; i < 12; ++i) a.init_p[i] = comp ? m->tfixed[18 + i] : I[i];
+    for (int i = 0; i < 3; ++i) a.init_c[i] = comp ? m->tfixed[30 + i] : 0.0;
+    a.chunks = m->d_chunks.p;
+    a.nchunks = (int)m->nchunks;
+    a.cell_first = m->d_cell_first.p;
+    a.chunk_part = m->d_chunk_part.p;
+  }
+}
+
+// Grid-stride evaluation kernel with `smem` bytes of dynamic shared memory, one full wave.
+template <typename K>
+static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalArgs& a) {
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kernel<<<full_wave(m, kernel, smem, m->nsamples), kBlock, smem, m->stream>>>(a);
+  return cudaGetLastError();
+}
+
+// B-spline / composite evaluation: node conversion, the per-sample pass
+// (MeanSquares, or Mattes pass 1 + finalize), then with the derivative the
+// per-chunk and per-parameter reductions.
+static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool deriv) {
+  cudaStream_t st = m->stream;
+  const int nper = (int)m->nper;
+  k_prepare_bspline<<<(nper + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, m->d_consts.p);
+  GB_CUDA(cudaGetLastError());
+  m->mark();
+  const size_t nb = a.nodes_smem ? bspline_node_bytes(m) : 0;
+  const bool mattes = m->kind == GB_METRIC_MATTES;
+  if (!mattes) {
+    GB_CUDA(cd ? launch_wave(m, k_msq_bspline<kGradCentralDifference>, nb, a)
+               : launch_wave(m, k_msq_bspline<kGradImage>, nb, a));
+    m->mark();
+  } else {
+    const int B = (int)m->bins;
+    const size_t sh1 = mattes_bspline_node_offset(B) + nb;
+    if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
+    GB_CUDA(cd ? launch_wave(m, k_mattes_pass1_bspline<kGradCentralDifference>, sh1, a)
+               : launch_wave(m, k_mattes_pass1_bspline<kGradImage>, sh1, a));
+    m->mark();
+    k_mattes_finalize<<<(B * B + kFinalizeThreads - 1) / kFinalizeThreads, kFinalizeThreads, 0, st>>>(a);
+    GB_CUDA(cudaGetLastError());
+    m->mark();
+  }
+  if (!deriv) return GB_OK;
+  if (m->nchunks > 0) {
+    if (mattes) k_bspline_chunks<true><<<(unsigned)m->nchunks, kChunkThreads, 0, st>>>(a);
+    else k_bspline_chunks<false><<<(unsigned)m->nchunks, kChunkThreads, 0, st>>>(a);
+    GB_CUDA(cudaGetLastError());
+    m->mark();
+  }
+  const int64_t threads = (int64_t)3 * nper * 32;
+  const unsigned pblocks = (unsigned)((threads + kParamsBlock - 1) / kParamsBlock);
+  if (mattes) k_bspline_params<true><<<pblocks, kParamsBlock, 0, st>>>(a);
+  else k_bspline_params<false><<<pblocks, kParamsBlock, 0, st>>>(a);
+  GB_CUDA(cudaGetLastError());
+  m->mark();
+  return GB_OK;
 }
 
 // Enqueues one evaluation; results land in d_out = [value, nvalid, derivative...].
@@ -594,6 +737,7 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   const bool cd = m->grad_source == GB_GRADIENT_CENTRAL_DIFFERENCE;
   m->nevents = 0;
   m->mark();
+  if (is_bspline(m)) return enqueue_eval_bspline(m, a, cd, deriv);
   if (m->kind == GB_METRIC_MEAN_SQUARES) {
     if (cd) {
       k_msq_affine<kGradCentralDifference>
@@ -663,12 +807,20 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
   if (deriv && (size_t)nparams != P) return fail(GB_ERR_BAD_ARG, "derivative size must equal the number of parameters");
   GB_CUDA(cudaSetDevice(m->ctx->device));
   cudaStream_t st = m->stream;
-  // per-evaluation constants in FP64 on the host, uploaded with the parameters
-  const bool dense = !m->use_sampled;
-  affine_consts(m->tparams.data(), m->tfixed.data(), m->moving.p2i, m->moving.origin, dense ? m->virt.i2p : nullptr,
-                m->virt.origin, *m->h_consts);
-  GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
-  int rc = enqueue_eval(m, nullptr, m->d_out.p, deriv);
+  const double* d_params = nullptr;
+  if (is_bspline(m)) {
+    // B-spline coefficients go to the device; k_prepare_bspline converts them there
+    std::copy(m->tparams.begin(), m->tparams.end(), m->h_params);
+    GB_CUDA(cudaMemcpyAsync(m->d_params.p, m->h_params, sizeof(double) * P, cudaMemcpyHostToDevice, st));
+    d_params = m->d_params.p;
+  } else {
+    // per-evaluation constants in FP64 on the host, uploaded with the parameters
+    const bool dense = !m->use_sampled;
+    affine_consts(m->tparams.data(), m->tfixed.data(), m->moving.p2i, m->moving.origin, dense ? m->virt.i2p : nullptr,
+                  m->virt.origin, *m->h_consts);
+    GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
+  }
+  int rc = enqueue_eval(m, d_params, m->d_out.p, deriv);
   if (rc) return rc;
   GB_CUDA(cudaMemcpyAsync(m->h_out, m->d_out.p, sizeof(double) * (2 + (deriv ? P : 0)), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaMemcpyAsync(m->h_status, m->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -747,8 +899,10 @@ extern "C" int gb_metric_evaluate_device(gb_metric* m, const double* device_para
   GB_CUDA(cudaSetDevice(m->ctx->device));
   EvalArgs a;
   fill_eval_args(m, a, device_params, device_out, with_derivative != 0);
-  k_prepare_affine<<<1, 32, 0, m->stream>>>(a, m->d_consts.p);
-  GB_CUDA(cudaGetLastError());
+  if (!is_bspline(m)) {  // the B-spline path converts its parameters inside enqueue_eval
+    k_prepare_affine<<<1, 32, 0, m->stream>>>(a, m->d_consts.p);
+    GB_CUDA(cudaGetLastError());
+  }
   return enqueue_eval(m, device_params, device_out, with_derivative != 0);
 }
 

@@ -20,7 +20,7 @@ from __future__ import annotations
 import numpy as np
 
 from .image import GradientImage, Image
-from .transforms import AffineTransform
+from .transforms import AffineTransform, BSplineTransform, CompositeTransform
 
 
 def blob_volume(size_xyz, seed, n_blobs=12, noise_sigma=2.0, spacing=(1.0, 1.0, 1.0)):
@@ -140,6 +140,40 @@ def dense_points(image: Image):
     idx = np.arange(nx * ny * nz)
     ijk = np.stack([idx % nx, (idx // nx) % ny, idx // (nx * ny)], axis=1).astype(np.float64)
     return (ijk @ image.index_to_physical().T + image.origin).astype(np.float32)
+
+
+def bspline_over_image(image: Image, mesh_size):
+    """BSplineTransform (order 3) whose transform domain is the image's physical extent
+    (origin, spacing * (size - 1), direction), as BSplineTransformInitializer sets it up."""
+    T = BSplineTransform()
+    size = np.asarray(image.GetSize(), np.float64)
+    T.SetTransformDomain(image.origin, image.spacing * (size - 1.0), mesh_size, image.direction)
+    return T
+
+
+def random_bspline_coefficients(T: BSplineTransform, seed, max_disp=4.0):
+    """Uniform coefficients with |c| <= max_disp / sqrt(3) per component: the cubic B-spline weights are a
+    nonnegative partition of unity, so every displacement vector is at most max_disp long."""
+    rng = np.random.default_rng(seed)
+    T.SetParameters(rng.uniform(-1.0, 1.0, size=T.GetNumberOfParameters()) * (max_disp / np.sqrt(3.0)))
+    return T
+
+
+def pair_bspline(size_xyz, mesh_size=(8, 8, 8), instance=0, max_disp=4.0, multimodal_map=True, config=2):
+    """(fixed, moving, affine, B-spline) of the B-spline config: the blob volume; the moving image is the
+    fixed one resampled under the composite [affine, B-spline] (B-spline applied first) with a seeded
+    smooth displacement (at most max_disp mm), then the multimodal intensity map."""
+    seed = 1000 * config + instance
+    fixed = blob_volume(size_xyz, seed)
+    A = random_affine(seed + 1, fixed.physical_center())
+    B = random_bspline_coefficients(bspline_over_image(fixed, mesh_size), seed + 4, max_disp)
+    C = CompositeTransform()
+    C.AddTransform(A)
+    C.AddTransform(B)
+    moving = resample(fixed, C, seed_noise=seed + 2, noise_sigma=0.0 if multimodal_map else 2.0)
+    if multimodal_map:
+        moving = multimodal(moving, seed + 3)
+    return fixed, moving, A, B
 
 
 def pair_affine(size_xyz, config, instance=0, multimodal_map=False):
