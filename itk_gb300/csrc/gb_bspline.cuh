@@ -22,8 +22,7 @@
 
 namespace gb {
 
-constexpr int kChunkLen = 256;     // samples per chunk (at most)
-constexpr int kChunkThreads = 64;  // one thread per support node
+constexpr int kChunkLen = 256;     // samples per chunk (at most); also the chunk kernel's block size
 constexpr int kParamsBlock = 256;  // 8 parameters per block in k_bspline_params
 
 __device__ __forceinline__ void unpack_support(float w, int& sx, int& sy, int& sz, bool& valid) {
@@ -45,23 +44,27 @@ __device__ __forceinline__ void bspline_basis(float t, float* w) {
   for (int k = 0; k < 4; ++k) w[k] = fmaf(w6[k], c_hi, w6[k] * c_lo);
 }
 
+// One coefficient node (c_x, c_y, c_z, 0) from the FP64 parameters
+// (BSplineTransform's parameter layout: all x coefficients, then y, then z).
+__device__ __forceinline__ float4 node_from_params(const double* __restrict__ p, int nper, int n) {
+  return make_float4((float)__ldg(p + n), (float)__ldg(p + nper + n), (float)__ldg(p + 2 * nper + n), 0.f);
+}
+
 #ifndef GB_KERNELS_HELPERS_ONLY
-// Converts the coefficients to float4 nodes (c_x, c_y, c_z, 0) and writes the
-// transform constants of the initial affine (block 0).
-__global__ void k_prepare_bspline(EvalArgs a, EvalConsts* out) {
+// Global float4 node array, for grids too large to stage in shared memory.
+__global__ void k_prepare_bspline(EvalArgs a) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n < a.nper)
-    a.nodes[n] = make_float4((float)a.params[n], (float)a.params[a.nper + n], (float)a.params[2 * a.nper + n], 0.f);
-  if (blockIdx.x == 0 && threadIdx.x < 13)
-    affine_const_entry(threadIdx.x, a.init_p, a.init_c, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin,
-                       *out);
+  if (n < a.nper) a.nodes[n] = node_from_params(a.params, a.nper, n);
 }
 #endif  // GB_KERNELS_HELPERS_ONLY
 
-// Shared-memory copy of the nodes when they fit, else the global array.
+// Nodes converted from the parameters into shared memory (SMEM), else the global
+// array written by k_prepare_bspline.  A compile-time choice, so node reads
+// compile to shared-memory loads rather than generic ones.
+template <bool SMEM>
 __device__ __forceinline__ const float4* stage_nodes(const EvalArgs& a, float4* sh) {
-  if (!a.nodes_smem) return a.nodes;
-  for (int k = threadIdx.x; k < a.nper; k += blockDim.x) sh[k] = __ldcg(a.nodes + k);
+  if (!SMEM) return a.nodes;
+  for (int k = threadIdx.x; k < a.nper; k += blockDim.x) sh[k] = node_from_params(a.params, a.nper, k);
   return sh;
 }
 
@@ -117,14 +120,14 @@ __device__ __forceinline__ float3 grad_map(const EvalConsts& K, float3 g) {
 
 #ifndef GB_KERNELS_HELPERS_ONLY
 // MeanSquares, B-spline: value sum and count; per sample a = 2 (f - m) M^T g in the cache.
-template <int GRAD>
+template <int GRAD, bool SMEM>
 __global__ void __launch_bounds__(kBlock) k_msq_bspline(EvalArgs a) {
   extern __shared__ float4 nodes_sh[];
   __shared__ EvalConsts K;
   __shared__ float red[kBlock / 32][1];
   __shared__ double blk[1], fin[1];
   load_consts(a.consts, K);
-  const float4* nodes = stage_nodes(a, nodes_sh);
+  const float4* nodes = stage_nodes<SMEM>(a, nodes_sh);
   __syncthreads();
   KahanF acc[1];
   acc[0].zero();
@@ -173,8 +176,8 @@ __host__ __device__ inline size_t mattes_bspline_node_offset(int B) {
 }
 
 // Mattes pass 1, B-spline: as k_mattes_pass1_affine, caching (term, M^T g).
-template <int GRAD>
-__global__ void __launch_bounds__(kBlock) k_mattes_pass1_bspline(EvalArgs a) {
+template <int GRAD, bool SMEM>
+__global__ void __launch_bounds__(kBlock, SMEM ? 4 : 3) k_mattes_pass1_bspline(EvalArgs a) {
   extern __shared__ unsigned long long smem_u64[];
   const int B = a.bins;
   unsigned long long* hist = smem_u64;
@@ -188,7 +191,7 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_bspline(EvalArgs a) {
     cs[k] = 0ull;
   }
   load_consts(a.consts, K);
-  const float4* nodes = stage_nodes(a, nodes_sh);
+  const float4* nodes = stage_nodes<SMEM>(a, nodes_sh);
   __syncthreads();
   unsigned nv = 0;
   const int lane = threadIdx.x & 31;
@@ -228,67 +231,93 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass1_bspline(EvalArgs a) {
   mattes_pass1_epilogue(a, nv, hist, cs, fm);
 }
 
-// One block per chunk of same-cell samples; thread t = support node
-// (kx, ky, kz) = (t & 3, (t >> 2) & 3, t >> 4) sums over the chunk
-// W_t(s) a_s, a_s = 2 (f - m) M^T g (MeanSquares) or w(term) M^T g (Mattes,
-// w = sum_k log(p/pm)[f][m_k] beta3'(m_k - term)); compensated FP32.
+// One block per chunk of same-cell samples (at most kChunkLen = blockDim).
+// Load phase: thread j stages sample j's 12 axis weights and its 3-vector
+// a_s = 2 (f - m) M^T g (MeanSquares) or w(term) M^T g (Mattes,
+// w = sum_k log(p/pm)[f][m_k] beta3'(m_k - term)).  Sum phase: thread t owns
+// the 4 x-adjacent support nodes of row (ky, kz) = (t & 3, (t >> 2) & 3) over
+// the sample slice t >> 4 (16 slices of 16 samples): per sample one 16-byte
+// load of the x weights, 12 FMAs.  The 16 slice sums of each output are then
+// added in slice order.
+constexpr int kChunkSlices = 16;
 template <bool MATTES>
-__global__ void __launch_bounds__(kChunkThreads) k_bspline_chunks(EvalArgs a) {
-  __shared__ float W1[kChunkLen][12];
+__global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
+  __shared__ __align__(16) float W1[kChunkLen][12];
   __shared__ float4 AV[kChunkLen];
+  __shared__ float qs[kChunkSlices][192];
   const int4 ch = a.chunks[blockIdx.x];
   const int len = ch.y - ch.x;
   const int B = a.bins;
-  for (int j = threadIdx.x; j < len; j += kChunkThreads) {
-    const int64_t i = (int64_t)ch.x + j;
+  const int t = threadIdx.x;
+  if (t < len) {
+    const int64_t i = (int64_t)ch.x + t;
     const float4 su = __ldg(a.sup + i);
     const float4 c = __ldcg(a.cache + i);
     float4 av = make_float4(0.f, 0.f, 0.f, 0.f);
     if (MATTES) {
+      const int fbin = __float_as_int(__ldg(&a.samples[i].w));
       if (c.x == c.x) {
         int pdfm;
-        float t, d[4];
-        parzen_window(c.x, B, pdfm, t);
-        parzen_deriv(t, d);
-        const float* row = a.pratio + __float_as_int(__ldg(&a.samples[i].w)) * B + pdfm;
+        float tt, d[4];
+        parzen_window(c.x, B, pdfm, tt);
+        parzen_deriv(tt, d);
+        const float* row = a.pratio + fbin * B + pdfm;
         const float w = __ldcg(row) * d[0] + __ldcg(row + 1) * d[1] + __ldcg(row + 2) * d[2] + __ldcg(row + 3) * d[3];
         av = make_float4(w * c.y, w * c.z, w * c.w, 0.f);
       }
     } else {
       av = make_float4(c.x, c.y, c.z, 0.f);
     }
-    bspline_basis(su.x, &W1[j][0]);
-    bspline_basis(su.y, &W1[j][4]);
-    bspline_basis(su.z, &W1[j][8]);
-    AV[j] = av;
+    bspline_basis(su.x, &W1[t][0]);
+    bspline_basis(su.y, &W1[t][4]);
+    bspline_basis(su.z, &W1[t][8]);
+    AV[t] = av;
   }
   __syncthreads();
-  const int t = threadIdx.x;
-  const int kx = t & 3, ky = (t >> 2) & 3, kz = t >> 4;
-  KahanF s0, s1, s2;
-  s0.zero();
-  s1.zero();
-  s2.zero();
-  for (int j = 0; j < len; ++j) {
-    const float W = W1[j][kx] * W1[j][4 + ky] * W1[j][8 + kz];
+  const int ky = t & 3, kz = (t >> 2) & 3, sl = t >> 4;
+  constexpr int kSlice = kChunkLen / kChunkSlices;
+  const int j0 = sl * kSlice, j1 = min(len, j0 + kSlice);
+  float acc[4][3];
+#pragma unroll
+  for (int kx = 0; kx < 4; ++kx) acc[kx][0] = acc[kx][1] = acc[kx][2] = 0.f;
+  for (int j = j0; j < j1; ++j) {
+    const float4 wx = *reinterpret_cast<const float4*>(&W1[j][0]);
+    const float wyz = W1[j][4 + ky] * W1[j][8 + kz];
     const float4 v = AV[j];
-    s0.add(W * v.x);
-    s1.add(W * v.y);
-    s2.add(W * v.z);
+    const float w[4] = {wx.x * wyz, wx.y * wyz, wx.z * wyz, wx.w * wyz};
+#pragma unroll
+    for (int kx = 0; kx < 4; ++kx) {
+      acc[kx][0] = fmaf(w[kx], v.x, acc[kx][0]);
+      acc[kx][1] = fmaf(w[kx], v.y, acc[kx][1]);
+      acc[kx][2] = fmaf(w[kx], v.z, acc[kx][2]);
+    }
   }
-  float* out = a.chunk_part + (size_t)blockIdx.x * 192;
-  out[t] = s0.value();
-  out[64 + t] = s1.value();
-  out[128 + t] = s2.value();
+  const int k0 = 4 * ky + 16 * kz;
+#pragma unroll
+  for (int kx = 0; kx < 4; ++kx) {
+    qs[sl][k0 + kx] = acc[kx][0];
+    qs[sl][64 + k0 + kx] = acc[kx][1];
+    qs[sl][128 + k0 + kx] = acc[kx][2];
+  }
+  __syncthreads();
+  if (t < 192) {
+    float s = qs[0][t];
+#pragma unroll
+    for (int q = 1; q < kChunkSlices; ++q) s = __fadd_rn(s, qs[q][t]);
+    a.chunk_part[(size_t)blockIdx.x * 192 + t] = s;
+  }
 }
 
-// One warp per parameter (node n, dimension d): FP64 sum, in a fixed order, of
-// the chunk sums of every cell whose 4x4x4 support holds node n; then the
-// metric's scale (1/N for MeanSquares, -1/(binsize N) for Mattes,
-// MeanSquares...Threader.hxx:71-79, Mattes...Threader.hxx:446-457).
+// One warp per node n: for its three parameters (n + d * nper), the sum of the
+// chunk sums of every cell whose 4x4x4 support holds n, listed at Initialize in
+// node_entries (chunk * 192 + support position).  Lane-strided over the list
+// with compensated FP32 (GB300's FP64 pipe is a small fraction of FP32), a
+// fixed XOR tree across lanes, FP64 only for the metric's scale (1/N for
+// MeanSquares, -1/(binsize N) for Mattes, MeanSquares...Threader.hxx:71-79,
+// Mattes...Threader.hxx:446-457).
 template <bool MATTES>
 __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const unsigned long long N = __ldcg(a.acc_n);
   const int st = __ldcg(a.status);
@@ -296,30 +325,26 @@ __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
     a.out[1] = (double)N;
     if (MATTES) a.out[0] = st == GB_OK ? __ldcg(a.final_value) : 0.0;
   }
-  if (gw >= 3 * a.nper) return;
-  const int d = gw / a.nper, n = gw - d * a.nper;
-  const int ix = n % a.gx, iy = (n / a.gx) % a.gy, iz = n / (a.gx * a.gy);
-  // cells (first support node) c with c <= i <= c + 3 and 0 <= c <= g - 4
-  const int cx0 = max(0, ix - 3), cx1 = min(ix, a.gx - 4);
-  const int cy0 = max(0, iy - 3), cy1 = min(iy, a.gy - 4);
-  const int cz0 = max(0, iz - 3), cz1 = min(iz, a.gz - 4);
-  const int ncx = cx1 - cx0 + 1, ncy = cy1 - cy0 + 1, ncz = cz1 - cz0 + 1;
-  double s = 0.0;
-  if (ncx > 0 && ncy > 0 && ncz > 0) {
-    for (int c = lane; c < ncx * ncy * ncz; c += 32) {
-      const int cx = cx0 + c % ncx, cy = cy0 + (c / ncx) % ncy, cz = cz0 + c / (ncx * ncy);
-      const int cell = 1 + cx + a.gx * (cy + a.gy * cz);
-      const int k = (ix - cx) + 4 * (iy - cy) + 16 * (iz - cz);
-      const int q1 = __ldg(a.cell_first + cell + 1);
-      for (int q = __ldg(a.cell_first + cell); q < q1; ++q)
-        s += (double)__ldcg(a.chunk_part + (size_t)q * 192 + d * 64 + k);
-    }
+  if (n >= a.nper) return;
+  const int e0 = __ldg(a.node_first + n), e1 = __ldg(a.node_first + n + 1);
+  KahanF s0, s1, s2;
+  s0.zero();
+  s1.zero();
+  s2.zero();
+#pragma unroll 4
+  for (int e = e0 + lane; e < e1; e += 32) {
+    const float* src = a.chunk_part + __ldg(a.node_entries + e);
+    s0.add(__ldcg(src));
+    s1.add(__ldcg(src + 64));
+    s2.add(__ldcg(src + 128));
   }
-  s = warp_sum_d(s);
+  const float t0 = warp_sum(s0.value()), t1 = warp_sum(s1.value()), t2 = warp_sum(s2.value());
   if (lane == 0) {
     double scale = 0.0;
     if (st == GB_OK && N > 0) scale = MATTES ? -1.0 / (a.m_bs * (double)N) : 1.0 / (double)N;
-    a.out[2 + gw] = s * scale;
+    a.out[2 + n] = (double)t0 * scale;
+    a.out[2 + a.nper + n] = (double)t1 * scale;
+    a.out[2 + 2 * a.nper + n] = (double)t2 * scale;
   }
 }
 #endif  // GB_KERNELS_HELPERS_ONLY

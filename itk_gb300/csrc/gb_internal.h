@@ -96,7 +96,8 @@ struct gb_metric {
   gb::DevBuf<float4> d_cache;    // per-sample pass-1 result for the derivative pass
   gb::DevBuf<float4> d_sup;      // per-sample B-spline support (tx, ty, tz, packed start | valid)
   gb::DevBuf<int4> d_chunks;     // (first sample, end sample, cell, 0) of same-cell sample runs
-  gb::DevBuf<int> d_cell_first;  // first chunk of each B-spline cell, cells 0 .. nper + 1
+  gb::DevBuf<int> d_node_first;    // per node: first entry in d_node_entries (nper + 1)
+  gb::DevBuf<int> d_node_entries;  // chunk * 192 + support position of each (node, chunk) pair
   gb::DevBuf<float> d_chunk_part;  // nchunks x 192 Jacobian partial sums
   gb::DevBuf<float4> d_nodes;    // B-spline coefficients as float4 nodes
   int64_t nchunks = 0;

@@ -170,11 +170,10 @@ struct EvalArgs {
   float4* nodes;                     // coefficient nodes (cx, cy, cz, 0), written by k_prepare_bspline
   int gx, gy, gz, nper;
   int nodes_smem;                    // evaluation kernels stage the nodes in shared memory
-  double init_p[12];                 // initial affine of a composite (identity for a plain B-spline)
-  double init_c[3];
   const int4* __restrict__ chunks;   // (first sample, end sample, cell id, 0) of same-cell sample runs
   int nchunks;
-  const int* __restrict__ cell_first;  // first chunk of each cell id; cell ids 1 .. gx*gy*gz
+  const int* __restrict__ node_first;    // per node: first entry in node_entries (nper + 1 values)
+  const int* __restrict__ node_entries;  // chunk * 192 + support position of each (node, chunk) pair
   float* chunk_part;                 // nchunks x 192 per-chunk Jacobian partial sums
 };
 
@@ -471,7 +470,7 @@ __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigne
 }
 
 template <int GRAD>
-__global__ void __launch_bounds__(kBlock) k_mattes_pass1_affine(EvalArgs a) {
+__global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_pass1_affine(EvalArgs a) {
   extern __shared__ unsigned long long smem_u64[];
   const int B = a.bins;
   unsigned long long* hist = smem_u64;

@@ -117,6 +117,15 @@ static bool is_bspline(const gb_metric* m) {
   return m->tkind == GB_TRANSFORM_BSPLINE || m->tkind == GB_TRANSFORM_COMPOSITE;
 }
 
+// Initial affine of a B-spline path: the composite's first transform ([affine,
+// B-spline] queue, B-spline applied first), the identity for a plain B-spline.
+static void bspline_init_affine(const gb_metric* m, double p[12], double c[3]) {
+  const double I[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+  const bool comp = m->tkind == GB_TRANSFORM_COMPOSITE;
+  for (int i = 0; i < 12; ++i) p[i] = comp ? m->tfixed[18 + i] : I[i];
+  for (int i = 0; i < 3; ++i) c[i] = comp ? m->tfixed[30 + i] : 0.0;
+}
+
 // Dynamic shared memory of the evaluation kernels' B-spline nodes: staged when
 // they leave room for at least two resident blocks per SM, else read from HBM/L2.
 static size_t bspline_node_bytes(const gb_metric* m) { return (size_t)m->nper * sizeof(float4); }
@@ -539,17 +548,42 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
       i = j;
     }
     for (size_t c = 1; c < cell_first.size(); ++c) cell_first[c] += cell_first[c - 1];
+    if (chunks.size() > (size_t)(0x7fffffff / 192) || chunks.size() * 64 > (size_t)0x7fffffff)
+      return fail(GB_ERR_UNSUPPORTED, "too many B-spline sample chunks for 32-bit chunk-sum indices");
+    // per node: the chunk-sum entries (chunk * 192 + support position k) of every
+    // cell whose 4x4x4 support holds the node, cells in z, y, x order, chunks in order
+    const int gx = m->grid[0], gy = m->grid[1], gz = m->grid[2];
+    std::vector<int> node_first((size_t)m->nper + 1, 0);
+    std::vector<int> entries;
+    entries.reserve(chunks.size() * 64);
+    for (int64_t n = 0; n < m->nper; ++n) {
+      node_first[n] = (int)entries.size();
+      const int ix = (int)(n % gx), iy = (int)((n / gx) % gy), iz = (int)(n / ((int64_t)gx * gy));
+      for (int cz = std::max(0, iz - 3); cz <= std::min(iz, gz - 4); ++cz)
+        for (int cy = std::max(0, iy - 3); cy <= std::min(iy, gy - 4); ++cy)
+          for (int cx = std::max(0, ix - 3); cx <= std::min(ix, gx - 4); ++cx) {
+            const int64_t cell = 1 + cx + (int64_t)gx * (cy + (int64_t)gy * cz);
+            const int k = (ix - cx) + 4 * (iy - cy) + 16 * (iz - cz);
+            for (int q = cell_first[cell]; q < cell_first[cell + 1]; ++q) entries.push_back(q * 192 + k);
+          }
+    }
+    node_first[m->nper] = (int)entries.size();
     m->nchunks = (int64_t)chunks.size();
     m->d_chunks.reset();
-    m->d_cell_first.reset();
+    m->d_node_first.reset();
+    m->d_node_entries.reset();
     m->d_chunk_part.reset();
     GB_CUDA(m->d_chunks.alloc(std::max<size_t>(1, chunks.size())));
-    GB_CUDA(m->d_cell_first.alloc(cell_first.size()));
+    GB_CUDA(m->d_node_first.alloc(node_first.size()));
+    GB_CUDA(m->d_node_entries.alloc(std::max<size_t>(1, entries.size())));
     GB_CUDA(m->d_chunk_part.alloc(std::max<size_t>(1, chunks.size()) * 192));
     if (!chunks.empty())
       GB_CUDA(cudaMemcpyAsync(m->d_chunks.p, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, st));
-    GB_CUDA(cudaMemcpyAsync(m->d_cell_first.p, cell_first.data(), sizeof(int) * cell_first.size(),
+    GB_CUDA(cudaMemcpyAsync(m->d_node_first.p, node_first.data(), sizeof(int) * node_first.size(),
                             cudaMemcpyHostToDevice, st));
+    if (!entries.empty())
+      GB_CUDA(cudaMemcpyAsync(m->d_node_entries.p, entries.data(), sizeof(int) * entries.size(),
+                              cudaMemcpyHostToDevice, st));
     m->d_nodes.reset();
     GB_CUDA(m->d_nodes.alloc((size_t)m->nper));
     GB_CUDA(cudaStreamSynchronize(st));  // the host vectors die here
@@ -592,6 +626,14 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   GB_CUDA(cudaMallocHost(&m->h_out, sizeof(double) * (2 + P)));
   GB_CUDA(m->d_consts.alloc(1));
   if (!m->h_consts) GB_CUDA(cudaMallocHost(&m->h_consts, sizeof(EvalConsts)));
+  if (bspline) {
+    // the B-spline paths' constants depend only on the fixed initial affine: once, here
+    double p[12], c[3];
+    bspline_init_affine(m, p, c);
+    affine_consts(p, c, m->moving.p2i, m->moving.origin, sampled ? nullptr : m->virt.i2p, m->virt.origin,
+                  *m->h_consts);
+    GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
+  }
   GB_CUDA(cudaStreamSynchronize(st));
   m->initialized = true;
   return GB_OK;
@@ -656,14 +698,10 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
     a.gz = m->grid[2];
     a.nper = (int)m->nper;
     a.nodes_smem = nodes_in_smem(m) ? 1 : 0;
-    // initial affine of the composite ([affine, B-spline] queue: B-spline applied first), else identity
-    const double I[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
-    const bool comp = m->tkind == GB_TRANSFORM_COMPOSITE;
-    for (int i = 0; i < 12; ++i) a.init_p[i] = comp ? m->tfixed[18 + i] : I[i];
-    for (int i = 0; i < 3; ++i) a.init_c[i] = comp ? m->tfixed[30 + i] : 0.0;
     a.chunks = m->d_chunks.p;
     a.nchunks = (int)m->nchunks;
-    a.cell_first = m->d_cell_first.p;
+    a.node_first = m->d_node_first.p;
+    a.node_entries = m->d_node_entries.p;
     a.chunk_part = m->d_chunk_part.p;
   }
 }
@@ -683,21 +721,32 @@ static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalAr
 static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool deriv) {
   cudaStream_t st = m->stream;
   const int nper = (int)m->nper;
-  k_prepare_bspline<<<(nper + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, m->d_consts.p);
-  GB_CUDA(cudaGetLastError());
-  m->mark();
-  const size_t nb = a.nodes_smem ? bspline_node_bytes(m) : 0;
+  const bool sm = a.nodes_smem != 0;
+  if (!sm) {  // staged kernels convert the parameters themselves
+    k_prepare_bspline<<<(nper + kBlock - 1) / kBlock, kBlock, 0, st>>>(a);
+    GB_CUDA(cudaGetLastError());
+    m->mark();
+  }
+  const size_t nb = sm ? bspline_node_bytes(m) : 0;
   const bool mattes = m->kind == GB_METRIC_MATTES;
   if (!mattes) {
-    GB_CUDA(cd ? launch_wave(m, k_msq_bspline<kGradCentralDifference>, nb, a)
-               : launch_wave(m, k_msq_bspline<kGradImage>, nb, a));
+    cudaError_t e;
+    if (cd) e = sm ? launch_wave(m, k_msq_bspline<kGradCentralDifference, true>, nb, a)
+                   : launch_wave(m, k_msq_bspline<kGradCentralDifference, false>, nb, a);
+    else e = sm ? launch_wave(m, k_msq_bspline<kGradImage, true>, nb, a)
+                : launch_wave(m, k_msq_bspline<kGradImage, false>, nb, a);
+    GB_CUDA(e);
     m->mark();
   } else {
     const int B = (int)m->bins;
     const size_t sh1 = mattes_bspline_node_offset(B) + nb;
     if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
-    GB_CUDA(cd ? launch_wave(m, k_mattes_pass1_bspline<kGradCentralDifference>, sh1, a)
-               : launch_wave(m, k_mattes_pass1_bspline<kGradImage>, sh1, a));
+    cudaError_t e;
+    if (cd) e = sm ? launch_wave(m, k_mattes_pass1_bspline<kGradCentralDifference, true>, sh1, a)
+                   : launch_wave(m, k_mattes_pass1_bspline<kGradCentralDifference, false>, sh1, a);
+    else e = sm ? launch_wave(m, k_mattes_pass1_bspline<kGradImage, true>, sh1, a)
+                : launch_wave(m, k_mattes_pass1_bspline<kGradImage, false>, sh1, a);
+    GB_CUDA(e);
     m->mark();
     k_mattes_finalize<<<(B * B + kFinalizeThreads - 1) / kFinalizeThreads, kFinalizeThreads, 0, st>>>(a);
     GB_CUDA(cudaGetLastError());
@@ -705,12 +754,12 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
   }
   if (!deriv) return GB_OK;
   if (m->nchunks > 0) {
-    if (mattes) k_bspline_chunks<true><<<(unsigned)m->nchunks, kChunkThreads, 0, st>>>(a);
-    else k_bspline_chunks<false><<<(unsigned)m->nchunks, kChunkThreads, 0, st>>>(a);
+    if (mattes) k_bspline_chunks<true><<<(unsigned)m->nchunks, kChunkLen, 0, st>>>(a);
+    else k_bspline_chunks<false><<<(unsigned)m->nchunks, kChunkLen, 0, st>>>(a);
     GB_CUDA(cudaGetLastError());
     m->mark();
   }
-  const int64_t threads = (int64_t)3 * nper * 32;
+  const int64_t threads = (int64_t)nper * 32;  // one warp per node
   const unsigned pblocks = (unsigned)((threads + kParamsBlock - 1) / kParamsBlock);
   if (mattes) k_bspline_params<true><<<pblocks, kParamsBlock, 0, st>>>(a);
   else k_bspline_params<false><<<pblocks, kParamsBlock, 0, st>>>(a);

@@ -35,9 +35,21 @@ def touched_voxels(points, transform, moving, chunk=1 << 21):
     return int(mark.sum())
 
 
-def evaluation_bytes(n_samples, v_touched, sparse=True):
-    """B_alg of one GetValueAndDerivative evaluation."""
-    return n_samples * (12 if sparse else 0) + v_touched * 20
+def evaluation_bytes(n_samples, v_touched, sparse=True, nparams=0):
+    """B_alg of one GetValueAndDerivative evaluation (+ the parameters in and the derivative out, 8 B each)."""
+    return n_samples * (12 if sparse else 0) + v_touched * 20 + nparams * 16
+
+
+def mattes_pass1_bspline_bytes(n_samples, v_touched, nodes):
+    """Minimal DRAM traffic of the B-spline Mattes pass-1 kernel: as the affine pass 1 plus each
+    sample's B-spline support record (16 B) and the float4 control nodes once (16 B each)."""
+    return n_samples * 48 + v_touched * 16 + nodes * 16
+
+
+def msq_bspline_bytes(n_samples, v_touched, nodes):
+    """Minimal DRAM traffic of the B-spline MeanSquares kernel: sample record and support record
+    read, per-sample derivative factor written (16 B each), touched voxels and nodes once."""
+    return n_samples * 48 + v_touched * 16 + nodes * 16
 
 
 def mattes_pass1_bytes(n_samples, v_touched):

@@ -158,16 +158,17 @@ class BSplineTransform:
         start = np.floor(ci - 1.0).astype(np.int64)
         u = ci - start
         w1 = [np.stack([_bspline3(u[:, j] - k) for k in range(4)], axis=1) for j in range(3)]
-        coeff = self.coefficient_images()
+        coeff = np.ascontiguousarray(self.params.reshape(3, -1).T)  # (nodes, 3)
         out = x.copy()
         disp = np.zeros_like(x)
         st = np.where(inside[:, None], start, 1)
+        base = st[:, 0] + g[0] * (st[:, 1] + g[1] * st[:, 2])
+        k4 = np.arange(4)
         for iz in range(4):
             for iy in range(4):
-                for ix in range(4):
-                    w = w1[0][:, ix] * w1[1][:, iy] * w1[2][:, iz]
-                    c = coeff[:, st[:, 2] + iz, st[:, 1] + iy, st[:, 0] + ix]
-                    disp += (w[:, None] * c.T)
+                # the 4 x-consecutive nodes of one (y, z) row in one gather: (n, 4, 3)
+                row = coeff[(base + g[0] * (iy + g[1] * iz))[:, None] + k4]
+                disp += (w1[1][:, iy] * w1[2][:, iz])[:, None] * np.einsum("nk,nkc->nc", w1[0], row)
         out[inside] += disp[inside]
         return out
 
