@@ -53,6 +53,8 @@ __device__ __forceinline__ float4 node_from_params(const double* __restrict__ p,
 #ifndef GB_KERNELS_HELPERS_ONLY
 // Global float4 node array, for grids too large to stage in shared memory.
 __global__ void k_prepare_bspline(EvalArgs a) {
+  griddep_wait();
+  griddep_launch_dependents();
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n < a.nper) a.nodes[n] = node_from_params(a.params, a.nper, n);
 }
@@ -126,6 +128,8 @@ __global__ void __launch_bounds__(kBlock) k_msq_bspline(EvalArgs a) {
   __shared__ EvalConsts K;
   __shared__ float red[kBlock / 32][1];
   __shared__ double blk[1], fin[1];
+  griddep_wait();
+  griddep_launch_dependents();
   load_consts(a.consts, K);
   const float4* nodes = stage_nodes<SMEM>(a, nodes_sh);
   __syncthreads();
@@ -190,6 +194,8 @@ __global__ void __launch_bounds__(kBlock, SMEM ? 4 : 3) k_mattes_pass1_bspline(E
     fm[k] = 0u;
     cs[k] = 0ull;
   }
+  griddep_wait();
+  griddep_launch_dependents();
   load_consts(a.consts, K);
   const float4* nodes = stage_nodes<SMEM>(a, nodes_sh);
   __syncthreads();
@@ -245,6 +251,7 @@ __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
   __shared__ __align__(16) float W1[kChunkLen][12];
   __shared__ float4 AV[kChunkLen];
   __shared__ float qs[kChunkSlices][192];
+  griddep_wait();  // several waves of blocks: dependents are released at each block's end
   const int4 ch = a.chunks[blockIdx.x];
   const int len = ch.y - ch.x;
   const int B = a.bins;
@@ -306,6 +313,7 @@ __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
     for (int q = 1; q < kChunkSlices; ++q) s = __fadd_rn(s, qs[q][t]);
     a.chunk_part[(size_t)blockIdx.x * 192 + t] = s;
   }
+  griddep_launch_dependents();
 }
 
 // One warp per node n: for its three parameters (n + d * nper), the sum of the
@@ -319,6 +327,8 @@ template <bool MATTES>
 __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
   const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
+  griddep_wait();
+  griddep_launch_dependents();
   const unsigned long long N = __ldcg(a.acc_n);
   const int st = __ldcg(a.status);
   if (blockIdx.x == 0 && threadIdx.x == 0) {

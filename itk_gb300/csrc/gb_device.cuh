@@ -37,6 +37,17 @@ __host__ __device__ __forceinline__ double dadd(double a, double b) {
 }
 
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch.  The kernels of one evaluation run back to
+// back on a stream; each one after the first is launched with programmatic
+// stream serialization, so its blocks may be scheduled while its predecessor
+// drains.  griddep_wait() blocks until the predecessor grids have completed
+// and their memory writes are visible (a no-op for a normal launch); nothing
+// before it may touch global memory that a predecessor reads or writes.
+// griddep_launch_dependents() lets the next kernel's blocks be scheduled.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
 // Kahan-compensated FP32 accumulator (the reference's CompensatedSummation,
 // Core/Common/include/itkCompensatedSummation.hxx:38-48, at FP32).
 struct KahanF {

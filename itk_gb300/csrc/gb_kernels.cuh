@@ -19,6 +19,7 @@
 #include <cfloat>
 
 #include "../../include/itk_gb300.h"
+#include "gb_bulk.cuh"
 #include "gb_device.cuh"
 
 namespace gb {
@@ -181,6 +182,8 @@ struct EvalArgs {
 // Device twin of the host constant computation (parameters already in HBM).
 // 13 threads, one output each, so the FP64 dependency chains run side by side.
 __global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
+  griddep_wait();
+  griddep_launch_dependents();
   if (threadIdx.x < 13)
     affine_const_entry(threadIdx.x, a.params, a.center, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin,
                        *out);
@@ -335,6 +338,8 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
   __shared__ EvalConsts K;
   __shared__ float red[kBlock / 32][13];
   __shared__ double blk[13], fin[13];
+  griddep_wait();
+  griddep_launch_dependents();
   load_consts(a.consts, K);
   __syncthreads();
   KahanF acc[13];
@@ -482,6 +487,8 @@ __global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_p
     fm[k] = 0u;
     cs[k] = 0ull;
   }
+  griddep_wait();
+  griddep_launch_dependents();
   load_consts(a.consts, K);
   __syncthreads();
   unsigned nv = 0;
@@ -531,6 +538,8 @@ __global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_p
 // JointPDFSum .hxx:533-541).  Block partials are added in block order by the
 // last block.
 __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a) {
+  griddep_wait();
+  griddep_launch_dependents();
   const int B = a.bins;
   const int lane = threadIdx.x;
   const double T = __ldcg(&a.marg[0]);
@@ -579,46 +588,98 @@ __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a
 #endif  // GB_KERNELS_HELPERS_ONLY
 
 #ifndef GB_KERNELS_HELPERS_ONLY
+// Streamed record tiles: each block owns a contiguous, tile-aligned range of
+// samples; thread 0 keeps kStreamStages tiles of (cache, sample) records in
+// flight with bulk asynchronous copies, completed on one mbarrier per stage.
+constexpr int kStreamStages = 4;
+constexpr int kStreamTile = kBlock;  // records per stage and stream
+constexpr size_t kStreamBytes = (size_t)2 * kStreamStages * kStreamTile * sizeof(float4);
+
+__device__ __forceinline__ void block_range(int64_t n, int64_t& b0, int64_t& b1) {
+  const int64_t per = ((n + gridDim.x - 1) / gridDim.x + kStreamTile - 1) / kStreamTile * kStreamTile;
+  b0 = min(n, (int64_t)blockIdx.x * per);
+  b1 = min(n, b0 + per);
+}
+
 // Mattes pass 2, affine: derivative from the cached Parzen terms and gradients.
+// Dynamic shared memory: kStreamBytes of record stages, then the bins^2 log(p/pm) table.
 __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
-  extern __shared__ float pr[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* cbuf = reinterpret_cast<float4*>(smem_raw);  // [stage][tile] cache records
+  float4* sbuf = cbuf + kStreamStages * kStreamTile;    // [stage][tile] sample records
+  float* pr = reinterpret_cast<float*>(smem_raw + kStreamBytes);
+  __shared__ unsigned long long full[kStreamStages];
+  __shared__ int failed;
   __shared__ EvalConsts K;
   __shared__ float red[kBlock / 32][12];
   __shared__ double blk[12], fin[12];
   const int B = a.bins;
+  int64_t b0, b1;
+  block_range(a.n, b0, b1);
+  const int ntiles = (int)((b1 - b0 + kStreamTile - 1) / kStreamTile);
+  // tile t -> stage t % kStreamStages; the stage's phase parity is (t / kStreamStages) & 1
+  auto issue = [&](int t) {
+    const int st = t % kStreamStages;
+    const int64_t r0 = b0 + (int64_t)t * kStreamTile;
+    const unsigned bytes = (unsigned)(min((int64_t)kStreamTile, b1 - r0) * sizeof(float4));
+    mbar_arrive_expect_tx(&full[st], 2 * bytes);
+    bulk_g2s(cbuf + st * kStreamTile, a.cache + r0, bytes, &full[st]);
+    bulk_g2s(sbuf + st * kStreamTile, a.samples + r0, bytes, &full[st]);
+  };
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kStreamStages; ++st) mbar_init(&full[st], 1);
+    mbar_init_fence();
+    failed = 0;
+  }
+  griddep_wait();
+  griddep_launch_dependents();
+  if (threadIdx.x == 0)
+    for (int t = 0; t < min(kStreamStages, ntiles); ++t) issue(t);
   for (int k = threadIdx.x; k < B * B; k += blockDim.x) pr[k] = __ldcg(&a.pratio[k]);
   load_consts(a.consts, K);
   __syncthreads();
   KahanF acc[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k].zero();
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  constexpr int kUnroll = 2;  // independent loads in flight per thread
-  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < a.n; i0 += kUnroll * stride) {
-    float4 cc[kUnroll], s[kUnroll];
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      const int64_t i = i0 + u * stride;
-      cc[u] = i < a.n ? __ldcs(a.cache + i) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
-      s[u] = i < a.n ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  int t = 0;
+  for (; t < ntiles; ++t) {
+    const int st = t % kStreamStages;
+    if (!mbar_wait(&full[st], (unsigned)(t / kStreamStages) & 1u)) failed = 1;
+    const int64_t r0 = b0 + (int64_t)t * kStreamTile;
+    if (!failed && threadIdx.x < b1 - r0) {
+      const float4 cc = cbuf[st * kStreamTile + threadIdx.x];
+      const float4 s = sbuf[st * kStreamTile + threadIdx.x];
+      if (cc.x == cc.x) {  // NaN term: rejected sample
+        int pdfm;
+        float tt, d[4];
+        parzen_window(cc.x, B, pdfm, tt);
+        parzen_deriv(tt, d);
+        const float* row = pr + __float_as_int(s.w) * B + pdfm;
+        const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
+        const float3 v = jac_vec(K, s.x, s.y, s.z);
+        const float vx = v.x, vy = v.y, vz = v.z;
+        const float t0 = w * cc.y, t1 = w * cc.z, t2 = w * cc.w;
+        acc[0].add(t0 * vx); acc[1].add(t0 * vy); acc[2].add(t0 * vz);
+        acc[3].add(t1 * vx); acc[4].add(t1 * vy); acc[5].add(t1 * vz);
+        acc[6].add(t2 * vx); acc[7].add(t2 * vy); acc[8].add(t2 * vz);
+        acc[9].add(t0); acc[10].add(t1); acc[11].add(t2);
+      }
     }
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      if (cc[u].x != cc[u].x) continue;  // rejected sample
-      int pdfm;
-      float t, d[4];
-      parzen_window(cc[u].x, B, pdfm, t);
-      parzen_deriv(t, d);
-      const float* row = pr + __float_as_int(s[u].w) * B + pdfm;
-      const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
-      const float3 v = jac_vec(K, s[u].x, s[u].y, s[u].z);
-      const float vx = v.x, vy = v.y, vz = v.z;
-      const float t0 = w * cc[u].y, t1 = w * cc[u].z, t2 = w * cc[u].w;
-      acc[0].add(t0 * vx); acc[1].add(t0 * vy); acc[2].add(t0 * vz);
-      acc[3].add(t1 * vx); acc[4].add(t1 * vy); acc[5].add(t1 * vz);
-      acc[6].add(t2 * vx); acc[7].add(t2 * vy); acc[8].add(t2 * vz);
-      acc[9].add(t0); acc[10].add(t1); acc[11].add(t2);
+    __syncthreads();  // stage st consumed by every thread
+    if (failed) break;
+    if (threadIdx.x == 0 && t + kStreamStages < ntiles) {
+      fence_proxy_async_smem();
+      issue(t + kStreamStages);
     }
+  }
+  if (failed) {
+    // a copy never completed: report, drain what is still in flight (bounded), leave
+    if (threadIdx.x == 0) {
+      atomicExch(a.status, GB_ERR_TIMEOUT);
+      for (int u = t + 1; u < min(ntiles, t + kStreamStages); ++u)
+        mbar_wait(&full[u % kStreamStages], (unsigned)(u / kStreamStages) & 1u);
+    }
+    return;
   }
   block_sums<12>(acc, red, blk);
   if (!grid_sums<12>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin)) return;

@@ -706,13 +706,31 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   }
 }
 
+// One kernel of the evaluation chain on the handle's stream, launched with
+// programmatic stream serialization: its blocks may be scheduled while the
+// previous kernel drains, and wait in griddep_wait() for its results.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_chain(gb_metric* m, void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                                Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = m->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // Grid-stride evaluation kernel with `smem` bytes of dynamic shared memory, one full wave.
 template <typename K>
 static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalArgs& a) {
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kernel<<<full_wave(m, kernel, smem, m->nsamples), kBlock, smem, m->stream>>>(a);
-  return cudaGetLastError();
+  return launch_chain(m, kernel, (unsigned)full_wave(m, kernel, smem, m->nsamples), kBlock, smem, a);
 }
 
 // B-spline / composite evaluation: node conversion, the per-sample pass
@@ -723,8 +741,7 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
   const int nper = (int)m->nper;
   const bool sm = a.nodes_smem != 0;
   if (!sm) {  // staged kernels convert the parameters themselves
-    k_prepare_bspline<<<(nper + kBlock - 1) / kBlock, kBlock, 0, st>>>(a);
-    GB_CUDA(cudaGetLastError());
+    GB_CUDA(launch_chain(m, k_prepare_bspline, (unsigned)((nper + kBlock - 1) / kBlock), kBlock, 0, a));
     m->mark();
   }
   const size_t nb = sm ? bspline_node_bytes(m) : 0;
@@ -748,32 +765,33 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
                 : launch_wave(m, k_mattes_pass1_bspline<kGradImage, false>, sh1, a);
     GB_CUDA(e);
     m->mark();
-    k_mattes_finalize<<<(B * B + kFinalizeThreads - 1) / kFinalizeThreads, kFinalizeThreads, 0, st>>>(a);
-    GB_CUDA(cudaGetLastError());
+    GB_CUDA(launch_chain(m, k_mattes_finalize, (unsigned)((B * B + kFinalizeThreads - 1) / kFinalizeThreads),
+                         kFinalizeThreads, 0, a));
     m->mark();
   }
   if (!deriv) return GB_OK;
   if (m->nchunks > 0) {
-    if (mattes) k_bspline_chunks<true><<<(unsigned)m->nchunks, kChunkLen, 0, st>>>(a);
-    else k_bspline_chunks<false><<<(unsigned)m->nchunks, kChunkLen, 0, st>>>(a);
-    GB_CUDA(cudaGetLastError());
+    GB_CUDA(mattes ? launch_chain(m, k_bspline_chunks<true>, (unsigned)m->nchunks, kChunkLen, 0, a)
+                   : launch_chain(m, k_bspline_chunks<false>, (unsigned)m->nchunks, kChunkLen, 0, a));
     m->mark();
   }
   const int64_t threads = (int64_t)nper * 32;  // one warp per node
   const unsigned pblocks = (unsigned)((threads + kParamsBlock - 1) / kParamsBlock);
-  if (mattes) k_bspline_params<true><<<pblocks, kParamsBlock, 0, st>>>(a);
-  else k_bspline_params<false><<<pblocks, kParamsBlock, 0, st>>>(a);
-  GB_CUDA(cudaGetLastError());
+  GB_CUDA(mattes ? launch_chain(m, k_bspline_params<true>, pblocks, kParamsBlock, 0, a)
+                 : launch_chain(m, k_bspline_params<false>, pblocks, kParamsBlock, 0, a));
   m->mark();
   return GB_OK;
 }
 
 // Enqueues one evaluation; results land in d_out = [value, nvalid, derivative...].
-static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv) {
+// device_consts: the affine constants are computed on the device from d_params
+// (otherwise the host has uploaded them).
+static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_consts) {
   cudaStream_t st = m->stream;
   EvalArgs a;
   fill_eval_args(m, a, d_params, d_out, deriv);
   GB_CUDA(cudaMemsetAsync(m->d_acc.p, 0, m->acc_bytes, st));
+  if (device_consts && !is_bspline(m)) GB_CUDA(launch_chain(m, k_prepare_affine, 1, 32, 0, a, m->d_consts.p));
   if (m->nsamples == 0) {
     // no valid fixed sample at all: every point is invalid
     const int code = GB_ERR_NO_VALID_POINTS;
@@ -788,40 +806,24 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   m->mark();
   if (is_bspline(m)) return enqueue_eval_bspline(m, a, cd, deriv);
   if (m->kind == GB_METRIC_MEAN_SQUARES) {
-    if (cd) {
-      k_msq_affine<kGradCentralDifference>
-          <<<full_wave(m, k_msq_affine<kGradCentralDifference>, 0, m->nsamples), kBlock, 0, st>>>(a);
-    } else {
-      k_msq_affine<kGradImage><<<full_wave(m, k_msq_affine<kGradImage>, 0, m->nsamples), kBlock, 0, st>>>(a);
-    }
-    GB_CUDA(cudaGetLastError());
+    GB_CUDA(cd ? launch_wave(m, k_msq_affine<kGradCentralDifference>, 0, a)
+               : launch_wave(m, k_msq_affine<kGradImage>, 0, a));
     m->mark();
     return GB_OK;
   }
   // Mattes: pass 1, finalize, pass 2
   const int B = (int)m->bins;
   const size_t sh1 = sizeof(unsigned long long) * (B * B + B) + sizeof(unsigned) * B;
-  const size_t sh2 = sizeof(float) * B * B;
+  const size_t sh2 = kStreamBytes + sizeof(float) * B * B;  // record stages + log(p/pm) table
   if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
-  if (cd) {
-    cudaFuncSetAttribute(k_mattes_pass1_affine<kGradCentralDifference>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sh1);
-    k_mattes_pass1_affine<kGradCentralDifference>
-        <<<full_wave(m, k_mattes_pass1_affine<kGradCentralDifference>, sh1, m->nsamples), kBlock, sh1, st>>>(a);
-  } else {
-    cudaFuncSetAttribute(k_mattes_pass1_affine<kGradImage>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh1);
-    k_mattes_pass1_affine<kGradImage>
-        <<<full_wave(m, k_mattes_pass1_affine<kGradImage>, sh1, m->nsamples), kBlock, sh1, st>>>(a);
-  }
-  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cd ? launch_wave(m, k_mattes_pass1_affine<kGradCentralDifference>, sh1, a)
+             : launch_wave(m, k_mattes_pass1_affine<kGradImage>, sh1, a));
   m->mark();
-  k_mattes_finalize<<<(B * B + kFinalizeThreads - 1) / kFinalizeThreads, kFinalizeThreads, 0, st>>>(a);
-  GB_CUDA(cudaGetLastError());
+  GB_CUDA(launch_chain(m, k_mattes_finalize, (unsigned)((B * B + kFinalizeThreads - 1) / kFinalizeThreads),
+                       kFinalizeThreads, 0, a));
   m->mark();
   if (deriv) {
-    cudaFuncSetAttribute(k_mattes_pass2_affine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh2);
-    k_mattes_pass2_affine<<<full_wave(m, k_mattes_pass2_affine, sh2, m->nsamples), kBlock, sh2, st>>>(a);
-    GB_CUDA(cudaGetLastError());
+    GB_CUDA(launch_wave(m, k_mattes_pass2_affine, sh2, a));
     m->mark();
   }
   return GB_OK;
@@ -869,7 +871,7 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
                   m->virt.origin, *m->h_consts);
     GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
   }
-  int rc = enqueue_eval(m, d_params, m->d_out.p, deriv);
+  int rc = enqueue_eval(m, d_params, m->d_out.p, deriv, false);
   if (rc) return rc;
   GB_CUDA(cudaMemcpyAsync(m->h_out, m->d_out.p, sizeof(double) * (2 + (deriv ? P : 0)), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaMemcpyAsync(m->h_status, m->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -946,13 +948,7 @@ extern "C" int gb_metric_evaluate_device(gb_metric* m, const double* device_para
   if (!m || !device_params || !device_out) return fail(GB_ERR_BAD_ARG, "null argument");
   if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
   GB_CUDA(cudaSetDevice(m->ctx->device));
-  EvalArgs a;
-  fill_eval_args(m, a, device_params, device_out, with_derivative != 0);
-  if (!is_bspline(m)) {  // the B-spline path converts its parameters inside enqueue_eval
-    k_prepare_affine<<<1, 32, 0, m->stream>>>(a, m->d_consts.p);
-    GB_CUDA(cudaGetLastError());
-  }
-  return enqueue_eval(m, device_params, device_out, with_derivative != 0);
+  return enqueue_eval(m, device_params, device_out, with_derivative != 0, true);
 }
 
 extern "C" int gb_metric_synchronize(gb_metric* m) {
