@@ -65,9 +65,12 @@ __global__ void k_prepare_bspline(EvalArgs a) {
 // compile to shared-memory loads rather than generic ones.
 template <bool SMEM>
 __device__ __forceinline__ const float4* stage_nodes(const EvalArgs& a, float4* sh) {
-  if (!SMEM) return a.nodes;
-  for (int k = threadIdx.x; k < a.nper; k += blockDim.x) sh[k] = node_from_params(a.params, a.nper, k);
-  return sh;
+  if constexpr (SMEM) {
+    for (int k = threadIdx.x; k < a.nper; k += blockDim.x) sh[k] = node_from_params(a.params, a.nper, k);
+    return sh;
+  } else {
+    return a.nodes;
+  }
 }
 
 // Moving continuous index of one sample under the B-spline (+ initial affine):
@@ -252,6 +255,11 @@ __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
   __shared__ float4 AV[kChunkLen];
   __shared__ float qs[kChunkSlices][192];
   griddep_wait();  // several waves of blocks: dependents are released at each block's end
+  if (MATTES) mattes_value_groups(a);  // the value's group partials (the grid has at least one block per group)
+  if ((int)blockIdx.x >= a.nchunks) {
+    griddep_launch_dependents();
+    return;
+  }
   const int4 ch = a.chunks[blockIdx.x];
   const int len = ch.y - ch.x;
   const int B = a.bins;
@@ -330,10 +338,18 @@ __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
   griddep_wait();
   griddep_launch_dependents();
   const unsigned long long N = __ldcg(a.acc_n);
-  const int st = __ldcg(a.status);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.out[1] = (double)N;
-    if (MATTES) a.out[0] = st == GB_OK ? __ldcg(a.final_value) : 0.0;
+  // MeanSquares: the status of the value pass; Mattes: from the pass-1 totals, and
+  // block 0 forms the value from the chunk kernel's group partials
+  const int st = MATTES ? mattes_status(a) : __ldcg(a.status);
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    const double v = MATTES ? mattes_value_sum(a.part, mattes_groups(a.bins), threadIdx.x) : 0.0;
+    if (threadIdx.x == 0) {
+      a.out[1] = (double)N;
+      if (MATTES) {
+        *a.status = st;
+        a.out[0] = st == GB_OK ? -1.0 * v : 0.0;
+      }
+    }
   }
   if (n >= a.nper) return;
   const int e0 = __ldg(a.node_first + n), e1 = __ldg(a.node_first + n + 1);

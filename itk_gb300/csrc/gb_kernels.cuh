@@ -35,11 +35,8 @@ constexpr int kTicketPass1 = 176;         // last_block of Mattes pass 1
 constexpr int kTicketCount = 352;
 constexpr int kPartPass2 = 4096;          // offset of pass-2 partials (finalize blocks use [0, 4096))
 constexpr size_t kGroupOffset = kPartPass2 + (size_t)kMaxBlocks * 16;  // per-group partials: 128 groups x 16
-constexpr size_t kFinalOffset = kGroupOffset + 2048;
-constexpr size_t kMargOffset = kFinalOffset + 8;        // [T, 1/T]
-constexpr size_t kLogColOffset = kMargOffset + 8;       // bins doubles
-constexpr size_t kLogRowOffset = kLogColOffset + 4096;  // bins doubles
-constexpr size_t kScratchDoubles = kLogRowOffset + 4096;
+constexpr size_t kMargOffset = kGroupOffset + 2048;     // [T, 1/T]
+constexpr size_t kScratchDoubles = kMargOffset + 8;
 constexpr int kFinalizeThreads = 32;
 constexpr float kQScale = 67108864.f;  // 2^26 fixed point of histogram weights
 constexpr double kQInv = 1.0 / 67108864.0;
@@ -156,9 +153,6 @@ struct EvalArgs {
   // scratch (overwritten per evaluation)
   double* part;                 // per-block partials
   double* grp;                  // per-group partials
-  double* final_value;          // Mattes value handed from finalize to pass 2
-  double* logcol;               // bins: log of the fixed-point moving marginal
-  double* logrow;               // bins: log pf
   double* marg;                 // [fixed-point total T, 1 / T]
   float4* cache;
   float* pratio;
@@ -427,8 +421,17 @@ __device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, 
   }
 }
 
+static __device__ __noinline__ void mattes_pratio_table(const EvalArgs& a, double T, unsigned long long* cs,
+                                                        unsigned* fm);
+
+// u64 count -> float from its two 32-bit halves, FP32 arithmetic only (two roundings,
+// relative error below 2^-23)
+__device__ __forceinline__ float u64_to_float(unsigned long long v) {
+  return fmaf(__uint2float_rn((unsigned)(v >> 32)), 4294967296.f, __uint2float_rn((unsigned)v));
+}
+
 // End of Mattes pass 1 (any transform): flush the block histogram, marginals and
-// count; the last block computes the marginal logs.
+// count; the last block computes the marginal logs and the derivative's table.
 __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigned nv, unsigned long long* hist,
                                                       unsigned long long* cs, unsigned* fm) {
   const int B = a.bins;
@@ -449,10 +452,9 @@ __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigne
   }
   block_count(nv, a.acc_n);
   if (!last_block(a.tickets + kTicketPass1)) return;
-  // Last block: marginal logs once, in FP64, for the finalize.  With T the
-  // (fixed-point) joint-histogram total, p = h / T, pm = colsum / T and
-  // pf = count 2^26 / T, so log(p / pm) = log h - log colsum and
-  // log pf = log count + 26 ln 2 - log T.
+  // Last block: the fixed-point total T of the joint histogram (the value's
+  // normalization, JointPDFSum) and the derivative's table.  It is on the
+  // critical path, so it does no FP64 transcendental work.
   __shared__ unsigned long long tot_sh;
   if (threadIdx.x == 0) tot_sh = 0ull;
   __syncthreads();
@@ -461,16 +463,112 @@ __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigne
   atomicAdd(&tot_sh, t);
   __syncthreads();
   const double T = (double)tot_sh;
-  const double logT = T > 0.0 ? log(T) : 0.0;
-  for (int k = threadIdx.x; k < B; k += blockDim.x) {
-    const double c = (double)__ldcg(&a.colsum[k]);
-    a.logcol[k] = c > 0.0 ? log(c) : 0.0;
-    const double n = (double)__ldcg(&a.fmarg[k]);
-    a.logrow[k] = n > 0.0 ? log(n) + 26.0 * 0.69314718055994530942 - logT : 0.0;
-  }
   if (threadIdx.x == 0) {
     a.marg[0] = T;                         // fixed-point total
     a.marg[1] = T > 0.0 ? 1.0 / T : 0.0;   // normalization factor (of the fixed-point histogram)
+  }
+  mattes_pratio_table(a, T, cs, fm);
+}
+
+// The derivative's FP32 table log(p / pm) = log(h / colsum) (pRatio,
+// Mattes...v4.hxx:446-457), 0 where p, pm or pf is not above DBL_EPSILON:
+// for integer counts p > eps <=> h > floor(eps T) and pf > eps <=> count >
+// floor(eps T / 2^26).  Run by pass 1's last block; kept out of line so the
+// sample loop's code is unaffected.
+static __device__ __noinline__ void mattes_pratio_table(const EvalArgs& a, double T, unsigned long long* cs,
+                                                        unsigned* fm) {
+  const int B = a.bins;
+  const unsigned long long N = __ldcg(a.acc_n);
+  const bool bad = N == 0 || !(T * kQInv >= DBL_EPSILON);
+  const unsigned long long hthr = (unsigned long long)(DBL_EPSILON * T);
+  const unsigned long long fthr = (unsigned long long)(DBL_EPSILON * T * kQInv);
+  // marginals into shared memory (the block's own sums are flushed): column sums as
+  // floats (0 where pm is not above eps), fixed-bin validity
+  float* colf = reinterpret_cast<float*>(cs);
+  for (int k = threadIdx.x; k < B; k += blockDim.x) {
+    const unsigned long long c = __ldcg(&a.colsum[k]);
+    colf[k] = c > hthr ? u64_to_float(c) : 0.f;
+    fm[k] = __ldcg(&a.fmarg[k]) > fthr ? 1u : 0u;
+  }
+  __syncthreads();
+  constexpr int kBatch = 8;  // independent histogram loads in flight per thread
+  for (int k0 = threadIdx.x; k0 < B * B; k0 += kBatch * blockDim.x) {
+    unsigned long long h[kBatch];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int k = k0 + j * blockDim.x;
+      h[j] = (!bad && k < B * B) ? __ldcg(&a.hist[k]) : 0ull;
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int k = k0 + j * blockDim.x;
+      if (k >= B * B) break;
+      const int f = k / B, m = k - f * B;
+      const float c = colf[m];
+      a.pratio[k] = (h[j] > hthr && c > 0.f && fm[f]) ? logf(__fdiv_rn(u64_to_float(h[j]), c)) : 0.f;
+    }
+  }
+}
+
+// Mattes status after pass 1 (Mattes...v4.hxx:367-370 and the valid-point check).
+__device__ __forceinline__ int mattes_status(const EvalArgs& a) {
+  const unsigned long long N = __ldcg(a.acc_n);
+  if (N == 0) return GB_ERR_NO_VALID_POINTS;
+  return __ldcg(&a.marg[0]) * kQInv >= DBL_EPSILON ? GB_OK : GB_ERR_JOINT_PDF_SUM_ZERO;
+}
+
+// One warp, bins [32 g, 32 g + 32) of the joint histogram: the FP64 terms
+// p (log(p/pm) - log pf) (ComputeResults, Mattes...v4.hxx:358-499) summed over
+// the lanes by a fixed XOR tree, and the normalized PDF written out.  With T
+// the fixed-point total, p = h / T, pm = colsum / T and pf = count 2^26 / T, so
+// log(p / pm) = log h - log colsum and log pf = log count + 26 ln 2 - log T.
+// Every kernel that forms the value uses this and mattes_value_sum, so GetValue
+// and GetValueAndDerivative give the same bits.
+__device__ __forceinline__ double mattes_group_partial(const EvalArgs& a, int g, int lane) {
+  const int B = a.bins;
+  const double T = __ldcg(&a.marg[0]);
+  const double invT = __ldcg(&a.marg[1]);
+  const bool bad = (__ldcg(a.acc_n) == 0) || !(T * kQInv >= DBL_EPSILON);  // JointPDFSum
+  const int bin = g * 32 + lane;
+  double part = 0.0;
+  if (bin < B * B) {
+    const int f = bin / B, m = bin - f * B;
+    double p = 0.0;
+    if (!bad) {
+      const double h = (double)__ldcg(&a.hist[bin]);
+      const double c = (double)__ldcg(&a.colsum[m]);
+      const double n = (double)__ldcg(&a.fmarg[f]);
+      p = h * invT;
+      const double pm = c * invT;
+      const double pf = n * (invT * 67108864.0);
+      if (pf > DBL_EPSILON && pm > DBL_EPSILON && p > DBL_EPSILON) {
+        const double lr = log(h) - log(c);                                 // log(p / pm)
+        const double lf = log(n) + 26.0 * 0.69314718055994530942 - log(T);  // log pf
+        part = p * (lr - lf);
+      }
+    }
+    a.pdf_out[bin] = p;
+  }
+  return warp_sum_d(part);
+}
+
+__host__ __device__ inline int mattes_groups(int bins) { return (bins * bins + 31) / 32; }
+
+// Sum of the group partials part[0, ngroups): lane-strided, then a fixed XOR tree.
+__device__ __forceinline__ double mattes_value_sum(const double* part, int ngroups, int lane) {
+  double s = 0.0;
+  for (int r = lane; r < ngroups; r += 32) s += __ldcg(&part[r]);
+  return warp_sum_d(s);
+}
+
+// Group partials computed by the last warp of blocks b, b + gridDim.x, ... (all blocks participate).
+__device__ __forceinline__ void mattes_value_groups(const EvalArgs& a) {
+  if ((int)(threadIdx.x >> 5) != (int)(blockDim.x >> 5) - 1) return;
+  const int lane = threadIdx.x & 31;
+  const int ng = mattes_groups(a.bins);
+  for (int g = blockIdx.x; g < ng; g += gridDim.x) {
+    const double s = mattes_group_partial(a, g, lane);
+    if (lane == 0) a.part[g] = s;
   }
 }
 
@@ -532,56 +630,23 @@ __global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_p
 }
 
 #ifndef GB_KERNELS_HELPERS_ONLY
-// Mattes finalize: one thread per joint-histogram bin.  FP64 normalization and
-// p (log(p/pm) - log pf), with the marginal logs from pass 1's last block, and
-// the FP32 log(p/pm) table for pass 2 (ComputeResults, Mattes...v4.hxx:358-499;
-// JointPDFSum .hxx:533-541).  Block partials are added in block order by the
-// last block.
+// Mattes value without the derivative: one warp per group of 32 joint-histogram
+// bins (mattes_group_partial), the last block adds the group partials.  With the
+// derivative the same groups are formed by spare warps of the derivative pass
+// (k_mattes_pass2_affine, k_bspline_chunks) and summed at its end.
 __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a) {
   griddep_wait();
   griddep_launch_dependents();
-  const int B = a.bins;
   const int lane = threadIdx.x;
-  const double T = __ldcg(&a.marg[0]);
-  const double invT = __ldcg(&a.marg[1]);
-  const double total = T * kQInv;  // JointPDFSum
-  const unsigned long long N = __ldcg(a.acc_n);
-  const bool bad = (N == 0) || !(total >= DBL_EPSILON);
-  const int bin = blockIdx.x * kFinalizeThreads + lane;
-  double part = 0.0;
-  if (bin < B * B) {
-    const int f = bin / B, m = bin - f * B;
-    float pr = 0.f;
-    double p = 0.0;
-    if (!bad) {
-      const double h = (double)__ldcg(&a.hist[bin]);
-      p = h * invT;
-      const double pm = (double)__ldcg(&a.colsum[m]) * invT;
-      const double pf = (double)__ldcg(&a.fmarg[f]) * (invT * 67108864.0);
-      if (pf > DBL_EPSILON && pm > DBL_EPSILON && p > DBL_EPSILON) {
-        const double lr = log(h) - __ldcg(&a.logcol[m]);  // log(p / pm)
-        part = p * (lr - __ldcg(&a.logrow[f]));
-        pr = (float)lr;
-      }
-    }
-    a.pdf_out[bin] = p;
-    a.pratio[bin] = pr;
-  }
-  part = warp_sum_d(part);
+  const double part = mattes_group_partial(a, blockIdx.x, lane);
   if (lane == 0) a.part[blockIdx.x] = part;
   if (!last_block(a.tickets + kTicketFinalize)) return;
-  double s = 0.0;
-  for (int r = lane; r < (int)gridDim.x; r += 32) s += __ldcg(&a.part[r]);
-  s = warp_sum_d(s);
+  const double s = mattes_value_sum(a.part, (int)gridDim.x, lane);
   if (lane == 0) {
-    const int st = N == 0 ? GB_ERR_NO_VALID_POINTS : (bad ? GB_ERR_JOINT_PDF_SUM_ZERO : GB_OK);
+    const int st = mattes_status(a);
     *a.status = st;
-    const double value = st == GB_OK ? -1.0 * s : 0.0;  // metrics minimize: value = -MI
-    a.final_value[0] = value;
-    if (!a.with_derivative) {
-      a.out[0] = value;
-      a.out[1] = (double)N;
-    }
+    a.out[0] = st == GB_OK ? -1.0 * s : 0.0;  // metrics minimize: value = -MI
+    a.out[1] = (double)__ldcg(a.acc_n);
   }
 }
 
@@ -591,14 +656,16 @@ __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a
 // Streamed record tiles: each block owns a contiguous, tile-aligned range of
 // samples; thread 0 keeps kStreamStages tiles of (cache, sample) records in
 // flight with bulk asynchronous copies, completed on one mbarrier per stage.
-constexpr int kStreamStages = 4;
-constexpr int kStreamTile = kBlock;  // records per stage and stream
+constexpr int kStreamStages = 2;
+constexpr int kStreamPer = 2;                     // records per thread and tile
+constexpr int kStreamTile = kBlock * kStreamPer;  // records per stage and stream
 constexpr size_t kStreamBytes = (size_t)2 * kStreamStages * kStreamTile * sizeof(float4);
 
+// Whole tiles spread evenly: block b gets tiles [b T / G, (b + 1) T / G).
 __device__ __forceinline__ void block_range(int64_t n, int64_t& b0, int64_t& b1) {
-  const int64_t per = ((n + gridDim.x - 1) / gridDim.x + kStreamTile - 1) / kStreamTile * kStreamTile;
-  b0 = min(n, (int64_t)blockIdx.x * per);
-  b1 = min(n, b0 + per);
+  const int64_t tiles = (n + kStreamTile - 1) / kStreamTile;
+  b0 = min(n, (int64_t)blockIdx.x * tiles / gridDim.x * kStreamTile);
+  b1 = min(n, (int64_t)(blockIdx.x + 1) * tiles / gridDim.x * kStreamTile);
 }
 
 // Mattes pass 2, affine: derivative from the cached Parzen terms and gradients.
@@ -637,33 +704,38 @@ __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
     for (int t = 0; t < min(kStreamStages, ntiles); ++t) issue(t);
   for (int k = threadIdx.x; k < B * B; k += blockDim.x) pr[k] = __ldcg(&a.pratio[k]);
   load_consts(a.consts, K);
+  mattes_value_groups(a);  // the value's FP64 group partials, last warp (thread 0 feeds the copies)
   __syncthreads();
-  KahanF acc[12];
+  // plain FP32 per thread (a thread adds a few dozen samples; the warp tree and the
+  // FP64 cross-block sums follow)
+  float acc[12];
 #pragma unroll
-  for (int k = 0; k < 12; ++k) acc[k].zero();
+  for (int k = 0; k < 12; ++k) acc[k] = 0.f;
   int t = 0;
   for (; t < ntiles; ++t) {
     const int st = t % kStreamStages;
     if (!mbar_wait(&full[st], (unsigned)(t / kStreamStages) & 1u)) failed = 1;
     const int64_t r0 = b0 + (int64_t)t * kStreamTile;
-    if (!failed && threadIdx.x < b1 - r0) {
-      const float4 cc = cbuf[st * kStreamTile + threadIdx.x];
-      const float4 s = sbuf[st * kStreamTile + threadIdx.x];
-      if (cc.x == cc.x) {  // NaN term: rejected sample
-        int pdfm;
-        float tt, d[4];
-        parzen_window(cc.x, B, pdfm, tt);
-        parzen_deriv(tt, d);
-        const float* row = pr + __float_as_int(s.w) * B + pdfm;
-        const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
-        const float3 v = jac_vec(K, s.x, s.y, s.z);
-        const float vx = v.x, vy = v.y, vz = v.z;
-        const float t0 = w * cc.y, t1 = w * cc.z, t2 = w * cc.w;
-        acc[0].add(t0 * vx); acc[1].add(t0 * vy); acc[2].add(t0 * vz);
-        acc[3].add(t1 * vx); acc[4].add(t1 * vy); acc[5].add(t1 * vz);
-        acc[6].add(t2 * vx); acc[7].add(t2 * vy); acc[8].add(t2 * vz);
-        acc[9].add(t0); acc[10].add(t1); acc[11].add(t2);
-      }
+    const int cnt = (int)min((int64_t)kStreamTile, b1 - r0);
+#pragma unroll
+    for (int u = 0; u < kStreamPer; ++u) {
+      const int j = threadIdx.x + u * kBlock;
+      if (failed || j >= cnt) continue;
+      const float4 cc = cbuf[st * kStreamTile + j];
+      const float4 s = sbuf[st * kStreamTile + j];
+      if (cc.x != cc.x) continue;  // NaN term: rejected sample
+      int pdfm;
+      float tt, d[4];
+      parzen_window(cc.x, B, pdfm, tt);
+      parzen_deriv(tt, d);
+      const float* row = pr + __float_as_int(s.w) * B + pdfm;
+      const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
+      const float3 v = jac_vec(K, s.x, s.y, s.z);
+      const float t0 = w * cc.y, t1 = w * cc.z, t2 = w * cc.w;
+      acc[0] = fmaf(t0, v.x, acc[0]); acc[1] = fmaf(t0, v.y, acc[1]); acc[2] = fmaf(t0, v.z, acc[2]);
+      acc[3] = fmaf(t1, v.x, acc[3]); acc[4] = fmaf(t1, v.y, acc[4]); acc[5] = fmaf(t1, v.z, acc[5]);
+      acc[6] = fmaf(t2, v.x, acc[6]); acc[7] = fmaf(t2, v.y, acc[7]); acc[8] = fmaf(t2, v.z, acc[8]);
+      acc[9] += t0; acc[10] += t1; acc[11] += t2;
     }
     __syncthreads();  // stage st consumed by every thread
     if (failed) break;
@@ -681,21 +753,32 @@ __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
     }
     return;
   }
-  block_sums<12>(acc, red, blk);
+  KahanF kacc[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    kacc[k].s = acc[k];
+    kacc[k].c = 0.f;
+  }
+  block_sums<12>(kacc, red, blk);
   if (!grid_sums<12>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin)) return;
-  if (threadIdx.x == 0) {
-    const unsigned long long N = __ldcg(a.acc_n);
-    const int st = __ldcg(a.status);
-    a.out[1] = (double)N;
-    if (st != GB_OK) {
-      a.out[0] = 0.0;
-      for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = 0.0;
-      return;
+  // last block: the value from the group partials (all blocks wrote theirs before their tickets)
+  if (threadIdx.x < 32) {
+    const double s = mattes_value_sum(a.part, mattes_groups(B), threadIdx.x);
+    if (threadIdx.x == 0) {
+      const unsigned long long N = __ldcg(a.acc_n);
+      const int st = mattes_status(a);
+      *a.status = st;
+      a.out[1] = (double)N;
+      if (st != GB_OK) {
+        a.out[0] = 0.0;
+        for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = 0.0;
+        return;
+      }
+      // nFactor = -1 / (MovingImageBinSize * N), Mattes...Threader.hxx:446-457
+      const double nFactor = -1.0 / (a.m_bs * (double)N);
+      a.out[0] = -1.0 * s;
+      for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = fin[p] * nFactor;
     }
-    // nFactor = -1 / (MovingImageBinSize * N), Mattes...Threader.hxx:446-457
-    const double nFactor = -1.0 / (a.m_bs * (double)N);
-    a.out[0] = __ldcg(a.final_value);
-    for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = fin[p] * nFactor;
   }
 }
 

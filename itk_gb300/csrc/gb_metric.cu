@@ -680,10 +680,7 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.consts = m->d_consts.p;
   a.part = m->d_scratch.p;
   a.grp = m->d_scratch.p + kGroupOffset;
-  a.final_value = m->d_scratch.p + kFinalOffset;
   a.marg = m->d_scratch.p + kMargOffset;
-  a.logcol = m->d_scratch.p + kLogColOffset;
-  a.logrow = m->d_scratch.p + kLogRowOffset;
   a.cache = m->d_cache.p;
   a.pratio = m->d_pratio.p;
   a.pdf_out = m->d_pdf.p;
@@ -733,11 +730,10 @@ static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalAr
   return launch_chain(m, kernel, (unsigned)full_wave(m, kernel, smem, m->nsamples), kBlock, smem, a);
 }
 
-// B-spline / composite evaluation: node conversion, the per-sample pass
-// (MeanSquares, or Mattes pass 1 + finalize), then with the derivative the
-// per-chunk and per-parameter reductions.
+// B-spline / composite evaluation: node conversion (large grids), the per-sample
+// pass (MeanSquares or Mattes pass 1), then the value (Mattes without the
+// derivative: finalize) or the per-chunk and per-parameter reductions.
 static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool deriv) {
-  cudaStream_t st = m->stream;
   const int nper = (int)m->nper;
   const bool sm = a.nodes_smem != 0;
   if (!sm) {  // staged kernels convert the parameters themselves
@@ -765,14 +761,17 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
                 : launch_wave(m, k_mattes_pass1_bspline<kGradImage, false>, sh1, a);
     GB_CUDA(e);
     m->mark();
-    GB_CUDA(launch_chain(m, k_mattes_finalize, (unsigned)((B * B + kFinalizeThreads - 1) / kFinalizeThreads),
-                         kFinalizeThreads, 0, a));
-    m->mark();
+    if (!deriv) {  // with the derivative the value is formed by the chunk and params kernels
+      GB_CUDA(launch_chain(m, k_mattes_finalize, (unsigned)mattes_groups(B), kFinalizeThreads, 0, a));
+      m->mark();
+    }
   }
   if (!deriv) return GB_OK;
-  if (m->nchunks > 0) {
-    GB_CUDA(mattes ? launch_chain(m, k_bspline_chunks<true>, (unsigned)m->nchunks, kChunkLen, 0, a)
-                   : launch_chain(m, k_bspline_chunks<false>, (unsigned)m->nchunks, kChunkLen, 0, a));
+  // Mattes: at least one chunk-kernel block per value group
+  const int64_t cblocks = mattes ? std::max<int64_t>(m->nchunks, mattes_groups((int)m->bins)) : m->nchunks;
+  if (cblocks > 0) {
+    GB_CUDA(mattes ? launch_chain(m, k_bspline_chunks<true>, (unsigned)cblocks, kChunkLen, 0, a)
+                   : launch_chain(m, k_bspline_chunks<false>, (unsigned)cblocks, kChunkLen, 0, a));
     m->mark();
   }
   const int64_t threads = (int64_t)nper * 32;  // one warp per node
@@ -819,10 +818,10 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   GB_CUDA(cd ? launch_wave(m, k_mattes_pass1_affine<kGradCentralDifference>, sh1, a)
              : launch_wave(m, k_mattes_pass1_affine<kGradImage>, sh1, a));
   m->mark();
-  GB_CUDA(launch_chain(m, k_mattes_finalize, (unsigned)((B * B + kFinalizeThreads - 1) / kFinalizeThreads),
-                       kFinalizeThreads, 0, a));
-  m->mark();
-  if (deriv) {
+  if (!deriv) {  // with the derivative, pass 2 forms the value as well
+    GB_CUDA(launch_chain(m, k_mattes_finalize, (unsigned)mattes_groups(B), kFinalizeThreads, 0, a));
+    m->mark();
+  } else {
     GB_CUDA(launch_wave(m, k_mattes_pass2_affine, sh2, a));
     m->mark();
   }
