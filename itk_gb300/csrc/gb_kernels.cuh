@@ -71,9 +71,10 @@ __host__ __device__ inline void split_df(double x, float& hi, float& lo) {
 // dom2phys / dom_origin: domain coordinates -> physical point (the virtual
 // grid's index-to-physical map for dense sampling; null for a point set).
 // One output of the constants: e in [0, 9) the map's matrix entry (r, c) = (e / 3, e % 3),
-// e in [9, 12) its offset row e - 9, e == 12 the Jacobian terms.  Rows of the
-// physical-point -> moving-index map: A = P2I M, b = P2I (offset - origin_m),
-// offset = t + c - M c.
+// e in [9, 12) its offset row e - 9, e == 12 the Jacobian terms and M^T, e in
+// [13, 22) the entry e - 13 of P2I M.  Rows of the physical-point -> moving-index
+// map: A = P2I M, b = P2I (offset - origin_m), offset = t + c - M c.
+constexpr int kConstEntries = 22;
 __host__ __device__ inline void affine_const_entry(int e, const double* p, const double center[3],
                                                    const double m_p2i[9], const double m_origin[3],
                                                    const double* dom2phys, const double* dom_origin, EvalConsts& K) {
@@ -84,12 +85,14 @@ __host__ __device__ inline void affine_const_entry(int e, const double* p, const
     for (int i = 0; i < 9; ++i) K.U[i] = (float)U[i];
     for (int i = 0; i < 3; ++i) K.joff[i] = (float)(u0[i] - center[i]);
     for (int r = 0; r < 3; ++r)
-      for (int c = 0; c < 3; ++c) {
-        K.Mg[r * 3 + c] = (float)p[c * 3 + r];  // M^T
-        double s = 0.0;
-        for (int k = 0; k < 3; ++k) s = dadd(s, dmul(m_p2i[r * 3 + k], p[k * 3 + c]));
-        K.Pm[r * 3 + c] = (float)s;
-      }
+      for (int c = 0; c < 3; ++c) K.Mg[r * 3 + c] = (float)p[c * 3 + r];  // M^T
+    return;
+  }
+  if (e >= 13) {
+    const int r = (e - 13) / 3, c = (e - 13) % 3;
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) s = dadd(s, dmul(m_p2i[r * 3 + k], p[k * 3 + c]));
+    K.Pm[r * 3 + c] = (float)s;
     return;
   }
   const int r = e < 9 ? e / 3 : e - 9;
@@ -119,7 +122,7 @@ __host__ __device__ inline void affine_const_entry(int e, const double* p, const
 __host__ __device__ inline void affine_consts(const double* p, const double center[3], const double m_p2i[9],
                                               const double m_origin[3], const double* dom2phys,
                                               const double* dom_origin, EvalConsts& K) {
-  for (int e = 0; e < 13; ++e) affine_const_entry(e, p, center, m_p2i, m_origin, dom2phys, dom_origin, K);
+  for (int e = 0; e < kConstEntries; ++e) affine_const_entry(e, p, center, m_p2i, m_origin, dom2phys, dom_origin, K);
 }
 
 struct EvalArgs {
@@ -175,12 +178,14 @@ struct EvalArgs {
 #ifndef GB_KERNELS_HELPERS_ONLY
 // Device twin of the host constant computation (parameters already in HBM).
 // 13 threads, one output each, so the FP64 dependency chains run side by side.
+// One warp per output (lane 0): the entries take different code paths, and
+// within one warp those would run one after another at FP64 latency.
 __global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
   griddep_wait();
   griddep_launch_dependents();
-  if (threadIdx.x < 13)
-    affine_const_entry(threadIdx.x, a.params, a.center, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin,
-                       *out);
+  const int e = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0 && e < kConstEntries)
+    affine_const_entry(e, a.params, a.center, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin, *out);
 }
 
 #endif  // GB_KERNELS_HELPERS_ONLY
