@@ -352,8 +352,8 @@ def run_gb300(args):
     v_touched = roofline.touched_voxels(pts, U, moving)
     nodes = (args.mesh + 3) ** 3
     if bs:
-        # kernel order (nodes staged in shared memory): pass 1 (or MeanSquares), [finalize], chunks, params
-        kidx = 0
+        # kernel order of the device-resident call: nodes, pass 1 (or MeanSquares), chunks, params
+        kidx = 1
         if args.metric == "mattes":
             kbytes = roofline.mattes_pass1_bspline_bytes(n, v_touched, nodes)
             kname = "k_mattes_pass1_bspline"

@@ -51,7 +51,9 @@ __device__ __forceinline__ float4 node_from_params(const double* __restrict__ p,
 }
 
 #ifndef GB_KERNELS_HELPERS_ONLY
-// Global float4 node array, for grids too large to stage in shared memory.
+// Float4 node array from device-resident parameters (the host call converts on
+// the host and uploads the nodes); one conversion per node per evaluation,
+// rather than one per node in every block of the sample pass.
 __global__ void k_prepare_bspline(EvalArgs a) {
   griddep_wait();
   griddep_launch_dependents();
@@ -60,13 +62,12 @@ __global__ void k_prepare_bspline(EvalArgs a) {
 }
 #endif  // GB_KERNELS_HELPERS_ONLY
 
-// Nodes converted from the parameters into shared memory (SMEM), else the global
-// array written by k_prepare_bspline.  A compile-time choice, so node reads
-// compile to shared-memory loads rather than generic ones.
+// The nodes in shared memory (SMEM), else the global array.  A compile-time
+// choice, so node reads compile to shared-memory loads rather than generic ones.
 template <bool SMEM>
 __device__ __forceinline__ const float4* stage_nodes(const EvalArgs& a, float4* sh) {
   if constexpr (SMEM) {
-    for (int k = threadIdx.x; k < a.nper; k += blockDim.x) sh[k] = node_from_params(a.params, a.nper, k);
+    for (int k = threadIdx.x; k < a.nper; k += blockDim.x) sh[k] = __ldcg(a.nodes + k);
     return sh;
   } else {
     return a.nodes;

@@ -733,10 +733,10 @@ static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalAr
 // B-spline / composite evaluation: node conversion (large grids), the per-sample
 // pass (MeanSquares or Mattes pass 1), then the value (Mattes without the
 // derivative: finalize) or the per-chunk and per-parameter reductions.
-static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool deriv) {
+static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool deriv, bool device_params) {
   const int nper = (int)m->nper;
   const bool sm = a.nodes_smem != 0;
-  if (!sm) {  // staged kernels convert the parameters themselves
+  if (device_params) {  // the host call uploads converted nodes
     GB_CUDA(launch_chain(m, k_prepare_bspline, (unsigned)((nper + kBlock - 1) / kBlock), kBlock, 0, a));
     m->mark();
   }
@@ -783,14 +783,15 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
 }
 
 // Enqueues one evaluation; results land in d_out = [value, nvalid, derivative...].
-// device_consts: the affine constants are computed on the device from d_params
-// (otherwise the host has uploaded them).
-static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_consts) {
+// device_params: the parameters are in device memory (d_params), so the affine
+// constants or the B-spline nodes are formed on the device; otherwise the host
+// has uploaded them.
+static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_params) {
   cudaStream_t st = m->stream;
   EvalArgs a;
   fill_eval_args(m, a, d_params, d_out, deriv);
   GB_CUDA(cudaMemsetAsync(m->d_acc.p, 0, m->acc_bytes, st));
-  if (device_consts && !is_bspline(m))
+  if (device_params && !is_bspline(m))
     GB_CUDA(launch_chain(m, k_prepare_affine, 1, 32 * kConstEntries, 0, a, m->d_consts.p));
   if (m->nsamples == 0) {
     // no valid fixed sample at all: every point is invalid
@@ -804,7 +805,7 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   const bool cd = m->grad_source == GB_GRADIENT_CENTRAL_DIFFERENCE;
   m->nevents = 0;
   m->mark();
-  if (is_bspline(m)) return enqueue_eval_bspline(m, a, cd, deriv);
+  if (is_bspline(m)) return enqueue_eval_bspline(m, a, cd, deriv, device_params);
   if (m->kind == GB_METRIC_MEAN_SQUARES) {
     GB_CUDA(cd ? launch_wave(m, k_msq_affine<kGradCentralDifference>, 0, a)
                : launch_wave(m, k_msq_affine<kGradImage>, 0, a));
@@ -860,10 +861,13 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
   cudaStream_t st = m->stream;
   const double* d_params = nullptr;
   if (is_bspline(m)) {
-    // B-spline coefficients go to the device; k_prepare_bspline converts them there
-    std::copy(m->tparams.begin(), m->tparams.end(), m->h_params);
-    GB_CUDA(cudaMemcpyAsync(m->d_params.p, m->h_params, sizeof(double) * P, cudaMemcpyHostToDevice, st));
-    d_params = m->d_params.p;
+    // float4 coefficient nodes converted here (IEEE round to nearest, as the device
+    // conversion of the device-resident call), staged in the pinned parameter buffer
+    float4* hn = reinterpret_cast<float4*>(m->h_params);
+    const int64_t np = m->nper;
+    const double* c = m->tparams.data();
+    for (int64_t n = 0; n < np; ++n) hn[n] = make_float4((float)c[n], (float)c[np + n], (float)c[2 * np + n], 0.f);
+    GB_CUDA(cudaMemcpyAsync(m->d_nodes.p, hn, sizeof(float4) * np, cudaMemcpyHostToDevice, st));
   } else {
     // per-evaluation constants in FP64 on the host, uploaded with the parameters
     const bool dense = !m->use_sampled;
