@@ -178,13 +178,13 @@ struct EvalArgs {
 #ifndef GB_KERNELS_HELPERS_ONLY
 // Device twin of the host constant computation (parameters already in HBM).
 // 13 threads, one output each, so the FP64 dependency chains run side by side.
-// One warp per output (lane 0): the entries take different code paths, and
-// within one warp those would run one after another at FP64 latency.
+// One block (one warp, lane 0) per output: the entries take different code
+// paths, and one SM's FP64 pipe would serve them one after another.
 __global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
   griddep_wait();
   griddep_launch_dependents();
-  const int e = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0 && e < kConstEntries)
+  const int e = blockIdx.x;
+  if (threadIdx.x == 0 && e < kConstEntries)
     affine_const_entry(e, a.params, a.center, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin, *out);
 }
 

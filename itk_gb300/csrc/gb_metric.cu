@@ -792,7 +792,7 @@ static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, boo
   fill_eval_args(m, a, d_params, d_out, deriv);
   GB_CUDA(cudaMemsetAsync(m->d_acc.p, 0, m->acc_bytes, st));
   if (device_params && !is_bspline(m))
-    GB_CUDA(launch_chain(m, k_prepare_affine, 1, 32 * kConstEntries, 0, a, m->d_consts.p));
+    GB_CUDA(launch_chain(m, k_prepare_affine, kConstEntries, 32, 0, a, m->d_consts.p));
   if (m->nsamples == 0) {
     // no valid fixed sample at all: every point is invalid
     const int code = GB_ERR_NO_VALID_POINTS;
