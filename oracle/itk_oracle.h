@@ -166,6 +166,32 @@ int orc_interpolate_flat(const float *img, const int64_t size[3], const double g
 int orc_central_difference_flat(const float *img, const int64_t size[3], const double geo[15],
                                 const double *points, int64_t n, double *grads);
 
+/* ---- per-level image filters (itk_oracle_filters.c) ---- */
+
+/* RecursiveGaussianImageFilter coefficients (Farneback / Deriche IIR), order 0, 1 or 2 */
+typedef struct {
+  double N0, N1, N2, N3;
+  double D1, D2, D3, D4;
+  double M1, M2, M3, M4;
+  double BN1, BN2, BN3, BN4;
+  double BM1, BM2, BM3, BM4;
+} orc_rg_coef;
+
+int orc_rg_setup(double sigma, double spacing, int order, int normalize_across_scale, orc_rg_coef *c);
+/* RecursiveSeparableImageFilter::FilterDataArray on one line of length ln >= 4 */
+void orc_rg_filter_line(const orc_rg_coef *c, const double *data, double *outs, double *scratch, int64_t ln);
+/* SmoothingRecursiveGaussianImageFilter on Image<float,3> (sigma in physical units per axis) */
+int orc_smooth_recursive_gaussian(const float *in, float *out, const int64_t size[3], const double spacing[3],
+                                  const double sigma[3]);
+/* GradientRecursiveGaussianImageFilter on Image<float,3>: 3 doubles per voxel */
+int orc_gradient_recursive_gaussian(const float *in, double *out, const int64_t size[3], const double spacing[3],
+                                    const double direction[9], double sigma, int normalize_across_scale,
+                                    int use_image_direction);
+/* ShrinkImageFilter output geometry (start index 0) */
+int orc_shrink_geometry(const int64_t size[3], const double spacing[3], const double origin[3],
+                        const double direction[9], const int64_t factors[3], int64_t out_size[3],
+                        double out_spacing[3], double out_origin[3]);
+
 #ifdef __cplusplus
 }
 #endif

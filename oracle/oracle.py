@@ -44,7 +44,7 @@ def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (portable C, no ISA flags)."""
     if force or not os.path.exists(_LIB_PATH) or (
         os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(os.path.join(_HERE, f))
-                                          for f in ("itk_oracle.c", "itk_oracle.h"))):
+                                          for f in ("itk_oracle.c", "itk_oracle_filters.c", "itk_oracle.h"))):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -68,6 +68,12 @@ def lib():
         L.orc_bspline3.restype = ctypes.c_double
         L.orc_bspline3_derivative.argtypes = [ctypes.c_double]
         L.orc_bspline3_derivative.restype = ctypes.c_double
+        d, ci = ctypes.c_double, ctypes.c_int
+        L.orc_rg_setup.argtypes = [d, d, ci, ci, P]
+        L.orc_rg_filter_line.argtypes = [P, P, P, P, i64]
+        L.orc_smooth_recursive_gaussian.argtypes = [P, P, P, P, P]
+        L.orc_gradient_recursive_gaussian.argtypes = [P, P, P, P, P, d, ci, ci]
+        L.orc_shrink_geometry.argtypes = [P] * 8
         _lib = L
     return _lib
 
@@ -206,6 +212,74 @@ def bspline_weights(cindex):
     st = np.zeros(3, np.int64)
     L.orc_bspline_weights(_p(ci), _p(w), _p(st))
     return w, st
+
+
+class RGCoef(ctypes.Structure):
+    """orc_rg_coef: RecursiveGaussianImageFilter's IIR coefficients."""
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("N0", "N1", "N2", "N3", "D1", "D2", "D3", "D4", "M1", "M2", "M3", "M4",
+                 "BN1", "BN2", "BN3", "BN4", "BM1", "BM2", "BM3", "BM4")]
+
+
+def rg_coefficients(sigma, spacing=1.0, order=0, normalize_across_scale=False):
+    c = RGCoef()
+    rc = lib().orc_rg_setup(float(sigma), float(spacing), int(order), int(normalize_across_scale),
+                            ctypes.addressof(c))
+    if rc:
+        raise ValueError(f"oracle rg_setup error {STATUS_NAMES.get(rc, rc)}")
+    return c
+
+
+def rg_filter_line(line, sigma, spacing=1.0, order=0, normalize_across_scale=False):
+    """RecursiveGaussianImageFilter on one 1-D line (FilterDataArray in double)."""
+    c = rg_coefficients(sigma, spacing, order, normalize_across_scale)
+    data = np.ascontiguousarray(np.asarray(line, np.float64))
+    outs = np.zeros_like(data)
+    scratch = np.zeros_like(data)
+    lib().orc_rg_filter_line(ctypes.addressof(c), _p(data), _p(outs), _p(scratch), data.size)
+    return outs
+
+
+def smooth_recursive_gaussian(img, spacing, sigma):
+    """SmoothingRecursiveGaussianImageFilter<Image<float,3>> (sigma per axis, physical units)."""
+    a = _img(img)
+    out = np.zeros_like(a)
+    size = np.array([a.shape[2], a.shape[1], a.shape[0]], np.int64)
+    sp = np.asarray(spacing, np.float64).reshape(3)
+    sg = np.broadcast_to(np.asarray(sigma, np.float64), (3,)).copy()
+    rc = lib().orc_smooth_recursive_gaussian(_p(a), _p(out), _p(size), _p(sp), _p(sg))
+    if rc:
+        raise ValueError(f"oracle smoothing error {STATUS_NAMES.get(rc, rc)}")
+    return out
+
+
+def gradient_recursive_gaussian(img, spacing, direction, sigma, normalize_across_scale=True,
+                                use_image_direction=True):
+    """GradientRecursiveGaussianImageFilter<Image<float,3>>: (nz, ny, nx, 3) float64."""
+    a = _img(img)
+    out = np.zeros(a.shape + (3,), np.float64)
+    size = np.array([a.shape[2], a.shape[1], a.shape[0]], np.int64)
+    sp = np.asarray(spacing, np.float64).reshape(3)
+    d = np.ascontiguousarray(np.asarray(direction, np.float64).reshape(9))
+    rc = lib().orc_gradient_recursive_gaussian(_p(a), _p(out), _p(size), _p(sp), _p(d), ctypes.c_double(sigma),
+                                               int(normalize_across_scale), int(use_image_direction))
+    if rc:
+        raise ValueError(f"oracle gradient error {STATUS_NAMES.get(rc, rc)}")
+    return out
+
+
+def shrink_geometry(size_xyz, spacing, origin, direction, factors):
+    """ShrinkImageFilter output (size, spacing, origin)."""
+    sz = np.asarray(size_xyz, np.int64).reshape(3)
+    sp = np.asarray(spacing, np.float64).reshape(3)
+    org = np.asarray(origin, np.float64).reshape(3)
+    d = np.ascontiguousarray(np.asarray(direction, np.float64).reshape(9))
+    f = np.asarray(factors, np.int64).reshape(3)
+    osz = np.zeros(3, np.int64)
+    osp = np.zeros(3, np.float64)
+    oorg = np.zeros(3, np.float64)
+    lib().orc_shrink_geometry(_p(sz), _p(sp), _p(org), _p(d), _p(f), _p(osz), _p(osp), _p(oorg))
+    return osz, osp, oorg
 
 
 def bspline3(u):
