@@ -111,6 +111,20 @@ int gb_metric_set_moving_gradient_image(gb_metric *m, const double *gradient_xyz
 int gb_metric_set_virtual_domain(gb_metric *m, const int64_t size[3], const double spacing[3],
                                  const double origin[3], const double direction[9]);
 
+/* Per-level set-up of ImageRegistrationMethodv4::InitializeRegistrationAtEachLevel
+ * (Registration/RegistrationMethodsv4/include/itkImageRegistrationMethodv4.hxx:262-640),
+ * done on the device by gb_metric_initialize, so a level's images never leave HBM:
+ *   level smoothing: the fixed and moving images pass through
+ *     SmoothingRecursiveGaussianImageFilter with sigma in physical units, or in
+ *     voxels (times each axis' spacing) when sigma_in_physical_units = 0
+ *     (SetSmoothingSigmasAreSpecifiedInPhysicalUnits); 0 = no smoothing;
+ *   level shrink: the virtual domain is the fixed image's geometry through
+ *     ShrinkImageFilter with these factors ({1,1,1} = full resolution); a domain
+ *     set with gb_metric_set_virtual_domain takes precedence.
+ * The images given with gb_metric_set_image stay unmodified. */
+int gb_metric_set_level_smoothing(gb_metric *m, double sigma, int sigma_in_physical_units);
+int gb_metric_set_level_shrink(gb_metric *m, const int64_t factors[3]);
+
 /* Sampled point sets: float xyz, n points.  virtual_space = 1 replaces
  * SetVirtualSampledPointSet + UseVirtualSampledPointSetOn (what
  * ImageRegistrationMethodv4::SetMetricSamplePoints installs,
@@ -206,13 +220,44 @@ int gb_msq_affine_noalloc(const void *device_samples, int64_t n, const void *dev
                           const double moving_origin[3], const double moving_direction[9],
                           const double params[12], const double center[3], double *device_out, uint64_t stream);
 
+/* ---- device image filters ---------------------------------------------- */
+/* Device forms of the filters the registration method and the metric run per
+ * level; device buffers in, device buffers out, enqueued on `stream` (0: the
+ * legacy default stream); scratch comes from the stream-ordered allocator.
+ * Images are x-fastest float buffers of size[0] x size[1] x size[2], each axis >= 4.
+ *
+ * SmoothingRecursiveGaussianImageFilter<Image<float,3>> with a sigma per axis in
+ * physical units (Filtering/Smoothing/include/itkSmoothingRecursiveGaussianImageFilter.hxx);
+ * d_in and d_out may be the same buffer. */
+int gb_smooth_recursive_gaussian(gb_ctx *ctx, uint64_t stream, const float *d_in, float *d_out, const int64_t size[3],
+                                 const double spacing[3], const double sigma[3]);
+/* GradientRecursiveGaussianImageFilter<Image<float,3>>
+ * (Filtering/ImageGradient/include/itkGradientRecursiveGaussianImageFilter.hxx):
+ * 3 floats (x, y, z) per voxel in d_out_xyz. */
+int gb_gradient_recursive_gaussian(gb_ctx *ctx, uint64_t stream, const float *d_in, float *d_out_xyz,
+                                   const int64_t size[3], const double spacing[3], const double direction[9],
+                                   double sigma, int normalize_across_scale, int use_image_direction);
+/* The same two filters on host buffers (copied in and out; synchronous). */
+int gb_smooth_recursive_gaussian_host(gb_ctx *ctx, const float *in, float *out, const int64_t size[3],
+                                      const double spacing[3], const double sigma[3]);
+int gb_gradient_recursive_gaussian_host(gb_ctx *ctx, const float *in, float *out_xyz, const int64_t size[3],
+                                        const double spacing[3], const double direction[9], double sigma,
+                                        int normalize_across_scale, int use_image_direction);
+/* ShrinkImageFilter output geometry for start index 0
+ * (Filtering/ImageGrid/include/itkShrinkImageFilter.hxx:230-290). */
+int gb_shrink_geometry(const int64_t size[3], const double spacing[3], const double origin[3],
+                       const double direction[9], const int64_t factors[3], int64_t out_size[3],
+                       double out_spacing[3], double out_origin[3]);
+
 /* ---- observability ----------------------------------------------------- */
 /* Per-kernel CUDA-event timing of evaluations (the reference's TimeProbe,
  * Core/Common/include/itkTimeProbe.h:44, at kernel granularity).  When on,
  * each evaluation records an event before and after every kernel it launches. */
 int gb_metric_set_profiling(gb_metric *m, int on);
 /* Device milliseconds of each kernel of the last evaluation, in launch order
- * (MeanSquares: 1 kernel; Mattes: pass 1, finalize, pass 2).  Synchronizes. */
+ * (affine MeanSquares: 1 kernel; affine Mattes: pass 1 then pass 2, or the
+ * value-only finalize; B-spline: [node conversion], the sample pass, [Mattes
+ * finalize], chunk sums, parameter gather).  Synchronizes. */
 int gb_metric_get_kernel_times(gb_metric *m, double *ms, int max_kernels, int *count);
 
 #ifdef __cplusplus

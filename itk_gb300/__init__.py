@@ -6,13 +6,16 @@ B-spline and [affine, B-spline] composite transforms, computed by hand-written
 sm_103a CUDA kernels behind the C ABI in include/itk_gb300.h.
 """
 from ._capi import ExceptionObject, lib, library_path
+from .filters import (GradientRecursiveGaussianImageFilter, ShrinkImageFilter, SmoothingRecursiveGaussianImageFilter,
+                      shrink_geometry)
 from .image import GradientImage, Image
 from .metrics import (ImageToImageMetricv4, MattesMutualInformationImageToImageMetricv4,
                       MeanSquaresImageToImageMetricv4, context)
 from .transforms import AffineTransform, BSplineTransform, CompositeTransform
 
 __all__ = [
-    "AffineTransform", "BSplineTransform", "CompositeTransform", "ExceptionObject", "GradientImage", "Image",
-    "ImageToImageMetricv4", "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
-    "context", "lib", "library_path",
+    "AffineTransform", "BSplineTransform", "CompositeTransform", "ExceptionObject", "GradientImage",
+    "GradientRecursiveGaussianImageFilter", "Image", "ImageToImageMetricv4",
+    "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4", "ShrinkImageFilter",
+    "SmoothingRecursiveGaussianImageFilter", "context", "lib", "library_path", "shrink_geometry",
 ]

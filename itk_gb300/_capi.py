@@ -61,6 +61,13 @@ SIGNATURES = {
     "gb_metric_set_gradient_source": [_P, _I],
     "gb_metric_set_moving_gradient_image": [_P, _P],
     "gb_metric_set_virtual_domain": [_P, _P, _P, _P, _P],
+    "gb_metric_set_level_smoothing": [_P, _D, _I],
+    "gb_metric_set_level_shrink": [_P, _P],
+    "gb_smooth_recursive_gaussian": [_P, _U64, _P, _P, _P, _P, _P],
+    "gb_gradient_recursive_gaussian": [_P, _U64, _P, _P, _P, _P, _P, _D, _I, _I],
+    "gb_smooth_recursive_gaussian_host": [_P, _P, _P, _P, _P, _P],
+    "gb_gradient_recursive_gaussian_host": [_P, _P, _P, _P, _P, _P, _D, _I, _I],
+    "gb_shrink_geometry": [_P, _P, _P, _P, _P, _P, _P, _P],
     "gb_metric_set_sampled_points": [_P, _P, _I64, _I],
     "gb_metric_use_sampled_point_set": [_P, _I],
     "gb_metric_set_moving_transform": [_P, _I, _P, _I64, _P, _I64],

@@ -59,6 +59,15 @@ cudaError_t sort_pairs_u64(const uint64_t* keys_in, uint64_t* keys_out, const ui
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
 
+// Device image filters (gb_filters.cu).
+int smooth_rg_device(cudaStream_t st, const float* in, float* out, float* t1, float* t2, const int64_t size[3],
+                     const double spacing[3], const double sigma[3]);
+int gradient_rg_device(cudaStream_t st, const float* in, const int64_t size[3], const double spacing[3],
+                       const double direction[9], double sigma, bool normalize_across_scale, bool use_direction,
+                       float4* out4, float* out3);
+void shrink_geometry(const int64_t size[3], const double spacing[3], const double origin[3], const double dir[9],
+                     const int64_t factors[3], int64_t out_size[3], double out_spacing[3], double out_origin[3]);
+
 }  // namespace gb
 
 struct gb_ctx {
@@ -75,6 +84,13 @@ struct gb_metric {
   gb::Geom fixed, moving, virt;
   bool virt_user = false;
   gb::DevBuf<float> d_fixed, d_moving;
+  // per-level set-up (gb_metric_set_level_smoothing / _shrink)
+  double level_sigma = 0.0;
+  bool level_sigma_physical = true;
+  int64_t level_shrink[3] = {1, 1, 1};
+  gb::DevBuf<float> d_fixed_s, d_moving_s;  // the level's smoothed images
+  const float* fixed_img() const { return level_sigma > 0.0 ? d_fixed_s.p : d_fixed.p; }
+  const float* moving_img() const { return level_sigma > 0.0 ? d_moving_s.p : d_moving.p; }
   gb::DevBuf<double> d_grad_in;  // caller-supplied gradient image (xyz doubles)
   int grad_source = GB_GRADIENT_IMAGE;
   bool grad_set = false;

@@ -289,6 +289,22 @@ extern "C" int gb_metric_set_virtual_domain(gb_metric* m, const int64_t size[3],
   return GB_OK;
 }
 
+extern "C" int gb_metric_set_level_smoothing(gb_metric* m, double sigma, int sigma_in_physical_units) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  if (!(sigma >= 0.0) || !std::isfinite(sigma)) return fail(GB_ERR_BAD_ARG, "smoothing sigma must be >= 0");
+  m->level_sigma = sigma;
+  m->level_sigma_physical = sigma_in_physical_units != 0;
+  m->initialized = false;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_level_shrink(gb_metric* m, const int64_t factors[3]) {
+  if (!m || !factors) return fail(GB_ERR_BAD_ARG, "null argument");
+  for (int i = 0; i < 3; ++i) m->level_shrink[i] = factors[i] < 1 ? 1 : factors[i];  // ShrinkImageFilter clamps to 1
+  m->initialized = false;
+  return GB_OK;
+}
+
 extern "C" int gb_metric_set_sampled_points(gb_metric* m, const float* xyz, int64_t n, int virtual_space) {
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (n < 0 || (n > 0 && !xyz)) return fail(GB_ERR_BAD_ARG, "bad point array");
@@ -389,8 +405,6 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   if (m->tkind < 0) return fail(GB_ERR_BAD_ARG, "MovingTransform is not present");
   if (m->grad_source == GB_GRADIENT_IMAGE && !m->grad_set)
     return fail(GB_ERR_BAD_ARG, "gradient source is a gradient image but none was set");
-  if (m->grad_source == GB_GRADIENT_RECURSIVE_GAUSSIAN)
-    return fail(GB_ERR_UNSUPPORTED, "device recursive-Gaussian gradient is not available in this build");
   const bool bspline = is_bspline(m);
   double g_p2i[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   if (bspline) {
@@ -408,7 +422,40 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   GB_CUDA(cudaSetDevice(m->ctx->device));
   m->initialized = false;
   cudaStream_t st = m->stream;
-  if (!m->virt_user) m->virt = m->fixed;  // virtual domain from the fixed image, itkImageToImageMetricv4.hxx:98-112
+
+  // ---- the level's images: both through SmoothingRecursiveGaussianImageFilter
+  // (ImageRegistrationMethodv4.hxx:590-640), kept on the device
+  if (m->level_sigma > 0.0) {
+    for (int w = 0; w < 2; ++w) {
+      const Geom& g = w == 0 ? m->fixed : m->moving;
+      const float* src = w == 0 ? m->d_fixed.p : m->d_moving.p;
+      DevBuf<float>& dst = w == 0 ? m->d_fixed_s : m->d_moving_s;
+      double sig[3];
+      for (int i = 0; i < 3; ++i) sig[i] = m->level_sigma_physical ? m->level_sigma : m->level_sigma * g.spacing[i];
+      const int64_t nv = g.voxels();
+      DevBuf<float> tmp;
+      GB_CUDA(dst.alloc(nv));
+      GB_CUDA(tmp.alloc(2 * (size_t)nv));
+      const int rc = smooth_rg_device(st, src, dst.p, tmp.p, tmp.p + nv, g.size, g.spacing, sig);
+      if (rc) return rc;
+      GB_CUDA(cudaStreamSynchronize(st));  // tmp is released at the end of this scope
+    }
+  } else {
+    m->d_fixed_s.reset();
+    m->d_moving_s.reset();
+  }
+  // ---- virtual domain: the fixed image's geometry (itkImageToImageMetricv4.hxx:98-112),
+  // shrunk for the level (ShrinkImageFilter, ImageRegistrationMethodv4.hxx:448-461)
+  if (!m->virt_user) {
+    m->virt = m->fixed;
+    if (m->level_shrink[0] != 1 || m->level_shrink[1] != 1 || m->level_shrink[2] != 1) {
+      int64_t sz[3];
+      double sp[3], org[3];
+      shrink_geometry(m->fixed.size, m->fixed.spacing, m->fixed.origin, m->fixed.dir, m->level_shrink, sz, sp, org);
+      const int rc = geom_init(m->virt, sz, sp, org, m->fixed.dir);
+      if (rc) return rc;
+    }
+  }
 
   const bool sampled = m->use_sampled;
   if (sampled && m->h_points.empty()) return fail(GB_ERR_BAD_ARG, "VirtualSampledPointSet must have 1 or more points.");
@@ -431,11 +478,11 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
                    float_to_ordered_host(-FLT_MAX)};
     GB_CUDA(cudaMemcpyAsync(d_mm.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
     if (sampled) {
-      k_minmax_points<<<grid_for(m, ncand, 4), kBlock, 0, st>>>(d_pts.p, ncand, dfixed, m->d_fixed.p, d_mm.p);
+      k_minmax_points<<<grid_for(m, ncand, 4), kBlock, 0, st>>>(d_pts.p, ncand, dfixed, m->fixed_img(), d_mm.p);
     } else {
-      k_minmax<<<grid_for(m, m->fixed.voxels(), 4), kBlock, 0, st>>>(m->d_fixed.p, m->fixed.voxels(), d_mm.p);
+      k_minmax<<<grid_for(m, m->fixed.voxels(), 4), kBlock, 0, st>>>(m->fixed_img(), m->fixed.voxels(), d_mm.p);
     }
-    k_minmax<<<grid_for(m, m->moving.voxels(), 4), kBlock, 0, st>>>(m->d_moving.p, m->moving.voxels(), d_mm.p + 2);
+    k_minmax<<<grid_for(m, m->moving.voxels(), 4), kBlock, 0, st>>>(m->moving_img(), m->moving.voxels(), d_mm.p + 2);
     GB_CUDA(cudaGetLastError());
     int res[4];
     GB_CUDA(cudaMemcpyAsync(res, d_mm.p, sizeof(res), cudaMemcpyDeviceToHost, st));
@@ -490,7 +537,7 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   b.points_virtual = m->points_virtual ? 1 : 0;
   b.virt = dvirt;
   b.fixed = dfixed;
-  b.fixed_img = m->d_fixed.p;
+  b.fixed_img = m->fixed_img();
   b.mattes = m->kind == GB_METRIC_MATTES;
   b.bins = (int)m->bins;
   b.f_bs = m->mstate[4];
@@ -589,14 +636,24 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     GB_CUDA(cudaStreamSynchronize(st));  // the host vectors die here
   }
 
-  // ---- moving image: packed (value, gradient) for the gradient-image path
+  // ---- moving image: packed (value, gradient) for the gradient-image paths
   if (m->grad_source == GB_GRADIENT_IMAGE) {
     const int64_t nv = m->moving.voxels();
     m->d_mov4.reset();
     GB_CUDA(m->d_mov4.alloc(nv));
-    k_pack_moving<<<(unsigned)((nv + kBlock - 1) / kBlock), kBlock, 0, st>>>(m->d_moving.p, m->d_grad_in.p, nv,
+    k_pack_moving<<<(unsigned)((nv + kBlock - 1) / kBlock), kBlock, 0, st>>>(m->moving_img(), m->d_grad_in.p, nv,
                                                                               m->d_mov4.p);
     GB_CUDA(cudaGetLastError());
+  } else if (m->grad_source == GB_GRADIENT_RECURSIVE_GAUSSIAN) {
+    // the metric's default gradient filter: sigma = max spacing, normalized across
+    // scale, image direction applied (itkImageToImageMetricv4.hxx:488-503)
+    const int64_t nv = m->moving.voxels();
+    m->d_mov4.reset();
+    GB_CUDA(m->d_mov4.alloc(nv));
+    const double sigma = std::max(m->moving.spacing[0], std::max(m->moving.spacing[1], m->moving.spacing[2]));
+    const int rc = gradient_rg_device(st, m->moving_img(), m->moving.size, m->moving.spacing, m->moving.dir, sigma,
+                                      true, true, m->d_mov4.p, nullptr);
+    if (rc) return rc;
   }
 
   // ---- evaluation buffers
@@ -647,7 +704,7 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.samples = m->d_samples.p;
   a.n = m->nsamples;
   a.mov4 = m->d_mov4.p;
-  a.mov1 = m->d_moving.p;
+  a.mov1 = m->moving_img();
   a.nx = (int)m->moving.size[0];
   a.ny = (int)m->moving.size[1];
   a.nz = (int)m->moving.size[2];

@@ -52,6 +52,9 @@ class ImageToImageMetricv4:
         self._virtual = None
         self._value = np.finfo(np.float64).max
         self._nparams = 0
+        self._level_sigma = 0.0
+        self._level_sigma_physical = True
+        self._level_shrink = (1, 1, 1)
 
     def __del__(self):
         try:
@@ -120,6 +123,18 @@ class ImageToImageMetricv4:
     def UseVirtualSampledPointSetOn(self):
         self._points_virtual = True
 
+    # ---- per-level set-up of ImageRegistrationMethodv4 (done on the device at Initialize)
+    def SetLevelSmoothingSigma(self, sigma: float, in_physical_units: bool = True):
+        """Smooth both images with SmoothingRecursiveGaussianImageFilter(sigma) at Initialize
+        (ImageRegistrationMethodv4.hxx:590-640); 0 = no smoothing.  The inputs stay unmodified."""
+        self._level_sigma = float(sigma)
+        self._level_sigma_physical = bool(in_physical_units)
+
+    def SetLevelShrinkFactors(self, factors):
+        """Virtual domain = the fixed image's geometry through ShrinkImageFilter(factors)
+        (ImageRegistrationMethodv4.hxx:448-461), unless a virtual domain was set."""
+        self._level_shrink = tuple(int(f) for f in np.broadcast_to(np.asarray(factors), (3,)))
+
     # ---- set-up
     def _push_transform(self):
         kind, params, fixed = self._transform.flat()
@@ -149,6 +164,8 @@ class ImageToImageMetricv4:
             check(self._L.gb_metric_set_sampled_points(self._h, ptr(self._points), self._points.shape[0],
                                                        int(self._points_virtual)))
         check(self._L.gb_metric_use_sampled_point_set(self._h, int(self._use_sampled)))
+        check(self._L.gb_metric_set_level_smoothing(self._h, self._level_sigma, int(self._level_sigma_physical)))
+        check(self._L.gb_metric_set_level_shrink(self._h, ptr(i64(self._level_shrink))))
         self._pre_initialize()
         check(self._L.gb_metric_initialize(self._h))
 

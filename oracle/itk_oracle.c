@@ -964,7 +964,8 @@ int orc_transform_from_flat(orc_transform *t, int tkind, const double *tparams, 
 
 static int inputs_from_flat(orc_inputs *in, const float *fixed, const int64_t fsize[3], const double fgeo[15],
                             const float *moving, const int64_t msize[3], const double mgeo[15],
-                            const double *moving_grad, const float *points, int64_t npoints, int nthreads)
+                            const double *moving_grad, const float *points, int64_t npoints, int nthreads,
+                            const int64_t *vsize, const double *vgeo)
 {
   int rc;
   memset(in, 0, sizeof(*in));
@@ -973,6 +974,10 @@ static int inputs_from_flat(orc_inputs *in, const float *fixed, const int64_t fs
   geom_from_flat(&in->moving_geom, msize, mgeo, &rc);
   if (rc) return rc;
   in->virtual_geom = in->fixed_geom; /* virtual domain defaults to the fixed image, itkImageToImageMetricv4.hxx:98-112 */
+  if (vsize) {
+    geom_from_flat(&in->virtual_geom, vsize, vgeo, &rc);
+    if (rc) return rc;
+  }
   in->fixed = fixed;
   in->moving = moving;
   in->moving_grad = moving_grad;
@@ -989,9 +994,21 @@ int orc_msq_flat(const float *fixed, const int64_t fsize[3], const double fgeo[1
                  int64_t nfixed, int nthreads, int compute_derivative, double *value, double *derivative,
                  uint64_t *nvalid)
 {
+  return orc_msq_flat_v(fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, tkind, tparams,
+                        nparams, tfixed, nfixed, nthreads, compute_derivative, value, derivative, nvalid, NULL,
+                        NULL);
+}
+
+int orc_msq_flat_v(const float *fixed, const int64_t fsize[3], const double fgeo[15], const float *moving,
+                   const int64_t msize[3], const double mgeo[15], const double *moving_grad, const float *points,
+                   int64_t npoints, int tkind, const double *tparams, int64_t nparams, const double *tfixed,
+                   int64_t nfixed, int nthreads, int compute_derivative, double *value, double *derivative,
+                   uint64_t *nvalid, const int64_t *vsize, const double *vgeo)
+{
   orc_inputs in;
   orc_transform t;
-  int rc = inputs_from_flat(&in, fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, nthreads);
+  int rc = inputs_from_flat(&in, fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, nthreads,
+                            vsize, vgeo);
   if (rc) return rc;
   rc = orc_transform_from_flat(&t, tkind, tparams, nparams, tfixed, nfixed);
   if (rc) return rc;
@@ -1004,10 +1021,23 @@ int orc_mattes_flat(const float *fixed, const int64_t fsize[3], const double fge
                     int64_t nfixed, int64_t bins, int nthreads, int compute_derivative, double *value,
                     double *derivative, uint64_t *nvalid, double *joint_pdf, double *state_out)
 {
+  return orc_mattes_flat_v(fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, tkind, tparams,
+                           nparams, tfixed, nfixed, bins, nthreads, compute_derivative, value, derivative, nvalid,
+                           joint_pdf, state_out, NULL, NULL);
+}
+
+int orc_mattes_flat_v(const float *fixed, const int64_t fsize[3], const double fgeo[15], const float *moving,
+                      const int64_t msize[3], const double mgeo[15], const double *moving_grad, const float *points,
+                      int64_t npoints, int tkind, const double *tparams, int64_t nparams, const double *tfixed,
+                      int64_t nfixed, int64_t bins, int nthreads, int compute_derivative, double *value,
+                      double *derivative, uint64_t *nvalid, double *joint_pdf, double *state_out,
+                      const int64_t *vsize, const double *vgeo)
+{
   orc_inputs in;
   orc_transform t;
   orc_mattes_state st;
-  int rc = inputs_from_flat(&in, fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, nthreads);
+  int rc = inputs_from_flat(&in, fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, nthreads,
+                            vsize, vgeo);
   if (rc) return rc;
   rc = orc_transform_from_flat(&t, tkind, tparams, nparams, tfixed, nfixed);
   if (rc) return rc;

@@ -60,6 +60,8 @@ def lib():
                                    ctypes.c_int, ctypes.c_int, P, P, P]
         L.orc_mattes_flat.argtypes = [P, P, P, P, P, P, P, P, i64, ctypes.c_int, P, i64, P, i64,
                                       i64, ctypes.c_int, ctypes.c_int, P, P, P, P, P]
+        L.orc_msq_flat_v.argtypes = L.orc_msq_flat.argtypes + [P, P]
+        L.orc_mattes_flat_v.argtypes = L.orc_mattes_flat.argtypes + [P, P]
         L.orc_transform_point_flat.argtypes = [ctypes.c_int, P, i64, P, i64, P, i64, P]
         L.orc_interpolate_flat.argtypes = [P, P, P, P, i64, P, P]
         L.orc_central_difference_flat.argtypes = [P, P, P, P, i64, P]
@@ -122,14 +124,19 @@ def _pts(p):
     return None if p is None else np.ascontiguousarray(np.asarray(p, dtype=np.float32).reshape(-1, 3))
 
 
+def _vgeom(g):
+    return (None, None) if g is None else (g.size_array(), g.flat())
+
+
 def _threads(nthreads, pixel_double):
     t = int(nthreads or os.cpu_count()) & 0xFFFF
     return t | (0x10000 if pixel_double else 0)
 
 
 def mean_squares(fixed, fgeom, moving, mgeom, transform, moving_grad=None, points=None, nthreads=None,
-                 compute_derivative=True, pixel_double=False):
-    """Returns (status, value, derivative, nvalid)."""
+                 compute_derivative=True, pixel_double=False, virtual_geom=None):
+    """Returns (status, value, derivative, nvalid).  virtual_geom: the dense virtual
+    domain (default: the fixed image's geometry)."""
     L = lib()
     fixed, moving = _img(fixed), _img(moving)
     mg, pts = _grad(moving_grad), _pts(points)
@@ -139,15 +146,16 @@ def mean_squares(fixed, fgeom, moving, mgeom, transform, moving_grad=None, point
     deriv = np.zeros(tp.size, np.float64)
     nvalid = np.zeros(1, np.uint64)
     fs, fg, ms, mgeo = fgeom.size_array(), fgeom.flat(), mgeom.size_array(), mgeom.flat()
-    rc = L.orc_msq_flat(_p(fixed), _p(fs), _p(fg), _p(moving), _p(ms), _p(mgeo), _p(mg), _p(pts),
-                        0 if pts is None else pts.shape[0], transform.kind, _p(tp), tp.size, _p(tf), tf.size,
-                        _threads(nthreads, pixel_double), int(compute_derivative), _p(value), _p(deriv),
-                        _p(nvalid))
+    vs, vg = _vgeom(virtual_geom)
+    rc = L.orc_msq_flat_v(_p(fixed), _p(fs), _p(fg), _p(moving), _p(ms), _p(mgeo), _p(mg), _p(pts),
+                          0 if pts is None else pts.shape[0], transform.kind, _p(tp), tp.size, _p(tf), tf.size,
+                          _threads(nthreads, pixel_double), int(compute_derivative), _p(value), _p(deriv),
+                          _p(nvalid), _p(vs), _p(vg))
     return rc, float(value[0]), deriv, int(nvalid[0])
 
 
 def mattes(fixed, fgeom, moving, mgeom, transform, bins=50, moving_grad=None, points=None, nthreads=None,
-           compute_derivative=True, pixel_double=False):
+           compute_derivative=True, pixel_double=False, virtual_geom=None):
     """Returns (status, value, derivative, nvalid, joint_pdf[bins,bins], state[8])."""
     L = lib()
     fixed, moving = _img(fixed), _img(moving)
@@ -161,10 +169,11 @@ def mattes(fixed, fgeom, moving, mgeom, transform, bins=50, moving_grad=None, po
     pdf = np.zeros((b, b), np.float64)
     state = np.zeros(8, np.float64)
     fs, fg, ms, mgeo = fgeom.size_array(), fgeom.flat(), mgeom.size_array(), mgeom.flat()
-    rc = L.orc_mattes_flat(_p(fixed), _p(fs), _p(fg), _p(moving), _p(ms), _p(mgeo), _p(mg), _p(pts),
-                           0 if pts is None else pts.shape[0], transform.kind, _p(tp), tp.size, _p(tf), tf.size,
-                           b, _threads(nthreads, pixel_double), int(compute_derivative), _p(value), _p(deriv),
-                           _p(nvalid), _p(pdf), _p(state))
+    vs, vg = _vgeom(virtual_geom)
+    rc = L.orc_mattes_flat_v(_p(fixed), _p(fs), _p(fg), _p(moving), _p(ms), _p(mgeo), _p(mg), _p(pts),
+                             0 if pts is None else pts.shape[0], transform.kind, _p(tp), tp.size, _p(tf), tf.size,
+                             b, _threads(nthreads, pixel_double), int(compute_derivative), _p(value), _p(deriv),
+                             _p(nvalid), _p(pdf), _p(state), _p(vs), _p(vg))
     return rc, float(value[0]), deriv, int(nvalid[0]), pdf, state
 
 
