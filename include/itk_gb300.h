@@ -249,6 +249,78 @@ int gb_shrink_geometry(const int64_t size[3], const double spacing[3], const dou
                        const double direction[9], const int64_t factors[3], int64_t out_size[3],
                        double out_spacing[3], double out_origin[3]);
 
+/* ---- device optimizer --------------------------------------------------- */
+/* Stop conditions, numbered as StopConditionObjectToObjectOptimizerEnum
+ * (Numerics/Optimizersv4/include/itkObjectToObjectOptimizerBase.h:42-51). */
+enum {
+  GB_STOP_MAXIMUM_NUMBER_OF_ITERATIONS = 0,
+  GB_STOP_COSTFUNCTION_ERROR = 1,
+  GB_STOP_UPDATE_PARAMETERS_ERROR = 2,
+  GB_STOP_STEP_TOO_SMALL = 3,
+  GB_STOP_CONVERGENCE_CHECKER_PASSED = 4,
+  GB_STOP_GRADIENT_MAGNITUDE_TOLERANCE = 5,
+  GB_STOP_OTHER_ERROR = 6
+};
+
+/* RegularStepGradientDescentOptimizerv4 settings; the reference's defaults are
+ * learning rate 1, relaxation 0.5, minimum step 1e-4, gradient tolerance 1e-4,
+ * 100 iterations, return-best off. */
+typedef struct {
+  double learning_rate;
+  double relaxation_factor;
+  double minimum_step_length;
+  double gradient_magnitude_tolerance;
+  int64_t number_of_iterations;
+  int return_best_parameters_and_value;
+} gb_regular_step_settings;
+
+typedef struct {
+  int stop_condition;          /* GB_STOP_* */
+  int metric_status;           /* status of the evaluation that stopped it (GB_OK unless COSTFUNCTION_ERROR) */
+  int64_t iterations;          /* GetCurrentIteration() */
+  double value;                /* GetValue(): the current (or, with return-best, the best) metric value */
+  double current_step_length;  /* GetCurrentStepLength() */
+  double gradient_magnitude;   /* magnitude of the last scaled gradient */
+  double learning_rate_relaxation;
+} gb_optimizer_report;
+
+/* RegularStepGradientDescentOptimizerv4::StartOptimization on an initialized
+ * metric (Numerics/Optimizersv4/include/itkRegularStepGradientDescentOptimizerv4.hxx:39-171,
+ * the loop of itkGradientDescentOptimizerv4.hxx:72-169): every iteration is one
+ * GetValueAndDerivative at the current parameters and one AdvanceOneStep
+ * (gradient / scales, ||g|| and g . g_prev by compensated sums, relaxation,
+ * update of the moving transform's parameters by g * relaxation * rate / ||g||),
+ * all in device memory on the handle's stream; the host only enqueues batches
+ * of iterations and reads the stop flag between batches.  scales: nscales = the
+ * number of parameters (each > DBL_EPSILON; within 0.01 of 1 everywhere counts as
+ * identity, as ObjectToObjectOptimizerBase does), or nscales = 0 for identity.
+ * On return the handle's parameters are the optimizer's final position
+ * (gb_metric_get_parameters).  A metric error during the loop stops it with
+ * GB_STOP_COSTFUNCTION_ERROR and is returned as the metric's status. */
+int gb_metric_optimize_regular_step(gb_metric *m, const gb_regular_step_settings *settings, const double *scales,
+                                    int64_t nscales, gb_optimizer_report *report);
+/* Capture each optimizer iteration in a CUDA graph (default on). */
+int gb_metric_set_optimizer_graphs(gb_metric *m, int on);
+
+/* ---- metric sample points ----------------------------------------------- */
+/* ImageRegistrationMethodv4's sampling strategies
+ * (Registration/RegistrationMethodsv4/include/itkImageRegistrationMethodv4.h, MetricSamplingStrategyEnum). */
+enum { GB_SAMPLING_NONE = 0, GB_SAMPLING_REGULAR = 1, GB_SAMPLING_RANDOM = 2 };
+/* Number of points gb_sample_points makes for a virtual domain of `size`
+ * voxels: RANDOM (unsigned long)((float)voxels * percentage), REGULAR every
+ * ceil(1 / percentage)-th voxel in scan order, NONE every voxel. */
+int gb_sample_count(int strategy, const int64_t size[3], double percentage, int64_t *count);
+/* ImageRegistrationMethodv4::SetMetricSamplePoints for one image metric and no
+ * fixed mask (Registration/RegistrationMethodsv4/include/itkImageRegistrationMethodv4.hxx:869-1024),
+ * bit for bit: REGULAR or RANDOM voxels of the virtual domain (geometry given),
+ * each moved by N(0,1) * spacing / 3 per axis, as float points (x, y, z) in
+ * xyz[0 .. 3 * count).  seed is the method's current random seed at this
+ * level: the jitter generator takes seed, RANDOM's voxel iterator seed + 1;
+ * *next_seed (may be null) receives the seed the next level starts from. */
+int gb_sample_points(int strategy, const int64_t size[3], const double spacing[3], const double origin[3],
+                     const double direction[9], double percentage, int32_t seed, float *xyz, int64_t capacity,
+                     int64_t *count, int32_t *next_seed);
+
 /* ---- observability ----------------------------------------------------- */
 /* Per-kernel CUDA-event timing of evaluations (the reference's TimeProbe,
  * Core/Common/include/itkTimeProbe.h:44, at kernel granularity).  When on,

@@ -11,11 +11,14 @@ from .filters import (GradientRecursiveGaussianImageFilter, ShrinkImageFilter, S
 from .image import GradientImage, Image
 from .metrics import (ImageToImageMetricv4, MattesMutualInformationImageToImageMetricv4,
                       MeanSquaresImageToImageMetricv4, context)
+from .optimizers import RegularStepGradientDescentOptimizerv4
+from .registration import ImageRegistrationMethodv4, sample_count, sample_points
 from .transforms import AffineTransform, BSplineTransform, CompositeTransform
 
 __all__ = [
     "AffineTransform", "BSplineTransform", "CompositeTransform", "ExceptionObject", "GradientImage",
-    "GradientRecursiveGaussianImageFilter", "Image", "ImageToImageMetricv4",
-    "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4", "ShrinkImageFilter",
-    "SmoothingRecursiveGaussianImageFilter", "context", "lib", "library_path", "shrink_geometry",
+    "GradientRecursiveGaussianImageFilter", "Image", "ImageRegistrationMethodv4", "ImageToImageMetricv4",
+    "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
+    "RegularStepGradientDescentOptimizerv4", "ShrinkImageFilter", "SmoothingRecursiveGaussianImageFilter", "context",
+    "lib", "library_path", "sample_count", "sample_points", "shrink_geometry",
 ]

@@ -40,6 +40,34 @@ GB_GRADIENT_IMAGE = 0
 GB_GRADIENT_CENTRAL_DIFFERENCE = 1
 GB_GRADIENT_RECURSIVE_GAUSSIAN = 2
 
+# MetricSamplingStrategyEnum
+GB_SAMPLING_NONE = 0
+GB_SAMPLING_REGULAR = 1
+GB_SAMPLING_RANDOM = 2
+
+# StopConditionObjectToObjectOptimizerEnum
+GB_STOP_MAXIMUM_NUMBER_OF_ITERATIONS = 0
+GB_STOP_COSTFUNCTION_ERROR = 1
+GB_STOP_UPDATE_PARAMETERS_ERROR = 2
+GB_STOP_STEP_TOO_SMALL = 3
+GB_STOP_CONVERGENCE_CHECKER_PASSED = 4
+GB_STOP_GRADIENT_MAGNITUDE_TOLERANCE = 5
+GB_STOP_OTHER_ERROR = 6
+
+
+class RegularStepSettings(ctypes.Structure):
+    """gb_regular_step_settings."""
+    _fields_ = [("learning_rate", ctypes.c_double), ("relaxation_factor", ctypes.c_double),
+                ("minimum_step_length", ctypes.c_double), ("gradient_magnitude_tolerance", ctypes.c_double),
+                ("number_of_iterations", ctypes.c_int64), ("return_best_parameters_and_value", ctypes.c_int)]
+
+
+class OptimizerReport(ctypes.Structure):
+    """gb_optimizer_report."""
+    _fields_ = [("stop_condition", ctypes.c_int), ("metric_status", ctypes.c_int), ("iterations", ctypes.c_int64),
+                ("value", ctypes.c_double), ("current_step_length", ctypes.c_double),
+                ("gradient_magnitude", ctypes.c_double), ("learning_rate_relaxation", ctypes.c_double)]
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _I64 = ctypes.c_int64
@@ -88,6 +116,10 @@ SIGNATURES = {
     "gb_msq_affine_noalloc": [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _U64],
     "gb_metric_set_profiling": [_P, _I],
     "gb_metric_get_kernel_times": [_P, _P, _I, _P],
+    "gb_metric_optimize_regular_step": [_P, _P, _P, _I64, _P],
+    "gb_metric_set_optimizer_graphs": [_P, _I],
+    "gb_sample_count": [_I, _P, _D, _P],
+    "gb_sample_points": [_I, _P, _P, _P, _P, _D, ctypes.c_int32, _P, _I64, _P, _P],
 }
 _RESTYPES = {"gb_last_error": ctypes.c_char_p, "gb_version": ctypes.c_char_p}
 

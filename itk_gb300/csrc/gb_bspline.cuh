@@ -56,6 +56,7 @@ __device__ __forceinline__ float4 node_from_params(const double* __restrict__ p,
 // rather than one per node in every block of the sample pass.
 __global__ void k_prepare_bspline(EvalArgs a) {
   griddep_wait();
+  if (halted(a)) return;
   griddep_launch_dependents();
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n < a.nper) a.nodes[n] = node_from_params(a.params, a.nper, n);
@@ -133,6 +134,7 @@ __global__ void __launch_bounds__(kBlock) k_msq_bspline(EvalArgs a) {
   __shared__ float red[kBlock / 32][1];
   __shared__ double blk[1], fin[1];
   griddep_wait();
+  if (halted(a)) return;
   griddep_launch_dependents();
   load_consts(a.consts, K);
   const float4* nodes = stage_nodes<SMEM>(a, nodes_sh);
@@ -199,6 +201,7 @@ __global__ void __launch_bounds__(kBlock, SMEM ? 4 : 3) k_mattes_pass1_bspline(E
     cs[k] = 0ull;
   }
   griddep_wait();
+  if (halted(a)) return;
   griddep_launch_dependents();
   load_consts(a.consts, K);
   const float4* nodes = stage_nodes<SMEM>(a, nodes_sh);
@@ -256,6 +259,7 @@ __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
   __shared__ float4 AV[kChunkLen];
   __shared__ float qs[kChunkSlices][192];
   griddep_wait();  // several waves of blocks: dependents are released at each block's end
+  if (halted(a)) return;
   if (MATTES) mattes_value_groups(a);  // the value's group partials (the grid has at least one block per group)
   if ((int)blockIdx.x >= a.nchunks) {
     griddep_launch_dependents();
@@ -337,6 +341,7 @@ __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
   const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   griddep_wait();
+  if (halted(a)) return;
   griddep_launch_dependents();
   const unsigned long long N = __ldcg(a.acc_n);
   // MeanSquares: the status of the value pass; Mattes: from the pass-1 totals, and

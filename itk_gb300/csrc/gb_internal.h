@@ -68,7 +68,15 @@ int gradient_rg_device(cudaStream_t st, const float* in, const int64_t size[3], 
 void shrink_geometry(const int64_t size[3], const double spacing[3], const double origin[3], const double dir[9],
                      const int64_t factors[3], int64_t out_size[3], double out_spacing[3], double out_origin[3]);
 
+struct OptState;  // device optimizer state (gb_optimizer.cu)
+
 }  // namespace gb
+
+// Enqueues one metric evaluation on the handle's stream (gb_metric.cu); results
+// land in d_out = [value, nvalid, derivative...] and the handle's status word.
+namespace gb {
+int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_params);
+}
 
 struct gb_ctx {
   int device = 0;
@@ -136,6 +144,14 @@ struct gb_metric {
   int* h_status = nullptr;
   uint64_t last_nvalid = 0;
   int last_status = GB_OK;
+
+  // device optimizer (gb_metric_optimize_regular_step)
+  const int* eval_halt = nullptr;   // while set, evaluation kernels return at once once it reads nonzero
+  gb::DevBuf<unsigned char> d_opt;  // optimizer state
+  gb::DevBuf<double> d_opt_vec;     // previous gradient, scaled gradient, best parameters, 1 / scales (4 x P)
+  unsigned char* h_opt = nullptr;   // pinned copy of the state
+  int* h_halt = nullptr;            // pinned halt flags, one per batch slot
+  bool opt_graphs = true;           // capture each iteration in a CUDA graph
 
   // per-kernel event timing (gb_metric_set_profiling)
   bool profiling = false;

@@ -173,7 +173,13 @@ struct EvalArgs {
   const int* __restrict__ node_first;    // per node: first entry in node_entries (nper + 1 values)
   const int* __restrict__ node_entries;  // chunk * 192 + support position of each (node, chunk) pair
   float* chunk_part;                 // nchunks x 192 per-chunk Jacobian partial sums
+  // optimizer loop: nonzero once the optimizer has stopped; every evaluation
+  // kernel then returns at once (iterations enqueued ahead become no-ops)
+  const int* halt;
 };
+
+// The optimizer's stop flag (read once per block, after the launch dependency).
+__device__ __forceinline__ bool halted(const EvalArgs& a) { return a.halt != nullptr && __ldcg(a.halt) != 0; }
 
 #ifndef GB_KERNELS_HELPERS_ONLY
 // Device twin of the host constant computation (parameters already in HBM).
@@ -182,6 +188,7 @@ struct EvalArgs {
 // paths, and one SM's FP64 pipe would serve them one after another.
 __global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
   griddep_wait();
+  if (halted(a)) return;
   griddep_launch_dependents();
   const int e = blockIdx.x;
   if (threadIdx.x == 0 && e < kConstEntries)
@@ -338,6 +345,7 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
   __shared__ float red[kBlock / 32][13];
   __shared__ double blk[13], fin[13];
   griddep_wait();
+  if (halted(a)) return;
   griddep_launch_dependents();
   load_consts(a.consts, K);
   __syncthreads();
@@ -591,6 +599,7 @@ __global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_p
     cs[k] = 0ull;
   }
   griddep_wait();
+  if (halted(a)) return;
   griddep_launch_dependents();
   load_consts(a.consts, K);
   __syncthreads();
@@ -641,6 +650,7 @@ __global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_p
 // (k_mattes_pass2_affine, k_bspline_chunks) and summed at its end.
 __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a) {
   griddep_wait();
+  if (halted(a)) return;
   griddep_launch_dependents();
   const int lane = threadIdx.x;
   const double part = mattes_group_partial(a, blockIdx.x, lane);
@@ -704,6 +714,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
     failed = 0;
   }
   griddep_wait();
+  if (halted(a)) return;
   griddep_launch_dependents();
   if (threadIdx.x == 0)
     for (int t = 0; t < min(kStreamStages, ntiles); ++t) issue(t);

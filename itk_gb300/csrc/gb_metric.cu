@@ -204,6 +204,8 @@ extern "C" int gb_metric_destroy(gb_metric* m) {
   if (m->h_out) cudaFreeHost(m->h_out);
   if (m->h_status) cudaFreeHost(m->h_status);
   if (m->h_consts) cudaFreeHost(m->h_consts);
+  if (m->h_opt) cudaFreeHost(m->h_opt);
+  if (m->h_halt) cudaFreeHost(m->h_halt);
   for (int i = 0; i < gb_metric::kMaxEvents; ++i)
     if (m->events[i]) cudaEventDestroy(m->events[i]);
   if (m->stream) cudaStreamDestroy(m->stream);
@@ -744,6 +746,7 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.out = d_out;
   a.status = m->d_status.p;
   a.with_derivative = deriv ? 1 : 0;
+  a.halt = m->eval_halt;
   if (is_bspline(m)) {
     a.sup = m->d_sup.p;
     a.nodes = m->d_nodes.p;
@@ -843,7 +846,7 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
 // device_params: the parameters are in device memory (d_params), so the affine
 // constants or the B-spline nodes are formed on the device; otherwise the host
 // has uploaded them.
-static int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_params) {
+int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_params) {
   cudaStream_t st = m->stream;
   EvalArgs a;
   fill_eval_args(m, a, d_params, d_out, deriv);

@@ -205,6 +205,16 @@ int orc_shrink_geometry(const int64_t size[3], const double spacing[3], const do
                         const double direction[9], const int64_t factors[3], int64_t out_size[3],
                         double out_spacing[3], double out_origin[3]);
 
+/* ---- metric sample points (itk_oracle_sampling.c) ---------------------- */
+/* MT19937 32-bit outputs after `skip` draws from a fresh seed */
+int orc_mt_sequence(uint32_t seed, int64_t skip, uint32_t *out, int64_t n);
+/* GetNormalVariate(0, 1) sequence from a fresh seed */
+int orc_mt_normals(uint32_t seed, double *out, int64_t n);
+/* SetMetricSamplePoints: strategy 1 REGULAR, 2 RANDOM; geometry = spacing[3],
+ * origin[3], direction[9]; float points (x, y, z) */
+int orc_sample_points(int strategy, const int64_t size[3], const double *geometry, double percentage, int32_t seed,
+                      float *xyz, int64_t capacity, int64_t *count);
+
 #ifdef __cplusplus
 }
 #endif

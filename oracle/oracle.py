@@ -44,7 +44,8 @@ def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (portable C, no ISA flags)."""
     if force or not os.path.exists(_LIB_PATH) or (
         os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(os.path.join(_HERE, f))
-                                          for f in ("itk_oracle.c", "itk_oracle_filters.c", "itk_oracle.h"))):
+                                          for f in ("itk_oracle.c", "itk_oracle_filters.c", "itk_oracle_sampling.c",
+                                                    "itk_oracle.h"))):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -76,6 +77,10 @@ def lib():
         L.orc_smooth_recursive_gaussian.argtypes = [P, P, P, P, P]
         L.orc_gradient_recursive_gaussian.argtypes = [P, P, P, P, P, d, ci, ci]
         L.orc_shrink_geometry.argtypes = [P] * 8
+        u32 = ctypes.c_uint32
+        L.orc_mt_sequence.argtypes = [u32, i64, P, i64]
+        L.orc_mt_normals.argtypes = [u32, P, i64]
+        L.orc_sample_points.argtypes = [ci, P, P, d, ctypes.c_int32, P, i64, P]
         _lib = L
     return _lib
 
@@ -297,3 +302,34 @@ def bspline3(u):
 
 def bspline3_derivative(u):
     return lib().orc_bspline3_derivative(float(u))
+
+
+def mt_sequence(seed, n, skip=0):
+    """MT19937 32-bit outputs (GetIntegerVariate) after `skip` draws from SetSeed(seed)."""
+    out = np.zeros(int(n), np.uint32)
+    lib().orc_mt_sequence(int(seed) & 0xFFFFFFFF, int(skip), _p(out), out.size)
+    return out
+
+
+def mt_normals(seed, n):
+    """GetNormalVariate() sequence from SetSeed(seed)."""
+    out = np.zeros(int(n), np.float64)
+    lib().orc_mt_normals(int(seed) & 0xFFFFFFFF, _p(out), out.size)
+    return out
+
+
+def sample_points(strategy, size_xyz, spacing, origin, direction, percentage, seed):
+    """ImageRegistrationMethodv4::SetMetricSamplePoints (strategy 1 REGULAR, 2 RANDOM)
+    over a virtual domain; float32 points, shape (n, 3)."""
+    size = np.ascontiguousarray(np.asarray(size_xyz, np.int64))
+    V = int(np.prod(size))
+    cap = V
+    geo = np.ascontiguousarray(np.concatenate([np.asarray(spacing, np.float64), np.asarray(origin, np.float64),
+                                               np.asarray(direction, np.float64).reshape(9)]))
+    out = np.zeros((max(cap, 1), 3), np.float32)
+    n = np.zeros(1, np.int64)
+    rc = lib().orc_sample_points(int(strategy), _p(size), _p(geo), float(percentage), int(seed), _p(out), cap,
+                                 _p(n))
+    if rc != 0:
+        raise ValueError(f"orc_sample_points status {rc}")
+    return out[:int(n[0])].copy()
