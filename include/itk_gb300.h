@@ -302,6 +302,37 @@ int gb_metric_optimize_regular_step(gb_metric *m, const gb_regular_step_settings
 /* Capture each optimizer iteration in a CUDA graph (default on). */
 int gb_metric_set_optimizer_graphs(gb_metric *m, int on);
 
+/* ---- batched registrations ---------------------------------------------- */
+/* No counterpart in the reference (which runs one registration per optimizer):
+ * many affine registrations, each an initialized metric handle with its own
+ * RegularStepGradientDescentOptimizerv4 settings, advance together -- one
+ * launch per phase of an iteration for all of them (accumulator clear,
+ * transform constants, MeanSquares pass, Mattes pass 1, Mattes pass 2,
+ * AdvanceOneStep), captured as a CUDA graph.  A registration's results do not
+ * depend on which others share the batch.  While a metric is in a batch, make
+ * no other call on it. */
+typedef struct gb_batch gb_batch;
+int gb_batch_create(gb_ctx *ctx, gb_batch **out);
+int gb_batch_destroy(gb_batch *b);
+/* StartOptimization of one registration in the batch; *slot identifies it. */
+int gb_batch_add(gb_batch *b, gb_metric *m, const gb_regular_step_settings *settings, const double *scales,
+                 int64_t nscales, int64_t *slot);
+/* Advance every running registration by up to max_iterations iterations
+ * (<= 0: until all have stopped); *running (may be null) = those still running. */
+int gb_batch_run(gb_batch *b, int64_t max_iterations, int64_t *running);
+/* *finished = 1 once registration `slot` has stopped; then *report is filled,
+ * the metric handle holds the final parameters, and the return value is the
+ * registration's status (as gb_metric_optimize_regular_step returns it). */
+int gb_batch_result(gb_batch *b, int64_t slot, int *finished, gb_optimizer_report *report);
+/* Samples per block of the MeanSquares pass, Mattes pass 1 and Mattes pass 2
+ * (default 8192 each); gb_batch_autotune picks them by timing the batch's
+ * evaluations (no optimizer state changes) and leaves the fastest set. */
+int gb_batch_set_samples_per_block(gb_batch *b, const int64_t spb[3]);
+int gb_batch_get_samples_per_block(gb_batch *b, int64_t spb[3]);
+int gb_batch_autotune(gb_batch *b, int iterations, int64_t spb[3]);
+/* Capture the iteration in a CUDA graph (default on). */
+int gb_batch_set_graphs(gb_batch *b, int on);
+
 /* ---- metric sample points ----------------------------------------------- */
 /* ImageRegistrationMethodv4's sampling strategies
  * (Registration/RegistrationMethodsv4/include/itkImageRegistrationMethodv4.h, MetricSamplingStrategyEnum). */

@@ -6,6 +6,7 @@ B-spline and [affine, B-spline] composite transforms, computed by hand-written
 sm_103a CUDA kernels behind the C ABI in include/itk_gb300.h.
 """
 from ._capi import ExceptionObject, lib, library_path
+from .batch import RegistrationBatch
 from .filters import (GradientRecursiveGaussianImageFilter, ShrinkImageFilter, SmoothingRecursiveGaussianImageFilter,
                       shrink_geometry)
 from .image import GradientImage, Image
@@ -19,6 +20,6 @@ __all__ = [
     "AffineTransform", "BSplineTransform", "CompositeTransform", "ExceptionObject", "GradientImage",
     "GradientRecursiveGaussianImageFilter", "Image", "ImageRegistrationMethodv4", "ImageToImageMetricv4",
     "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
-    "RegularStepGradientDescentOptimizerv4", "ShrinkImageFilter", "SmoothingRecursiveGaussianImageFilter", "context",
+    "RegistrationBatch", "RegularStepGradientDescentOptimizerv4", "ShrinkImageFilter", "SmoothingRecursiveGaussianImageFilter", "context",
     "lib", "library_path", "sample_count", "sample_points", "shrink_geometry",
 ]

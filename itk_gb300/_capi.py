@@ -118,6 +118,15 @@ SIGNATURES = {
     "gb_metric_get_kernel_times": [_P, _P, _I, _P],
     "gb_metric_optimize_regular_step": [_P, _P, _P, _I64, _P],
     "gb_metric_set_optimizer_graphs": [_P, _I],
+    "gb_batch_create": [_P, _P],
+    "gb_batch_destroy": [_P],
+    "gb_batch_add": [_P, _P, _P, _P, _I64, _P],
+    "gb_batch_run": [_P, _I64, _P],
+    "gb_batch_result": [_P, _I64, _P, _P],
+    "gb_batch_set_samples_per_block": [_P, _P],
+    "gb_batch_get_samples_per_block": [_P, _P],
+    "gb_batch_autotune": [_P, _I, _P],
+    "gb_batch_set_graphs": [_P, _I],
     "gb_sample_count": [_I, _P, _D, _P],
     "gb_sample_points": [_I, _P, _P, _P, _P, _D, ctypes.c_int32, _P, _I64, _P, _P],
 }

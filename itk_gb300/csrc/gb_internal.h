@@ -76,6 +76,8 @@ struct OptState;  // device optimizer state (gb_optimizer.cu)
 // land in d_out = [value, nvalid, derivative...] and the handle's status word.
 namespace gb {
 int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_params);
+struct EvalArgs;
+void batch_eval_args(gb_metric* m, EvalArgs& a);
 }
 
 struct gb_ctx {

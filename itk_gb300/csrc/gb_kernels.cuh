@@ -253,6 +253,14 @@ __device__ __forceinline__ bool eval_moving(const EvalArgs& a, const DFPos& p, b
 
 constexpr int kGroup = 16;
 
+// The blocks one evaluation of one registration runs on: block b of n.  A plain
+// launch uses the hardware grid; a batched launch (several registrations in one
+// grid) gives each registration its own range of blocks.
+struct VGrid {
+  int b, n;
+};
+__device__ __forceinline__ VGrid hw_grid() { return VGrid{(int)blockIdx.x, (int)gridDim.x}; }
+
 template <int NV>
 __device__ __forceinline__ void block_sums(KahanF (&acc)[NV], float (*red)[NV], double* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -288,11 +296,12 @@ __device__ __forceinline__ void strided_sums(const double* src, int cnt, double*
 
 // Returns true in exactly one block, which then holds the grid-wide sums in `fin`.
 template <int NV>
-__device__ __forceinline__ bool grid_sums(const double* blk, double* part, double* grp, unsigned* tick, double* fin) {
+__device__ __forceinline__ bool grid_sums(const double* blk, double* part, double* grp, unsigned* tick, double* fin,
+                                          VGrid vg = hw_grid()) {
   __shared__ unsigned t;
-  const int b = blockIdx.x, g = b / kGroup;
-  const int ng = (gridDim.x + kGroup - 1) / kGroup;
-  const int gsize = min(kGroup, (int)gridDim.x - g * kGroup);
+  const int b = vg.b, g = b / kGroup;
+  const int ng = (vg.n + kGroup - 1) / kGroup;
+  const int gsize = min(kGroup, vg.n - g * kGroup);
   for (int k = threadIdx.x; k < NV; k += blockDim.x) part[b * NV + k] = blk[k];
   __threadfence();
   __syncthreads();
@@ -326,11 +335,11 @@ __device__ __forceinline__ void block_count(unsigned nv, unsigned long long* gn)
 }
 
 // true in exactly one block: the last to finish (threadFenceReduction pattern)
-__device__ __forceinline__ bool last_block(unsigned* ticket) {
+__device__ __forceinline__ bool last_block(unsigned* ticket, VGrid vg = hw_grid()) {
   __shared__ bool is_last;
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) is_last = atomicAdd(ticket, 1u) == (unsigned)vg.n - 1u;
   __syncthreads();
   if (is_last) __threadfence();
   return is_last;
@@ -340,7 +349,7 @@ __device__ __forceinline__ bool last_block(unsigned* ticket) {
 // MeanSquares, affine: value = sum (f - m)^2 / N, d[p] = sum 2 (f - m) (J^T g)[p] / N
 
 template <int GRAD>
-__global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
+__device__ __forceinline__ void msq_affine_body(const EvalArgs& a, VGrid vg) {
   __shared__ EvalConsts K;
   __shared__ float red[kBlock / 32][13];
   __shared__ double blk[13], fin[13];
@@ -353,8 +362,8 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
 #pragma unroll
   for (int k = 0; k < 13; ++k) acc[k].zero();
   unsigned nv = 0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)vg.n * blockDim.x;
+  int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x;
   float4 s_next = i < a.n ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
   for (; i < a.n; i += stride) {
     const float4 s = s_next;
@@ -379,7 +388,7 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
   }
   block_count(nv, a.acc_n);
   block_sums<13>(acc, red, blk);
-  if (!grid_sums<13>(blk, a.part, a.grp, a.tickets + kTicketMain, fin)) return;
+  if (!grid_sums<13>(blk, a.part, a.grp, a.tickets + kTicketMain, fin, vg)) return;
   if (threadIdx.x == 0) {
     // AfterThreadedExecution + VerifyNumberOfValidPoints (ThreaderBase.hxx:116-172)
     const unsigned long long N = __ldcg(a.acc_n);
@@ -396,6 +405,11 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
       *a.status = GB_OK;
     }
   }
+}
+
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
+  msq_affine_body<GRAD>(a, hw_grid());
 }
 
 // ---------------------------------------------------------------------------
@@ -446,7 +460,7 @@ __device__ __forceinline__ float u64_to_float(unsigned long long v) {
 // End of Mattes pass 1 (any transform): flush the block histogram, marginals and
 // count; the last block computes the marginal logs and the derivative's table.
 __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigned nv, unsigned long long* hist,
-                                                      unsigned long long* cs, unsigned* fm) {
+                                                      unsigned long long* cs, unsigned* fm, VGrid vg = hw_grid()) {
   const int B = a.bins;
   __syncthreads();
   // flush the nonzero bins; the block's column sums ride along as shared atomics
@@ -464,7 +478,7 @@ __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigne
     if (cs[k]) atomicAdd(&a.colsum[k], cs[k]);
   }
   block_count(nv, a.acc_n);
-  if (!last_block(a.tickets + kTicketPass1)) return;
+  if (!last_block(a.tickets + kTicketPass1, vg)) return;
   // Last block: the fixed-point total T of the joint histogram (the value's
   // normalization, JointPDFSum) and the derivative's table.  It is on the
   // critical path, so it does no FP64 transcendental work.
@@ -575,18 +589,18 @@ __device__ __forceinline__ double mattes_value_sum(const double* part, int ngrou
 }
 
 // Group partials computed by the last warp of blocks b, b + gridDim.x, ... (all blocks participate).
-__device__ __forceinline__ void mattes_value_groups(const EvalArgs& a) {
+__device__ __forceinline__ void mattes_value_groups(const EvalArgs& a, VGrid vg = hw_grid()) {
   if ((int)(threadIdx.x >> 5) != (int)(blockDim.x >> 5) - 1) return;
   const int lane = threadIdx.x & 31;
   const int ng = mattes_groups(a.bins);
-  for (int g = blockIdx.x; g < ng; g += gridDim.x) {
+  for (int g = vg.b; g < ng; g += vg.n) {
     const double s = mattes_group_partial(a, g, lane);
     if (lane == 0) a.part[g] = s;
   }
 }
 
 template <int GRAD>
-__global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_pass1_affine(EvalArgs a) {
+__device__ __forceinline__ void mattes_pass1_affine_body(const EvalArgs& a, VGrid vg) {
   extern __shared__ unsigned long long smem_u64[];
   const int B = a.bins;
   unsigned long long* hist = smem_u64;
@@ -605,8 +619,8 @@ __global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_p
   __syncthreads();
   unsigned nv = 0;
   const int lane = threadIdx.x & 31;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  const int64_t stride = (int64_t)vg.n * blockDim.x;
+  int64_t base = (int64_t)vg.b * blockDim.x + (threadIdx.x & ~31);
   float4 s_next = base + lane < a.n ? __ldcs(a.samples + base + lane) : make_float4(0.f, 0.f, 0.f, 0.f);
   for (; base < a.n; base += stride) {
     const int64_t i = base + lane;
@@ -640,7 +654,12 @@ __global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_p
     hist_add_aggregated(ok, fidx * B + pdfm, fidx, q, hist, fm);
     nv += ok ? 1u : 0u;
   }
-  mattes_pass1_epilogue(a, nv, hist, cs, fm);
+  mattes_pass1_epilogue(a, nv, hist, cs, fm, vg);
+}
+
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_pass1_affine(EvalArgs a) {
+  mattes_pass1_affine_body<GRAD>(a, hw_grid());
 }
 
 #ifndef GB_KERNELS_HELPERS_ONLY
@@ -667,7 +686,6 @@ __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a
 
 #endif  // GB_KERNELS_HELPERS_ONLY
 
-#ifndef GB_KERNELS_HELPERS_ONLY
 // Streamed record tiles: each block owns a contiguous, tile-aligned range of
 // samples; thread 0 keeps kStreamStages tiles of (cache, sample) records in
 // flight with bulk asynchronous copies, completed on one mbarrier per stage.
@@ -677,15 +695,15 @@ constexpr int kStreamTile = kBlock * kStreamPer;  // records per stage and strea
 constexpr size_t kStreamBytes = (size_t)2 * kStreamStages * kStreamTile * sizeof(float4);
 
 // Whole tiles spread evenly: block b gets tiles [b T / G, (b + 1) T / G).
-__device__ __forceinline__ void block_range(int64_t n, int64_t& b0, int64_t& b1) {
+__device__ __forceinline__ void block_range(int64_t n, int64_t& b0, int64_t& b1, VGrid vg) {
   const int64_t tiles = (n + kStreamTile - 1) / kStreamTile;
-  b0 = min(n, (int64_t)blockIdx.x * tiles / gridDim.x * kStreamTile);
-  b1 = min(n, (int64_t)(blockIdx.x + 1) * tiles / gridDim.x * kStreamTile);
+  b0 = min(n, (int64_t)vg.b * tiles / vg.n * kStreamTile);
+  b1 = min(n, (int64_t)(vg.b + 1) * tiles / vg.n * kStreamTile);
 }
 
 // Mattes pass 2, affine: derivative from the cached Parzen terms and gradients.
 // Dynamic shared memory: kStreamBytes of record stages, then the bins^2 log(p/pm) table.
-__global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
+__device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGrid vg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float4* cbuf = reinterpret_cast<float4*>(smem_raw);  // [stage][tile] cache records
   float4* sbuf = cbuf + kStreamStages * kStreamTile;    // [stage][tile] sample records
@@ -697,7 +715,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
   __shared__ double blk[12], fin[12];
   const int B = a.bins;
   int64_t b0, b1;
-  block_range(a.n, b0, b1);
+  block_range(a.n, b0, b1, vg);
   const int ntiles = (int)((b1 - b0 + kStreamTile - 1) / kStreamTile);
   // tile t -> stage t % kStreamStages; the stage's phase parity is (t / kStreamStages) & 1
   auto issue = [&](int t) {
@@ -720,7 +738,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
     for (int t = 0; t < min(kStreamStages, ntiles); ++t) issue(t);
   for (int k = threadIdx.x; k < B * B; k += blockDim.x) pr[k] = __ldcg(&a.pratio[k]);
   load_consts(a.consts, K);
-  mattes_value_groups(a);  // the value's FP64 group partials, last warp (thread 0 feeds the copies)
+  mattes_value_groups(a, vg);  // the value's FP64 group partials, last warp (thread 0 feeds the copies)
   __syncthreads();
   // plain FP32 per thread (a thread adds a few dozen samples; the warp tree and the
   // FP64 cross-block sums follow)
@@ -776,7 +794,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
     kacc[k].c = 0.f;
   }
   block_sums<12>(kacc, red, blk);
-  if (!grid_sums<12>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin)) return;
+  if (!grid_sums<12>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin, vg)) return;
   // last block: the value from the group partials (all blocks wrote theirs before their tickets)
   if (threadIdx.x < 32) {
     const double s = mattes_value_sum(a.part, mattes_groups(B), threadIdx.x);
@@ -798,6 +816,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) {
   }
 }
 
+#ifndef GB_KERNELS_HELPERS_ONLY
+__global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) { mattes_pass2_affine_body(a, hw_grid()); }
 #endif  // GB_KERNELS_HELPERS_ONLY
 
 }  // namespace gb

@@ -763,6 +763,10 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   }
 }
 
+// Evaluation arguments of the device-resident form (parameters in d_params,
+// results in d_out, with the derivative), for the batched engine.
+void gb::batch_eval_args(gb_metric* m, EvalArgs& a) { fill_eval_args(m, a, m->d_params.p, m->d_out.p, true); }
+
 // One kernel of the evaluation chain on the handle's stream, launched with
 // programmatic stream serialization: its blocks may be scheduled while the
 // previous kernel drains, and wait in griddep_wait() for its results.

@@ -37,114 +37,11 @@
 
 #include "gb_device.cuh"
 #include "gb_internal.h"
+#include "gb_step.cuh"
 
 namespace gb {
 
-constexpr int kStepBlock = 256;
-constexpr int kStepMaxBlocks = 64;  // up to 16384 parameters
-constexpr int kMaxBatch = 16;       // iterations enqueued between reads of the halt word
-
-enum { kActNone = 0, kActStep = 1, kActRestoreBest = 2 };
-enum { kRunning = -1 };
-
-struct OptState {
-  double relaxation;   // m_CurrentLearningRateRelaxation
-  double value;        // m_CurrentMetricValue
-  double best_value;   // m_CurrentBestValue
-  double grad_mag;     // ||g|| of the last step
-  double step_length;  // relaxation * learning rate of the last step
-  double inv_mag;      // 1 / ||g||, the update factor
-  long long iteration; // m_CurrentIteration
-  int stop;            // GB_STOP_*, kRunning while the loop runs
-  int halt;            // nonzero once stopped
-  int status;          // metric status of the last evaluation
-  int action;          // what k_step_apply does this iteration
-  int save_best;       // k_step_apply copies the new position to the best parameters
-  unsigned ticket;
-  double part[kStepMaxBlocks][4];  // per block: (hi, lo) of ||g||^2 and of g . g_prev
-};
-
-struct StepArgs {
-  const double* out;   // metric output [value, nvalid, derivative...]
-  const int* status;   // metric status word
-  double* params;
-  double* prev;        // previous modified gradient (scaled, times relaxation * rate)
-  double* grad;        // this iteration's scaled gradient
-  double* best;        // best parameters (return-best)
-  const double* inv_scales;
-  OptState* st;
-  long long P;
-  double learning_rate, relaxation_factor, min_step, grad_tol;
-  int return_best;
-  int msq;  // MeanSquares: no valid points is a warning (value max, derivative 0), not an error
-};
-
-// Compensated pair: the sum is hi + lo, |lo| <= ulp(hi) / 2.
-struct DD {
-  double hi, lo;
-};
-
-__device__ __forceinline__ DD dd_add(DD a, DD b) {
-  const double s = __dadd_rn(a.hi, b.hi);
-  const double bb = __dsub_rn(s, a.hi);
-  const double e = __dadd_rn(__dsub_rn(a.hi, __dsub_rn(s, bb)), __dsub_rn(b.hi, bb));  // two-sum error
-  const double t = __dadd_rn(__dadd_rn(a.lo, b.lo), e);
-  const double hi = __dadd_rn(s, t);
-  return {hi, __dsub_rn(t, __dsub_rn(hi, s))};
-}
-
-__device__ __forceinline__ DD dd_shfl_down(DD v, int off) {
-  return {__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
-}
-
-// Sum over the block in a fixed order (lane tree, then warp tree); the result is in thread 0.
-__device__ __forceinline__ void block_dd2(DD& x, DD& y) {
-  __shared__ DD sx[kStepBlock / 32], sy[kStepBlock / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const DD ox = dd_shfl_down(x, off), oy = dd_shfl_down(y, off);
-    if (lane < off) {
-      x = dd_add(x, ox);
-      y = dd_add(y, oy);
-    }
-  }
-  if (lane == 0) {
-    sx[w] = x;
-    sy[w] = y;
-  }
-  __syncthreads();
-  if (w == 0) {
-    constexpr int W = kStepBlock / 32;
-    x = lane < W ? sx[lane] : DD{0.0, 0.0};
-    y = lane < W ? sy[lane] : DD{0.0, 0.0};
-#pragma unroll
-    for (int off = W / 2; off > 0; off >>= 1) {
-      const DD ox = dd_shfl_down(x, off), oy = dd_shfl_down(y, off);
-      if (lane < off) {
-        x = dd_add(x, ox);
-        y = dd_add(y, oy);
-      }
-    }
-  }
-}
-
-__device__ __forceinline__ bool metric_error(const StepArgs& s, int status) {
-  return status != GB_OK && !(s.msq && status == GB_ERR_NO_VALID_POINTS);
-}
-
-// StopOptimization (itkGradientDescentOptimizerv4.hxx:59-68): with return-best,
-// the value becomes the best value and k_step_apply restores the best parameters.
-__device__ __forceinline__ void stop_here(const StepArgs& s, OptState* S, int cond) {
-  S->stop = cond;
-  S->halt = 1;
-  if (s.return_best) {
-    S->value = S->best_value;
-    S->action = kActRestoreBest;
-  } else {
-    S->action = kActNone;
-  }
-}
+constexpr int kMaxBatch = 16;  // iterations enqueued between reads of the halt word
 
 __global__ void __launch_bounds__(kStepBlock) k_step_reduce(StepArgs s) {
   griddep_wait();
@@ -158,15 +55,7 @@ __global__ void __launch_bounds__(kStepBlock) k_step_reduce(StepArgs s) {
   const bool err = metric_error(s, status);
   const long long j = (long long)blockIdx.x * kStepBlock + threadIdx.x;
   DD q = {0.0, 0.0}, r = {0.0, 0.0};
-  if (j < s.P && !err) {
-    // ModifyGradientByScalesOverSubRange: g *= 1/scale, g_prev *= 1/scale
-    const double is = __ldg(s.inv_scales + j);
-    const double g = __dmul_rn(__ldcg(s.out + 2 + j), is);
-    const double gp = __dmul_rn(__ldcg(s.prev + j), is);
-    s.grad[j] = g;
-    q.hi = __dmul_rn(g, g);
-    r.hi = __dmul_rn(g, gp);
-  }
+  if (j < s.P && !err) step_terms(s, j, q.hi, r.hi);
   block_dd2(q, r);
   __shared__ bool last;
   if (threadIdx.x == 0) {
@@ -196,39 +85,7 @@ __global__ void __launch_bounds__(kStepBlock) k_step_reduce(StepArgs s) {
   }
   if (lane != 0) return;
   S->ticket = 0u;
-  S->status = status;
-  S->save_best = 0;
-  const double value = __ldcg(s.out);
-  S->value = value;
-  if (err) {  // the metric threw: COSTFUNCTION_ERROR, no iteration counted
-    stop_here(s, S, GB_STOP_COSTFUNCTION_ERROR);
-    return;
-  }
-  const double mag = sqrt(__dadd_rn(x.hi, x.lo));
-  S->grad_mag = mag;
-  if (mag < s.grad_tol) {
-    stop_here(s, S, GB_STOP_GRADIENT_MAGNITUDE_TOLERANCE);
-    S->iteration += 1;
-    return;
-  }
-  const double sp = __dadd_rn(y.hi, y.lo);
-  double relax = S->relaxation;
-  if (sp < 0.0) relax = __dmul_rn(relax, s.relaxation_factor);
-  S->relaxation = relax;
-  const double step = __dmul_rn(relax, s.learning_rate);
-  S->step_length = step;
-  if (step < s.min_step) {
-    stop_here(s, S, GB_STOP_STEP_TOO_SMALL);
-    S->iteration += 1;
-    return;
-  }
-  S->inv_mag = 1.0 / mag;
-  S->action = kActStep;
-  if (s.return_best && value < S->best_value) {
-    S->best_value = value;
-    S->save_best = 1;
-  }
-  S->iteration += 1;
+  step_decide(s, S, status, x, y);
 }
 
 __global__ void __launch_bounds__(kStepBlock) k_step_apply(StepArgs s) {
@@ -237,17 +94,7 @@ __global__ void __launch_bounds__(kStepBlock) k_step_apply(StepArgs s) {
   const OptState* S = s.st;
   const int act = __ldcg(&S->action);
   const long long j = (long long)blockIdx.x * kStepBlock + threadIdx.x;
-  if (j >= s.P || act == kActNone) return;
-  if (act == kActRestoreBest) {
-    s.params[j] = __ldcg(s.best + j);
-    return;
-  }
-  // ModifyGradientByLearningRateOverSubRange, then UpdateTransformParameters(g, 1/||g||)
-  const double glr = __dmul_rn(__dmul_rn(__ldcg(s.grad + j), __ldcg(&S->relaxation)), s.learning_rate);
-  s.prev[j] = glr;
-  const double p = __dadd_rn(s.params[j], __dmul_rn(glr, __ldcg(&S->inv_mag)));
-  s.params[j] = p;
-  if (__ldcg(&S->save_best)) s.best[j] = p;
+  if (j < s.P) step_apply(s, S, act, j);
 }
 
 // The loop ran out of iterations without another stop: MAXIMUM_NUMBER_OF_ITERATIONS.
@@ -316,18 +163,11 @@ struct LoopGuard {
   }
 };
 
-}  // namespace gb
-
-using namespace gb;
-
-extern "C" int gb_metric_set_optimizer_graphs(gb_metric* m, int on) {
-  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
-  m->opt_graphs = on != 0;
-  return GB_OK;
-}
-
-extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_step_settings* cfg,
-                                               const double* scales, int64_t nscales, gb_optimizer_report* report) {
+// StartOptimization for one registration: validates the settings and scales,
+// allocates the handle's optimizer buffers and enqueues their initial state on
+// the handle's stream (synchronized before returning); fills the step arguments.
+int opt_setup(gb_metric* m, const gb_regular_step_settings* cfg, const double* scales, int64_t nscales,
+              StepArgs& a) {
   if (!m || !cfg) return fail(GB_ERR_BAD_ARG, "null argument");
   if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
   const int64_t P = (int64_t)m->tparams.size();
@@ -372,7 +212,7 @@ extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_st
   double* d_best = d_grad + P;
   double* d_inv = d_best + P;
 
-  // StartOptimization: relaxation 1, iteration 0, zero gradients, best = start
+  // relaxation 1, iteration 0, zero gradients, best = start
   OptState* h = reinterpret_cast<OptState*>(m->h_opt);
   memset(h, 0, sizeof(OptState));
   h->relaxation = 1.0;
@@ -388,7 +228,6 @@ extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_st
   GB_OPT_CUDA(cudaMemcpyAsync(d_inv, inv_s.data(), sizeof(double) * P, cudaMemcpyHostToDevice, st));
   GB_OPT_CUDA(cudaStreamSynchronize(st));  // inv_s is pageable host memory
 
-  StepArgs a;
   memset(&a, 0, sizeof(a));
   a.out = m->d_out.p;
   a.status = m->d_status.p;
@@ -399,13 +238,69 @@ extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_st
   a.inv_scales = d_inv;
   a.st = S;
   a.P = P;
+  a.max_iterations = cfg->number_of_iterations;
   a.learning_rate = cfg->learning_rate;
   a.relaxation_factor = cfg->relaxation_factor;
   a.min_step = cfg->minimum_step_length;
   a.grad_tol = cfg->gradient_magnitude_tolerance;
   a.return_best = cfg->return_best_parameters_and_value ? 1 : 0;
   a.msq = m->kind == GB_METRIC_MEAN_SQUARES ? 1 : 0;
-  const unsigned blocks = (unsigned)((P + kStepBlock - 1) / kStepBlock);
+  return GB_OK;
+}
+
+// Enqueues the copies of the final state and parameters into the handle's pinned buffers.
+int opt_fetch(gb_metric* m, const StepArgs& a, cudaStream_t st) {
+  GB_OPT_CUDA(cudaMemcpyAsync(m->h_opt, a.st, sizeof(OptState), cudaMemcpyDeviceToHost, st));
+  GB_OPT_CUDA(cudaMemcpyAsync(m->h_params, a.params, sizeof(double) * a.P, cudaMemcpyDeviceToHost, st));
+  GB_OPT_CUDA(cudaMemcpyAsync(m->h_out, a.out, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
+  return GB_OK;
+}
+
+// After opt_fetch has completed: the handle's parameters, the report and the status.
+int opt_collect(gb_metric* m, const StepArgs& a, gb_optimizer_report* report) {
+  const OptState* h = reinterpret_cast<const OptState*>(m->h_opt);
+  std::copy(m->h_params, m->h_params + a.P, m->tparams.begin());
+  if (h->iteration > 0 || h->stop == GB_STOP_COSTFUNCTION_ERROR) m->last_nvalid = (uint64_t)m->h_out[1];
+  if (report) {
+    report->stop_condition = h->stop;
+    report->metric_status = h->status;
+    report->iterations = h->iteration;
+    report->value = h->value;
+    report->current_step_length = h->step_length;
+    report->gradient_magnitude = h->grad_mag;
+    report->learning_rate_relaxation = h->relaxation;
+  }
+  if (h->stop == GB_STOP_COSTFUNCTION_ERROR) {
+    m->last_status = h->status;
+    if (h->status == GB_ERR_NO_VALID_POINTS)
+      return fail(h->status,
+                  "All samples map outside moving image buffer. The images do not sufficiently overlap. They need to "
+                  "be initialized to have more overlap before this metric will work. For instance, you can align the "
+                  "image centers by translation.");
+    if (h->status == GB_ERR_JOINT_PDF_SUM_ZERO) return fail(h->status, "Joint PDF summed to zero");
+    return fail(h->status, "metric evaluation failed during optimization");
+  }
+  return GB_OK;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" int gb_metric_set_optimizer_graphs(gb_metric* m, int on) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  m->opt_graphs = on != 0;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_step_settings* cfg,
+                                               const double* scales, int64_t nscales, gb_optimizer_report* report) {
+  StepArgs a;
+  int rc = opt_setup(m, cfg, scales, nscales, a);
+  if (rc) return rc;
+  cudaStream_t st = m->stream;
+  OptState* S = a.st;
+  const unsigned blocks = (unsigned)((a.P + kStepBlock - 1) / kStepBlock);
 
   LoopGuard guard{m, m->profiling};
   m->profiling = false;
@@ -417,10 +312,10 @@ extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_st
   if (m->opt_graphs && m->nsamples > 0 && N > 0) {
     bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess;
     if (ok) {
-      const int rc = enqueue_iteration(m, a, blocks);
+      const int rc2 = enqueue_iteration(m, a, blocks);
       cudaGraph_t g = nullptr;
       const cudaError_t e = cudaStreamEndCapture(st, &g);
-      ok = rc == GB_OK && e == cudaSuccess && g != nullptr;
+      ok = rc2 == GB_OK && e == cudaSuccess && g != nullptr;
       if (g) guard.graph = g;
       if (ok) ok = cudaGraphInstantiate(&guard.exec, g, 0) == cudaSuccess;
     }
@@ -443,8 +338,8 @@ extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_st
       if (guard.exec) {
         GB_OPT_CUDA(cudaGraphLaunch(guard.exec, st));
       } else {
-        const int rc = enqueue_iteration(m, a, blocks);
-        if (rc) return rc;
+        const int rc2 = enqueue_iteration(m, a, blocks);
+        if (rc2) return rc2;
       }
     }
     done += k;
@@ -460,30 +355,8 @@ extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_st
   }
   // iterations exhausted without another stop: MAXIMUM_NUMBER_OF_ITERATIONS
   GB_OPT_CUDA(launch_dependent(st, k_opt_finish, 1u, a));
-  GB_OPT_CUDA(cudaMemcpyAsync(h, S, sizeof(OptState), cudaMemcpyDeviceToHost, st));
-  GB_OPT_CUDA(cudaMemcpyAsync(hp, m->d_params.p, sizeof(double) * P, cudaMemcpyDeviceToHost, st));
-  GB_OPT_CUDA(cudaMemcpyAsync(m->h_out, m->d_out.p, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
+  rc = opt_fetch(m, a, st);
+  if (rc) return rc;
   GB_OPT_CUDA(cudaStreamSynchronize(st));
-  std::copy(hp, hp + P, m->tparams.begin());
-  if (N > 0) m->last_nvalid = (uint64_t)m->h_out[1];
-  if (report) {
-    report->stop_condition = h->stop;
-    report->metric_status = h->status;
-    report->iterations = h->iteration;
-    report->value = h->value;
-    report->current_step_length = h->step_length;
-    report->gradient_magnitude = h->grad_mag;
-    report->learning_rate_relaxation = h->relaxation;
-  }
-  if (h->stop == GB_STOP_COSTFUNCTION_ERROR) {
-    m->last_status = h->status;
-    if (h->status == GB_ERR_NO_VALID_POINTS)
-      return fail(h->status,
-                  "All samples map outside moving image buffer. The images do not sufficiently overlap. They need to "
-                  "be initialized to have more overlap before this metric will work. For instance, you can align the "
-                  "image centers by translation.");
-    if (h->status == GB_ERR_JOINT_PDF_SUM_ZERO) return fail(h->status, "Joint PDF summed to zero");
-    return fail(h->status, "metric evaluation failed during optimization");
-  }
-  return GB_OK;
+  return opt_collect(m, a, report);
 }
