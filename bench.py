@@ -53,6 +53,13 @@ def parse():
     ap.add_argument("--metric", default="mattes", choices=["mattes", "msq"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forms-paths", default="plain,loop",
+                    help="paths measured beside the batched engine: plain (host loop, one call per iteration), "
+                         "loop (device optimizer loop per registration)")
+    ap.add_argument("--only-forms", action="store_true", help="skip the single-evaluation measurement")
+    ap.add_argument("--forms", default="batched,served",
+                    help="also measure the batched (64 registrations) and served (Poisson requests) forms; "
+                         "'' to skip")
     args = ap.parse_args()
     bs = args.transform == "bspline"
     if args.size is None:
@@ -254,8 +261,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_forms_only(args):
+    """The batched and served forms alone (for profiling their kernels)."""
+    t_gen = time.perf_counter()
+    inst = forms_instances(3, FORMS_N, 3000)
+    t_gen = time.perf_counter() - t_gen
+    line = {"metric": "batched/served forms", "impl": "gb300"}
+    if "batched" in args.forms:
+        line["batched"] = run_batched_form(args, inst, t_gen)
+    if "served" in args.forms:
+        line["served"] = run_served_form(args, inst)
+    print(json.dumps(line), flush=True)
+
+
 def run_gb300(args):
     world, rank, local, dist = dist_setup()
+    if args.only_forms:
+        return run_forms_only(args) if rank == 0 else None
     import torch
 
     from itk_gb300 import (MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4, context,
@@ -404,7 +426,294 @@ def run_gb300(args):
     }
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(args, fixed, moving, grad, pts, U, args.cpu_seconds)
+    if args.forms and world == 1:
+        t_gen = time.perf_counter()
+        inst = forms_instances(3, FORMS_N, 3000)
+        t_gen = time.perf_counter() - t_gen
+        if "batched" in args.forms:
+            line["batched"] = run_batched_form(args, inst, t_gen)
+        if "served" in args.forms:
+            line["served"] = run_served_form(args, inst)
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# batched and served forms
+#
+# Batched: 64 affine registrations, instances 0-31 MeanSquares (single-modality pair,
+# dense virtual domain), 32-63 Mattes MI 50 bins (multimodal pair, 20 % RANDOM
+# samples); volume sizes log-uniform in [48^3, 256x256x200]; one full-resolution
+# level; RegularStep from the identity (physical-shift scales: R^2 for the matrix,
+# 1 for the translation; learning rate 1 mm, minimum step 5e-3, 100 iterations).  Three
+# paths run the same registrations: the plain per-call GPU path (host optimizer
+# loop, one GetValueAndDerivative call per iteration), the device optimizer loop
+# one registration after another, and the batched engine.
+# Served: 64 requests on the same image pairs (other sampling seeds), 1-3 pyramid
+# levels (shrink 4/2/1, sigma 2/1/0), 50-200 iterations per level, Poisson
+# arrivals at 80 % of the server's measured capacity, 120 GB HBM budget; the
+# plain per-call path serves the same arrivals first come first served.
+
+FORMS_N = 64
+
+
+def _form_pair(spec):
+    """(fixed, moving) arrays of one instance; runs in a spawned worker process."""
+    from itk_gb300 import data
+    size, config, instance, mm = spec
+    fixed, moving, _ = data.pair_affine(size, config=config, instance=instance, multimodal_map=mm)
+    return fixed.array, moving.array
+
+
+def _form_images(specs):
+    import multiprocessing
+    from concurrent.futures import ProcessPoolExecutor
+    workers = max(1, min(16, os.cpu_count() or 1))
+    with ProcessPoolExecutor(max_workers=workers, mp_context=multiprocessing.get_context("spawn")) as ex:
+        return list(ex.map(_form_pair, specs, chunksize=1))
+
+
+def forms_instances(config, n, seed):
+    """(size, kind, images) of the batched (config 3) or served (config 4) instances."""
+    from itk_gb300 import data
+    sizes = data.batch_instance_sizes(n, seed)
+    kinds = ["msq" if i < n // 2 else "mattes" for i in range(n)]
+    specs = [(sizes[i], config, i, kinds[i] == "mattes") for i in range(n)]
+    return sizes, kinds, _form_images(specs)
+
+
+def identity_at_center(img):
+    from itk_gb300 import AffineTransform
+    T = AffineTransform()
+    T.SetCenter(img.physical_center())
+    return T
+
+
+def plain_loop(m, T, iters, lr, min_step, relax_factor=0.5, tol=1e-4, scales=None):
+    """The plain per-call GPU path: RegularStep on the host, one GetValueAndDerivative
+    call through the C ABI per iteration (parameters up, value and derivative down)."""
+    p = T.GetParameters().copy()
+    inv = np.ones_like(p) if scales is None else 1.0 / np.asarray(scales, np.float64)
+    prev = np.zeros_like(p)
+    relax = 1.0
+    it = 0
+    while it < iters:
+        T.SetParameters(p)
+        _, d = m.GetValueAndDerivative()
+        g = d * inv
+        mag = float(np.sqrt(np.dot(g, g)))
+        it += 1
+        if mag < tol:
+            break
+        if float(np.dot(g, prev * inv)) < 0:
+            relax *= relax_factor
+        if relax * lr < min_step:
+            break
+        g = g * relax * lr
+        p = p + g / mag
+        prev = g
+    T.SetParameters(p)
+    return it
+
+
+def make_form_metric(kind, fixed, moving, T, pct, seed, bins=50):
+    from itk_gb300 import MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4
+    from itk_gb300.registration import NONE, RANDOM, setup_level
+    m = MeanSquaresImageToImageMetricv4() if kind == "msq" else MattesMutualInformationImageToImageMetricv4()
+    if kind == "mattes":
+        m.SetNumberOfHistogramBins(bins)
+    m.SetFixedImage(fixed)
+    m.SetMovingImage(moving)
+    m.SetMovingTransform(T)
+    setup_level(m, fixed, (1, 1, 1), 0.0, True, NONE if kind == "msq" else RANDOM, pct, seed)
+    return m
+
+
+def forms_scales(img):
+    """Parameter scales in the manner of RegistrationParameterScalesFromPhysicalShift:
+    a matrix entry moves points by about the image's half extent R, a translation
+    by 1 mm, so the matrix scales are R^2 and the translation scales 1."""
+    R = 0.5 * float(max(np.asarray(img.GetSize()) * img.spacing))
+    return np.array([R * R] * 9 + [1.0] * 3)
+
+
+FORMS_LR, FORMS_MIN_STEP, FORMS_ITERS = 1.0, 5e-3, 100
+
+
+def run_batched_form(args, inst, t_gen):
+    from itk_gb300 import Image, RegistrationBatch, RegularStepGradientDescentOptimizerv4
+    sizes, kinds, imgs = inst
+    paths = args.forms_paths.split(",")
+    lr, min_step, iters = FORMS_LR, FORMS_MIN_STEP, FORMS_ITERS
+    regs = []
+    for i, (size, kind, (fa, ma)) in enumerate(zip(sizes, kinds, imgs)):
+        fixed, moving = Image(fa), Image(ma)
+        T = identity_at_center(fixed)
+        m = make_form_metric(kind, fixed, moving, T, 0.2, 3000 + i)
+        regs.append((m, T, T.GetParameters().copy(), m.GetNumberOfDomainPoints(), forms_scales(fixed), kind))
+
+    def optimizer(m, sc):
+        o = RegularStepGradientDescentOptimizerv4()
+        o.SetMetric(m)
+        o.SetLearningRate(lr)
+        o.SetMinimumStepLength(min_step)
+        o.SetNumberOfIterations(iters)
+        o.SetScales(sc)
+        return o
+
+    def plain(sel):
+        t0 = time.perf_counter()
+        its = []
+        for m, T, p0, _, sc, _ in sel:
+            T.SetParameters(p0)
+            its.append(plain_loop(m, T, iters, lr, min_step, scales=sc))
+        return time.perf_counter() - t0, its, [T.GetParameters().copy() for _, T, _, _, _, _ in sel]
+
+    def loop(sel):
+        t0 = time.perf_counter()
+        its = []
+        for m, T, p0, _, sc, _ in sel:
+            T.SetParameters(p0)
+            o = optimizer(m, sc)
+            o.StartOptimization()
+            its.append(o.GetCurrentIteration())
+        return time.perf_counter() - t0, its, [T.GetParameters().copy() for _, T, _, _, _, _ in sel]
+
+    def batched(sel, tune=True):
+        b = RegistrationBatch()
+        opts = []
+        for m, T, p0, _, sc, _ in sel:
+            T.SetParameters(p0)
+            opts.append(optimizer(m, sc))
+        for o in opts:
+            b.Add(o)
+        t_tune = time.perf_counter()
+        spb = b.Autotune(iterations=2) if tune else b.GetSamplesPerBlock()
+        t_tune = time.perf_counter() - t_tune
+        t0 = time.perf_counter()
+        b.Run()
+        dt = time.perf_counter() - t0
+        return dt, [o.GetCurrentIteration() for o in opts], [T.GetParameters().copy() for _, T, _, _, _, _ in sel], \
+            spb, t_tune, b.GetStats()
+
+    def disp(sel, a, b):
+        """Displacement-field difference of two affine results over each fixed image
+        (RMS over a 9^3 grid of points, in voxels)."""
+        out = []
+        for (m, T, _, _, _, _), x, y in zip(sel, a, b):
+            nx, ny, nz = m.GetFixedImage().GetSize()
+            g = np.stack(np.meshgrid(*(np.linspace(0, n - 1, 9) for n in (nx, ny, nz)), indexing="ij"), -1)
+            q = g.reshape(-1, 3) - T.GetCenter()
+            dm = x[:9].reshape(3, 3) - y[:9].reshape(3, 3)
+            d = q @ dm.T + (x[9:] - y[9:])
+            out.append(float(np.sqrt(np.mean(np.sum(d * d, axis=1)))))
+        return {"median": float(np.median(out)), "p95": float(np.percentile(out, 95)), "max": float(np.max(out))}
+
+    def evals(sel, its):
+        return float(sum(n * k for (_, _, _, n, _, _), k in zip(sel, its)))
+
+    out = {"registrations": FORMS_N,
+           "workload": "64 affine registrations, sizes log-uniform 48^3..256x256x200, 32 MeanSquares dense + "
+                       "32 Mattes 50 bins 20% RANDOM, 1 level, RegularStep from the identity: learning rate 1 mm, "
+                       "minimum step 5e-3, <=100 iterations, physical-shift scales (R^2 matrix, 1 translation)"}
+    groups = [("all", regs), ("mattes", [r for r in regs if r[5] == "mattes"])]
+    for name, sel in groups:
+        res = {}
+        tp, ip, pp = plain(sel) if "plain" in paths else (None, None, None)
+        tl, il, pl = loop(sel) if "loop" in paths else (None, None, None)
+        tb, ib, pb, spb, t_tune, stats = batched(sel)
+        res["regs_per_s"] = {"batched": len(sel) / tb}
+        res["msamples_per_s"] = {"batched": evals(sel, ib) / tb / 1e6}
+        res["seconds"] = {"batched": tb, "autotune": t_tune}
+        res["iterations_total"] = {"batched": int(sum(ib))}
+        if tp is not None:
+            res["regs_per_s"]["plain_per_call"] = len(sel) / tp
+            res["msamples_per_s"]["plain_per_call"] = evals(sel, ip) / tp / 1e6
+            res["seconds"]["plain_per_call"] = tp
+            res["iterations_total"]["plain_per_call"] = int(sum(ip))
+            res["speedup_batched_vs_plain"] = tp / tb
+            res["final_displacement_diff_voxels_batched_vs_plain"] = disp(sel, pb, pp)
+        if tl is not None:
+            res["regs_per_s"]["device_loop"] = len(sel) / tl
+            res["msamples_per_s"]["device_loop"] = evals(sel, il) / tl / 1e6
+            res["seconds"]["device_loop"] = tl
+            res["iterations_total"]["device_loop"] = int(sum(il))
+        res["samples_per_block"] = list(spb)
+        res["batch_stats"] = dict(zip(("iterations", "table_rebuilds", "rebuild_seconds"), stats))
+        out[name] = res
+    out["generate_inputs_s"] = t_gen
+    out["accuracy"] = ("same evaluation kernels as the plain path (value within 1e-5, derivative within 1e-4 of "
+                       "the FP64 oracle in the parity tests); registrations that stop after different numbers of "
+                       "relaxations end at different points of the same optimum's valley")
+    return out
+
+
+def run_served_form(args, inst):
+    from itk_gb300 import Image, RegistrationRequest, RegistrationServer
+    from itk_gb300.registration import NONE, RANDOM
+    sizes, kinds, imgs = inst
+    rng = np.random.default_rng(4000)
+    reqs = []
+    for i, (size, kind, (fa, ma)) in enumerate(zip(sizes, kinds, imgs)):
+        fixed, moving = Image(fa), Image(ma)
+        L = int(rng.integers(1, 4))
+        its = [int(x) for x in rng.integers(50, 201, size=L)]
+        reqs.append(RegistrationRequest(
+            fixed=fixed, moving=moving, transform=identity_at_center(fixed), metric=kind, bins=50,
+            shrink_factors=[4, 2, 1][3 - L:], smoothing_sigmas=[2.0, 1.0, 0.0][3 - L:],
+            sampling=NONE if kind == "msq" else RANDOM, sampling_percentage=0.2, seed=4000 + i, iterations=its,
+            learning_rate=FORMS_LR, minimum_step_length=FORMS_MIN_STEP, scales=forms_scales(fixed)))
+    # capacity: every request at t = 0
+    srv = RegistrationServer(hbm_budget_bytes=120e9)
+    res0, wall0 = srv.serve(reqs, [0.0] * len(reqs))
+    capacity = len(reqs) / wall0
+    rate = 0.8 * capacity
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs)))
+    arrivals -= arrivals[0]
+    srv = RegistrationServer(hbm_budget_bytes=120e9)
+    res, wall = srv.serve(reqs, list(arrivals))
+    lat = np.array([r.latency for r in res])
+    same = all(np.array_equal(a.parameters, b.parameters) for a, b in zip(res, res0))
+    # plain per-call path: the same requests first come first served (service times measured)
+    from itk_gb300 import MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4
+    from itk_gb300.registration import setup_level
+    service = []
+    for r in reqs:
+        t0 = time.perf_counter()
+        m = MeanSquaresImageToImageMetricv4() if r.metric == "msq" else MattesMutualInformationImageToImageMetricv4()
+        if r.metric == "mattes":
+            m.SetNumberOfHistogramBins(r.bins)
+        m.SetFixedImage(r.fixed)
+        m.SetMovingImage(r.moving)
+        T = identity_at_center(r.fixed)
+        m.SetMovingTransform(T)
+        seed = r.seed
+        for lv in range(r.levels):
+            _, seed = setup_level(m, r.fixed, (r.shrink_factors[lv],) * 3, r.smoothing_sigmas[lv], True, r.sampling,
+                                  r.sampling_percentage, seed)
+            plain_loop(m, T, r.iterations[lv], r.learning_rate, r.minimum_step_length, scales=r.scales)
+        service.append(time.perf_counter() - t0)
+    done, plain_lat = 0.0, []
+    for a, s in zip(arrivals, service):
+        start = max(a, done)
+        done = start + s
+        plain_lat.append(done - a)
+    plain_lat = np.array(plain_lat)
+    return {
+        "requests": len(reqs),
+        "workload": "64 requests, sizes log-uniform 48^3..256x256x200, half MeanSquares dense / half Mattes 50 bins "
+                    "20% RANDOM, 1-3 levels (shrink 4/2/1, sigma 2/1/0), 50-200 iterations per level",
+        "arrivals": f"Poisson, {rate:.2f} req/s = 80% of the measured capacity {capacity:.2f} req/s",
+        "hbm_budget_gb": 120, "peak_admitted_gb": srv.peak_bytes / 1e9,
+        "regs_per_s": {"served": len(reqs) / wall, "plain_per_call": len(reqs) / max(done, sum(service))},
+        "latency_s": {"served_p50": float(np.percentile(lat, 50)), "served_p99": float(np.percentile(lat, 99)),
+                      "plain_p50": float(np.percentile(plain_lat, 50)),
+                      "plain_p99": float(np.percentile(plain_lat, 99))},
+        "capacity_regs_per_s": capacity,
+        "level_setups": {"count": srv.setups, "seconds_total": srv.setup_seconds,
+                         "note": "image upload, device smoothing / shrink / gradient filter, host sample points, "
+                                 "Initialize; on 2 host threads beside the batch"},
+        "results_equal_alone_vs_mixed_arrivals": bool(same),
+    }
 
 
 def main():

@@ -177,6 +177,8 @@ int gb_metric_get_joint_pdf(gb_metric *m, double *out, int64_t n);
 int gb_metric_get_mattes_state(gb_metric *m, double out8[8]);
 
 /* ---- device-resident form (no host copies) ----------------------------- */
+/* Device memory the handle holds (images, pyramids, samples, caches, optimizer state), in bytes. */
+int gb_metric_get_device_bytes(gb_metric *m, uint64_t *bytes);
 /* CUDA stream the handle launches on (cudaStream_t as an integer). */
 int gb_metric_get_stream(gb_metric *m, uint64_t *stream);
 /* Enqueue one evaluation on the handle's stream with the parameters already
@@ -332,6 +334,9 @@ int gb_batch_get_samples_per_block(gb_batch *b, int64_t spb[3]);
 int gb_batch_autotune(gb_batch *b, int iterations, int64_t spb[3]);
 /* Capture the iteration in a CUDA graph (default on). */
 int gb_batch_set_graphs(gb_batch *b, int on);
+/* Iterations launched, table rebuilds (registrations joining or leaving) and
+ * the host seconds they took, since the batch was created. */
+int gb_batch_get_stats(gb_batch *b, int64_t *iterations, int64_t *rebuilds, double *rebuild_seconds);
 
 /* ---- metric sample points ----------------------------------------------- */
 /* ImageRegistrationMethodv4's sampling strategies

@@ -14,12 +14,14 @@ from .metrics import (ImageToImageMetricv4, MattesMutualInformationImageToImageM
                       MeanSquaresImageToImageMetricv4, context)
 from .optimizers import RegularStepGradientDescentOptimizerv4
 from .registration import ImageRegistrationMethodv4, sample_count, sample_points
+from .serving import RegistrationRequest, RegistrationResult, RegistrationServer
 from .transforms import AffineTransform, BSplineTransform, CompositeTransform
 
 __all__ = [
     "AffineTransform", "BSplineTransform", "CompositeTransform", "ExceptionObject", "GradientImage",
     "GradientRecursiveGaussianImageFilter", "Image", "ImageRegistrationMethodv4", "ImageToImageMetricv4",
     "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
-    "RegistrationBatch", "RegularStepGradientDescentOptimizerv4", "ShrinkImageFilter", "SmoothingRecursiveGaussianImageFilter", "context",
+    "RegistrationBatch", "RegistrationRequest", "RegistrationResult", "RegistrationServer",
+    "RegularStepGradientDescentOptimizerv4", "ShrinkImageFilter", "SmoothingRecursiveGaussianImageFilter", "context",
     "lib", "library_path", "sample_count", "sample_points", "shrink_geometry",
 ]

@@ -111,6 +111,7 @@ SIGNATURES = {
     "gb_metric_get_joint_pdf": [_P, _P, _I64],
     "gb_metric_get_mattes_state": [_P, _P],
     "gb_metric_get_stream": [_P, _P],
+    "gb_metric_get_device_bytes": [_P, _P],
     "gb_metric_evaluate_device": [_P, _P, _P, _I],
     "gb_metric_synchronize": [_P],
     "gb_msq_affine_noalloc": [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _U64],
@@ -127,6 +128,7 @@ SIGNATURES = {
     "gb_batch_get_samples_per_block": [_P, _P],
     "gb_batch_autotune": [_P, _I, _P],
     "gb_batch_set_graphs": [_P, _I],
+    "gb_batch_get_stats": [_P, _P, _P, _P],
     "gb_sample_count": [_I, _P, _D, _P],
     "gb_sample_points": [_I, _P, _P, _P, _P, _D, ctypes.c_int32, _P, _I64, _P, _P],
 }

@@ -91,5 +91,11 @@ class RegistrationBatch:
         check(self._L.gb_batch_autotune(self._h, int(iterations), ptr(out)))
         return tuple(int(x) for x in out)
 
+    def GetStats(self):
+        """(iterations launched, table rebuilds, host seconds spent rebuilding)."""
+        it, rb, sec = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+        check(self._L.gb_batch_get_stats(self._h, ctypes.byref(it), ctypes.byref(rb), ctypes.byref(sec)))
+        return int(it.value), int(rb.value), float(sec.value)
+
     def SetUseCudaGraphs(self, on: bool):
         check(self._L.gb_batch_set_graphs(self._h, int(bool(on))))

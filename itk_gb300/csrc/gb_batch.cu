@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -205,6 +206,10 @@ struct gb_batch {
   int* h_halts = nullptr;  // pinned, 2 slots of (capacity + 1)
   size_t h_halts_cap = 0;
   int64_t goff[kGroups] = {}, gcnt[kGroups] = {};
+  std::vector<int64_t> reg_work;  // work items of each running registration (all passes)
+  int64_t total_work = 0;
+  int64_t iterations = 0, rebuilds = 0;
+  double rebuild_seconds = 0.0;
   size_t smem1 = 0, smem2 = 0;
   bool dirty = true;
   cudaGraph_t graph = nullptr;
@@ -252,7 +257,17 @@ int enqueue_iteration(gb_batch* b, bool step) {
 }
 
 // Tables of the registrations still running, uploaded; the iteration graph re-captured.
+int rebuild_tables(gb_batch* b);
+
 int rebuild(gb_batch* b) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const int rc = rebuild_tables(b);
+  b->rebuild_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  b->rebuilds += 1;
+  return rc;
+}
+
+int rebuild_tables(gb_batch* b) {
   b->drop_graph();
   b->active.clear();
   for (size_t i = 0; i < b->regs.size(); ++i)
@@ -265,6 +280,8 @@ int rebuild(gb_batch* b) {
   std::vector<ClearItem> ci(n);
   std::vector<int4> work[kGroups];
   int maxbins = 0;
+  b->reg_work.assign(n, 0);
+  b->total_work = 0;
   for (size_t k = 0; k < n; ++k) {
     gb_batch::Reg& R = b->regs[(size_t)b->active[k]];
     gb_metric* m = R.m;
@@ -279,6 +296,7 @@ int rebuild(gb_batch* b) {
       const int64_t nv = vblocks(m->nsamples, b->spb[kSpbMsq]);
       for (int64_t v = 0; v < nv; ++v)
         work[cd ? kGrpMsqCD : kGrpMsqImage].push_back(make_int4((int)k, (int)v, (int)nv, 0));
+      b->reg_work[k] = nv;
     } else {
       maxbins = std::max(maxbins, (int)m->bins);
       const int64_t n1 = vblocks(m->nsamples, b->spb[kSpbPass1]);
@@ -286,7 +304,9 @@ int rebuild(gb_batch* b) {
         work[cd ? kGrpP1CD : kGrpP1Image].push_back(make_int4((int)k, (int)v, (int)n1, 0));
       const int64_t n2 = vblocks(m->nsamples, b->spb[kSpbPass2]);
       for (int64_t v = 0; v < n2; ++v) work[kGrpP2].push_back(make_int4((int)k, (int)v, (int)n2, 0));
+      b->reg_work[k] = n1 + n2;
     }
+    b->total_work += b->reg_work[k];
   }
   std::vector<int4> all;
   for (int g = 0; g < kGroups; ++g) {
@@ -337,16 +357,6 @@ int rebuild(gb_batch* b) {
       b->drop_graph();
     }
   }
-  return GB_OK;
-}
-
-// Final state of a stopped registration into its handle and report.
-int collect(gb_batch* b, gb_batch::Reg& R) {
-  int rc = opt_fetch(R.m, R.step, b->stream);
-  if (rc) return rc;
-  GB_B_CUDA(cudaStreamSynchronize(b->stream));
-  R.rc = opt_collect(R.m, R.step, &R.report);
-  R.done = true;
   return GB_OK;
 }
 
@@ -429,12 +439,40 @@ extern "C" int gb_batch_add(gb_batch* b, gb_metric* m, const gb_regular_step_set
   return GB_OK;
 }
 
+// Collects every registration of the current tables that has stopped (the stream drains first).
+static int collect_halted(gb_batch* b, bool& any) {
+  cudaStream_t st = b->stream;
+  const int n = (int)b->active.size();
+  any = false;
+  if (n == 0) return GB_OK;
+  GB_B_CUDA(cudaStreamSynchronize(st));
+  GB_B_CUDA(launch_dep(st, k_batch_halts, 1u, kBlock, 0, (const StepArgs*)b->d_step.p, n, b->d_halts.p));
+  GB_B_CUDA(cudaMemcpyAsync(b->h_halts, b->d_halts.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st));
+  GB_B_CUDA(cudaStreamSynchronize(st));
+  std::vector<int> idx;
+  for (int k = 0; k < n; ++k)
+    if (b->h_halts[k] && !b->regs[(size_t)b->active[k]].done) idx.push_back(b->active[k]);
+  for (int r : idx) {  // the copies of every stopped registration, then one wait
+    int rc = opt_fetch(b->regs[(size_t)r].m, b->regs[(size_t)r].step, st);
+    if (rc) return rc;
+  }
+  GB_B_CUDA(cudaStreamSynchronize(st));
+  for (int r : idx) {
+    gb_batch::Reg& R = b->regs[(size_t)r];
+    R.rc = opt_collect(R.m, R.step, &R.report);
+    R.done = true;
+    any = true;
+  }
+  return GB_OK;
+}
+
 extern "C" int gb_batch_run(gb_batch* b, int64_t max_iterations, int64_t* running) {
   if (!b) return fail(GB_ERR_BAD_ARG, "null batch");
   GB_B_CUDA(cudaSetDevice(b->ctx->device));
   cudaStream_t st = b->stream;
   int64_t done = 0;
   int64_t batch = 2;
+  bool collected = false;
   while (max_iterations <= 0 || done < max_iterations) {
     if (b->dirty) {
       const int rc = rebuild(b);
@@ -442,9 +480,12 @@ extern "C" int gb_batch_run(gb_batch* b, int64_t max_iterations, int64_t* runnin
     }
     const int n = (int)b->active.size();
     if (n == 0) break;
-    // two batches in flight: enqueue batch j + 1 before reading batch j's halt words
+    // Two batches of iterations in flight: batch j + 1 is enqueued before batch j's
+    // halt words are read.  Stopped registrations stay in the tables (their blocks
+    // return at once) until they hold half of the work items, then the tables are
+    // rebuilt without them.
     int slot = 0;
-    bool pending = false, changed = false;
+    bool pending = false, shrink = false;
     while (max_iterations <= 0 || done < max_iterations) {
       const int64_t k = max_iterations <= 0 ? batch : std::min(batch, max_iterations - done);
       for (int64_t i = 0; i < k; ++i) {
@@ -456,6 +497,7 @@ extern "C" int gb_batch_run(gb_batch* b, int64_t max_iterations, int64_t* runnin
         }
       }
       done += k;
+      b->iterations += k;
       batch = std::min<int64_t>(batch * 2, 16);
       int* hh = b->h_halts + slot * (n + 1);
       GB_B_CUDA(launch_dep(st, k_batch_halts, 1u, kBlock, 0, (const StepArgs*)b->d_step.p, n, b->d_halts.p));
@@ -463,34 +505,47 @@ extern "C" int gb_batch_run(gb_batch* b, int64_t max_iterations, int64_t* runnin
       GB_B_CUDA(cudaEventRecord(b->ev[slot], st));
       if (pending) {
         GB_B_CUDA(cudaEventSynchronize(b->ev[slot ^ 1]));
-        if (b->h_halts[(slot ^ 1) * (n + 1) + n] < n) {
-          changed = true;
+        const int* ph = b->h_halts + (slot ^ 1) * (n + 1);
+        if (ph[n] == 0) {  // all stopped
+          shrink = true;
           break;
+        }
+        if (ph[n] < n) {
+          int64_t hw = 0;
+          for (int r = 0; r < n; ++r)
+            if (ph[r]) hw += b->reg_work[(size_t)r];
+          if (2 * hw >= b->total_work) {
+            shrink = true;
+            break;
+          }
         }
       }
       pending = true;
       slot ^= 1;
     }
-    // collect every registration that has stopped (the stream drains first)
-    GB_B_CUDA(cudaStreamSynchronize(st));
-    GB_B_CUDA(launch_dep(st, k_batch_halts, 1u, kBlock, 0, (const StepArgs*)b->d_step.p, n, b->d_halts.p));
-    GB_B_CUDA(cudaMemcpyAsync(b->h_halts, b->d_halts.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st));
-    GB_B_CUDA(cudaStreamSynchronize(st));
     bool any = false;
-    for (int k = 0; k < n; ++k)
-      if (b->h_halts[k]) {
-        const int rc = collect(b, b->regs[(size_t)b->active[k]]);
-        if (rc) return rc;
-        any = true;
-      }
-    if (any) b->dirty = true;
-    if (!changed) break;  // iteration budget of this call used up
+    const int rc = collect_halted(b, any);
+    if (rc) return rc;
+    collected = collected || any;
+    if (!shrink) break;  // iteration budget of this call used up
+    b->dirty = true;
   }
+  // the caller may re-initialize or destroy the metrics of finished registrations:
+  // the next call starts from tables without them
+  if (collected) b->dirty = true;
   if (running) {
     int64_t r = 0;
     for (const gb_batch::Reg& R : b->regs) r += R.done ? 0 : 1;
     *running = r;
   }
+  return GB_OK;
+}
+
+extern "C" int gb_batch_get_stats(gb_batch* b, int64_t* iterations, int64_t* rebuilds, double* rebuild_seconds) {
+  if (!b) return fail(GB_ERR_BAD_ARG, "null batch");
+  if (iterations) *iterations = b->iterations;
+  if (rebuilds) *rebuilds = b->rebuilds;
+  if (rebuild_seconds) *rebuild_seconds = b->rebuild_seconds;
   return GB_OK;
 }
 

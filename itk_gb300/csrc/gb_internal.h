@@ -41,6 +41,7 @@ struct DevBuf {
     p = nullptr;
     n = 0;
   }
+  size_t bytes() const { return n * sizeof(T); }
   cudaError_t alloc(size_t count) {
     if (count <= n && p) return cudaSuccess;
     reset();
@@ -154,6 +155,8 @@ struct gb_metric {
   unsigned char* h_opt = nullptr;   // pinned copy of the state
   int* h_halt = nullptr;            // pinned halt flags, one per batch slot
   bool opt_graphs = true;           // capture each iteration in a CUDA graph
+
+  size_t device_bytes() const;  // all device buffers of the handle (gb_metric.cu)
 
   // per-kernel event timing (gb_metric_set_profiling)
   bool profiling = false;

@@ -1005,6 +1005,20 @@ extern "C" int gb_metric_get_mattes_state(gb_metric* m, double out8[8]) {
   return GB_OK;
 }
 
+size_t gb_metric::device_bytes() const {
+  return d_fixed.bytes() + d_moving.bytes() + d_fixed_s.bytes() + d_moving_s.bytes() + d_grad_in.bytes() +
+         d_mov4.bytes() + d_samples.bytes() + d_cache.bytes() + d_sup.bytes() + d_chunks.bytes() +
+         d_node_first.bytes() + d_node_entries.bytes() + d_chunk_part.bytes() + d_nodes.bytes() + d_params.bytes() +
+         d_acc.bytes() + d_scratch.bytes() + d_out.bytes() + d_status.bytes() + d_pratio.bytes() + d_pdf.bytes() +
+         d_consts.bytes() + d_opt.bytes() + d_opt_vec.bytes();
+}
+
+extern "C" int gb_metric_get_device_bytes(gb_metric* m, uint64_t* bytes) {
+  if (!m || !bytes) return fail(GB_ERR_BAD_ARG, "null argument");
+  *bytes = (uint64_t)m->device_bytes();
+  return GB_OK;
+}
+
 extern "C" int gb_metric_get_stream(gb_metric* m, uint64_t* stream) {
   if (!m || !stream) return fail(GB_ERR_BAD_ARG, "null argument");
   *stream = (uint64_t)(uintptr_t)m->stream;

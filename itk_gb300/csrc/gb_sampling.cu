@@ -15,10 +15,13 @@
 // (PointSet's default coordinate type), accumulated in float exactly as the
 // reference's compound assignments do, and the normal variates use the host's
 // log / cos, as the reference does.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <random>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "gb_internal.h"
 
@@ -26,44 +29,56 @@ namespace gb {
 
 namespace {
 
-class Variates {
- public:
-  explicit Variates(int32_t seed) : g_((uint32_t)seed) {}
-  uint32_t integer() { return (uint32_t)g_(); }
-  // GetVariateWithOpenRange: (0, 1)
-  double open_range() { return ((double)integer() + 0.5) / 4294967296.0; }
-  // GetVariateWithOpenUpperRange: [0, 1)
-  double open_upper_range() { return (double)integer() / 4294967296.0; }
-  // GetNormalVariate(0, 1): the Box-Muller cosine branch, one variate per call
-  double normal() {
-    const double r = std::sqrt((-2.0 * std::log(1.0 - open_range())) * 1.0);
-    const double phi = (2.0 * 3.141592653589793238462643383279502884) * open_upper_range();
-    return 0.0 + r * std::cos(phi);
-  }
+// GetVariateWithOpenRange (0, 1) and GetVariateWithOpenUpperRange [0, 1) of one 32-bit output.
+inline double open_range(uint32_t u) { return ((double)u + 0.5) / 4294967296.0; }
+inline double open_upper_range(uint32_t u) { return (double)u / 4294967296.0; }
 
- private:
-  std::mt19937 g_;
-};
+// GetNormalVariate(0, 1) from two consecutive outputs: the Box-Muller cosine branch.
+inline double normal(uint32_t u1, uint32_t u2) {
+  const double r = std::sqrt((-2.0 * std::log(1.0 - open_range(u1))) * 1.0);
+  const double phi = (2.0 * 3.141592653589793238462643383279502884) * open_upper_range(u2);
+  return 0.0 + r * std::cos(phi);
+}
 
 // TransformIndexToPhysicalPoint into a float point, then the jitter
-// point[d] += N(0,1) * spacing[d] / 3, each step rounded to float.
+// point[d] += N(0,1) * spacing[d] / 3, each step rounded to float; `u` holds the
+// sample's six jitter outputs.
 struct PointMaker {
   double i2p[9];
   double origin[3];
   double third[3];
-  void make(int64_t ix, int64_t iy, int64_t iz, Variates& rnd, float* out) const {
+  void make(int64_t ix, int64_t iy, int64_t iz, const uint32_t* u, float* out) const {
     const int64_t idx[3] = {ix, iy, iz};
     float p[3];
     for (int i = 0; i < 3; ++i) {
       p[i] = (float)origin[i];
       for (int j = 0; j < 3; ++j) p[i] = (float)((double)p[i] + i2p[3 * i + j] * (double)idx[j]);
     }
-    for (int d = 0; d < 3; ++d) p[d] = (float)((double)p[d] + rnd.normal() * third[d]);
+    for (int d = 0; d < 3; ++d) p[d] = (float)((double)p[d] + normal(u[2 * d], u[2 * d + 1]) * third[d]);
     out[0] = p[0];
     out[1] = p[1];
     out[2] = p[2];
   }
 };
+
+// body(k0, k1) over [0, n) split across the host's threads (at most 16).
+template <typename F>
+void parallel_ranges(int64_t n, F body) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const int64_t T = std::max<int64_t>(1, std::min<int64_t>(hw, n / 16384));
+  if (T == 1) {
+    body(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  int64_t started = 0;
+  try {
+    for (; started < T; ++started) th.emplace_back(body, n * started / T, n * (started + 1) / T);
+  } catch (...) {  // no more threads: the rest runs here
+  }
+  for (std::thread& x : th) x.join();
+  if (started < T) body(n * started / T, n);
+}
 
 }  // namespace
 
@@ -109,44 +124,44 @@ extern "C" int gb_sample_points(int strategy, const int64_t size[3], const doubl
     pm.origin[i] = origin[i];
     pm.third[i] = spacing[i] / 3.0;
   }
-  // the randomizer takes m_CurrentRandomSeed++; RANDOM's iterator the next one
-  int32_t s = seed;
-  Variates rnd(s);
-  s = (int32_t)((uint32_t)s + 1u);
+  // the randomizer takes m_CurrentRandomSeed++; RANDOM's iterator the next one.  The
+  // generators' outputs are drawn in sequence; the points (float index-to-point
+  // sums, normal variates) are then formed on all host threads.
+  const int32_t s_jitter = seed;
+  const int32_t s_iter = (int32_t)((uint32_t)seed + 1u);
+  const int32_t s = (int32_t)((uint32_t)seed + (strategy == GB_SAMPLING_RANDOM ? 2u : 1u));
+  std::vector<uint32_t> jitter((size_t)(6 * n));
+  auto draw_jitter = [&]() {
+    std::mt19937 rnd((uint32_t)s_jitter);
+    for (uint32_t& u : jitter) u = (uint32_t)rnd();
+  };
   const int64_t nx = size[0], ny = size[1];
+  std::vector<int64_t> vox((size_t)n);
   if (strategy == GB_SAMPLING_REGULAR) {
-    const uint64_t step = (uint64_t)std::ceil(1.0 / percentage);
-    uint64_t c = step;  // the first voxel is a sample
-    int64_t k = 0;
-    const int64_t V = size[0] * size[1] * size[2];
-    for (int64_t v = 0; v < V; ++v) {
-      if (c == step) {
-        c = 0;
-        pm.make(v % nx, (v / nx) % ny, v / (nx * ny), rnd, xyz + 3 * k);
-        ++k;
-      }
-      ++c;
-    }
+    // every ceil(1 / percentage)-th voxel in scan order, starting with the first
+    draw_jitter();
+    const int64_t step = (int64_t)std::ceil(1.0 / percentage);
+    for (int64_t k = 0; k < n; ++k) vox[(size_t)k] = k * step;
   } else {
-    Variates it(s);
-    s = (int32_t)((uint32_t)s + 1u);
-    const double span = (double)(size[0] * size[1] * size[2]) - 0.5;
-    // GoToBegin jumps once before the first sample; every ++ jumps again
-    auto jump = [&](int64_t& ix, int64_t& iy, int64_t& iz) {
-      int64_t pos = (int64_t)(it.open_range() * span);
-      ix = pos % nx;
-      pos = (pos - ix) / nx;
-      iy = pos % ny;
-      pos = (pos - iy) / ny;
-      iz = pos;
-    };
-    int64_t ix, iy, iz;
-    jump(ix, iy, iz);
-    for (int64_t k = 0; k < n; ++k) {
-      pm.make(ix, iy, iz, rnd, xyz + 3 * k);
-      jump(ix, iy, iz);
+    // ImageRandomConstIteratorWithIndex: GoToBegin jumps once, every ++ jumps again.
+    // The two generators are independent: the jitter stream is drawn on a second thread.
+    std::thread other;
+    try {
+      other = std::thread(draw_jitter);
+    } catch (...) {
+      draw_jitter();
     }
+    std::mt19937 it((uint32_t)s_iter);
+    const double span = (double)(size[0] * size[1] * size[2]) - 0.5;
+    for (int64_t k = 0; k < n; ++k) vox[(size_t)k] = (int64_t)(open_range((uint32_t)it()) * span);
+    if (other.joinable()) other.join();
   }
+  parallel_ranges(n, [&](int64_t k0, int64_t k1) {
+    for (int64_t k = k0; k < k1; ++k) {
+      const int64_t v = vox[(size_t)k];
+      pm.make(v % nx, (v / nx) % ny, v / (nx * ny), jitter.data() + 6 * k, xyz + 3 * k);
+    }
+  });
   *count = n;
   if (next_seed) *next_seed = s;
   return GB_OK;

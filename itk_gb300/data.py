@@ -185,3 +185,13 @@ def pair_affine(size_xyz, config, instance=0, multimodal_map=False):
     if multimodal_map:
         moving = multimodal(moving, seed + 3)
     return fixed, moving, T
+
+
+def batch_instance_sizes(n, seed, vmin=48 ** 3, vmax=256 * 256 * 200, aspect=(256, 256, 200)):
+    """Volume sizes of the batched / served workloads: voxel counts log-uniform in
+    [vmin, vmax], each axis the count's cube root scaled by the 256:256:200 aspect."""
+    rng = np.random.default_rng(seed)
+    v = np.exp(rng.uniform(np.log(vmin), np.log(vmax), size=n))
+    a = np.asarray(aspect, np.float64)
+    f = (v / np.prod(a)) ** (1.0 / 3.0)
+    return [tuple(int(max(8, round(x))) for x in a * fi) for fi in f]

@@ -221,6 +221,12 @@ class ImageToImageMetricv4:
         check(self._L.gb_metric_get_number_of_domain_points(self._h, ctypes.byref(n)))
         return int(n.value)
 
+    def GetDeviceBytes(self) -> int:
+        """Device memory this metric holds (images, pyramid, samples, caches, optimizer state)."""
+        n = ctypes.c_uint64()
+        check(self._L.gb_metric_get_device_bytes(self._h, ctypes.byref(n)))
+        return int(n.value)
+
     def GetNumberOfParameters(self):
         return self._transform.GetNumberOfParameters()
 

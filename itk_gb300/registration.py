@@ -47,6 +47,25 @@ def sample_points(strategy, size_xyz, spacing, origin, direction, percentage, se
     return out[:int(n[0])].copy(), int(nxt[0])
 
 
+def setup_level(metric, fixed: Image, shrink, sigma, sigma_physical, strategy, percentage, seed):
+    """InitializeRegistrationAtEachLevel for one image metric: the level's smoothing
+    and virtual-domain shrink (done on the device by Initialize), the metric sample
+    points (SetMetricSamplePoints), then Initialize.  Returns (points or None, the
+    seed the next level starts from)."""
+    metric.SetLevelShrinkFactors(shrink)
+    metric.SetLevelSmoothingSigma(sigma, sigma_physical)
+    pts = None
+    if strategy != NONE:
+        size, sp, org = shrink_geometry(fixed, shrink)
+        pts, seed = sample_points(strategy, size, sp, org, fixed.direction, percentage, seed)
+        metric.SetVirtualSampledPointSet(pts)
+        metric.SetUseSampledPointSet(True)
+    else:
+        metric.SetUseSampledPointSet(False)
+    metric.Initialize()
+    return pts, seed
+
+
 class ImageRegistrationMethodv4:
     """Defaults as the reference's: one level, shrink 1, sigma 0 in physical
     units, no sampling (the dense virtual domain), percentage 1."""
@@ -190,21 +209,10 @@ class ImageRegistrationMethodv4:
         self._level_points = []
         for level in range(self._levels):
             self._current_level = level
-            shrink = self._shrink[level]
-            m.SetLevelShrinkFactors(shrink)
-            m.SetLevelSmoothingSigma(self._sigmas[level], self._sigmas_physical)
-            if self._strategy != NONE:
-                size, sp, org = shrink_geometry(self._fixed, shrink)
-                s = int(time.time_ns() & 0x7FFFFFFF) if self._reseed_from_clock else seed
-                pts, seed = sample_points(self._strategy, size, sp, org, self._fixed.direction,
-                                          self._percentages[level], s)
-                m.SetVirtualSampledPointSet(pts)
-                m.SetUseSampledPointSet(True)
-                self._level_points.append(pts)
-            else:
-                m.SetUseSampledPointSet(False)
-                self._level_points.append(None)
-            m.Initialize()
+            s = int(time.time_ns() & 0x7FFFFFFF) if self._reseed_from_clock else seed
+            pts, seed = setup_level(m, self._fixed, self._shrink[level], self._sigmas[level], self._sigmas_physical,
+                                    self._strategy, self._percentages[level] if self._strategy != NONE else 1.0, s)
+            self._level_points.append(pts)
             opt.SetMetric(m)
             opt.StartOptimization()
         return self._transform
