@@ -7,9 +7,10 @@ transform, 256x256x200 float32 blob volumes (moving = fixed under a seeded
 affine with the multimodal intensity map), 20 % random sampling
 (2,621,440 points), gradient image supplied.  Synthetic seeded inputs stand
 in for real volumes.  `--transform bspline` measures the B-spline workload
-instead: [affine, BSplineTransform order 3 over an 8x8x8 mesh (11^3 nodes,
-3993 parameters)], 192x192x160 volumes whose moving image carries a seeded
-smooth displacement (at most 4 mm), 10 % random sampling.
+instead: [affine, BSplineTransform order 3 over a 4^3 mesh (7^3 control points,
+1029 parameters; `--mesh 5`: 8^3 control points, 1536 parameters)], 192x192x160
+volumes whose moving image carries a seeded smooth displacement (at most 4 mm),
+10 % random sampling.
 
 Prints one JSON line.  `value` is device-timed throughput with everything
 resident in HBM (CUDA events around each evaluation, L2 flushed between
@@ -44,11 +45,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--transform", default="affine", choices=["affine", "bspline"],
-                    help="affine: 256x256x200, 20%% sampling; bspline: [affine, B-spline 8x8x8 mesh], "
+                    help="affine: 256x256x200, 20%% sampling; bspline: [affine, B-spline order 3], "
                          "192x192x160, 10%% sampling")
     ap.add_argument("--size", default=None)
     ap.add_argument("--fraction", type=float, default=None)
-    ap.add_argument("--mesh", type=int, default=8)
+    ap.add_argument("--mesh", type=int, default=4,
+                    help="B-spline mesh size per axis: 4 = 7^3 control points (1029 parameters), "
+                         "5 = 8^3 control points (1536 parameters)")
     ap.add_argument("--bins", type=int, default=50)
     ap.add_argument("--metric", default="mattes", choices=["mattes", "msq"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -57,7 +60,7 @@ def parse():
                     help="paths measured beside the batched engine: plain (host loop, one call per iteration), "
                          "loop (device optimizer loop per registration)")
     ap.add_argument("--only-forms", action="store_true", help="skip the single-evaluation measurement")
-    ap.add_argument("--forms", default="batched,served",
+    ap.add_argument("--forms", default="registration,batched,served",
                     help="also measure the batched (64 registrations) and served (Poisson requests) forms; "
                          "'' to skip")
     args = ap.parse_args()
@@ -73,7 +76,7 @@ def workload(args):
     """The seeded inputs, cached (pickle) under .bench_cache/ in the repository: profiler runs
     re-run the same command."""
     import pickle
-    key = f"{args.transform}_{args.metric}_{args.size.replace(',', 'x')}_{args.fraction}_{args.mesh}"
+    key = f"{args.transform}_{args.metric}_{args.size.replace(',', 'x')}_{args.fraction}_{args.mesh}_itkpts"
     cache_dir = os.path.join(ROOT, ".bench_cache")
     os.makedirs(cache_dir, exist_ok=True)
     path = os.path.join(cache_dir, f"{key}.pkl")
@@ -91,6 +94,14 @@ def workload(args):
     return w
 
 
+def itk_points(fixed, fraction, seed):
+    """RANDOM sample points of the full-resolution level, as ImageRegistrationMethodv4 draws them."""
+    from itk_gb300 import sample_points
+    from itk_gb300.registration import RANDOM
+    pts, _ = sample_points(RANDOM, fixed.GetSize(), fixed.spacing, fixed.origin, fixed.direction, fraction, seed)
+    return pts
+
+
 def make_workload(args):
     from itk_gb300 import BSplineTransform, CompositeTransform, data
     size = tuple(int(s) for s in args.size.split(","))
@@ -99,7 +110,7 @@ def make_workload(args):
         fixed, moving, A, B = data.pair_bspline(size, (args.mesh,) * 3, instance=0,
                                                 multimodal_map=(args.metric == "mattes"))
         grad = data.gradient_image(moving)
-        pts = data.random_points(fixed, args.fraction, seed=2001)
+        pts = itk_points(fixed, args.fraction, 2001)
         Bm = BSplineTransform()
         Bm.SetFixedParameters(B.GetFixedParameters())
         Bm.SetParameters(0.5 * B.GetParameters())
@@ -109,7 +120,7 @@ def make_workload(args):
         return fixed, moving, grad, pts, U
     fixed, moving, T = data.pair_affine(size, config=1, multimodal_map=(args.metric == "mattes"))
     grad = data.gradient_image(moving)
-    pts = data.random_points(fixed, args.fraction, seed=1001)
+    pts = itk_points(fixed, args.fraction, 1001)
     # evaluate at a transform near (not at) the truth, as mid-optimization
     rng = np.random.default_rng(77)
     U = type(T)()
@@ -128,7 +139,7 @@ def config_dict(args, n_samples):
         "volume_xyz": size,
         "samples": int(n_samples),
         "bins": args.bins if args.metric == "mattes" else None,
-        "sampling": f"random {args.fraction:.0%} (virtual sampled point set)",
+        "sampling": f"RANDOM {args.fraction:.0%}, ImageRegistrationMethodv4's points (seeded Mersenne Twister)",
         "transform": (f"CompositeTransform [AffineTransform, BSplineTransform order 3, mesh {args.mesh}^3 "
                       f"({(args.mesh + 3) ** 3} nodes, {3 * (args.mesh + 3) ** 3} parameters)]")
                      if bs else "AffineTransform<double,3>",
@@ -261,12 +272,80 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_plain_registration(args):
+    """The reference's CPU-runnable case: MeanSquares registration of 64^3 blob volumes
+    (moving = fixed under a seeded affine + N(0,2) noise), dense sampling, one level,
+    RegularStep 100 iterations.  Timed through ImageRegistrationMethodv4 with the
+    device loop, and the FP64 oracle's restatement of the same loop on the host cores."""
+    from itk_gb300 import (ImageRegistrationMethodv4, MeanSquaresImageToImageMetricv4,
+                           RegularStepGradientDescentOptimizerv4, data)
+    fixed, moving, _ = data.pair_affine((64, 64, 64), config=0)
+    sc = forms_scales(fixed)
+    lr, min_step, iters = 1.0, 1e-3, 100
+
+    def run_once():
+        T = identity_at_center(fixed)
+        m = MeanSquaresImageToImageMetricv4()
+        o = RegularStepGradientDescentOptimizerv4()
+        o.SetLearningRate(lr)
+        o.SetMinimumStepLength(min_step)
+        o.SetNumberOfIterations(iters)
+        o.SetScales(sc)
+        reg = ImageRegistrationMethodv4()
+        reg.SetFixedImage(fixed)
+        reg.SetMovingImage(moving)
+        reg.SetMetric(m)
+        reg.SetOptimizer(o)
+        reg.SetInitialTransform(T)
+        t0 = time.perf_counter()
+        reg.Update()
+        return time.perf_counter() - t0, o, T
+
+    run_once()  # warm-up (module load, graph capture paths)
+    reps = 5
+    times, o, T = [], None, None
+    for _ in range(reps):
+        dt, o, T = run_once()
+        times.append(dt)
+    gpu_s = float(np.median(times))
+    out = {"workload": "MeanSquares affine registration, 64^3 blob volumes, dense, 1 level, RegularStep "
+                       f"lr {lr} min step {min_step} <= {iters} iterations, physical-shift scales",
+           "gpu_seconds_per_registration": gpu_s, "regs_per_s": 1.0 / gpu_s,
+           "iterations": o.GetCurrentIteration(), "stop": o.GetStopConditionName(),
+           "ms_per_iteration": gpu_s / max(o.GetCurrentIteration(), 1) * 1e3}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from cases import geom
+        from oracle import registration as R
+        T0 = identity_at_center(fixed)
+        k, p0, tf = T0.flat()
+        t0 = time.perf_counter()
+        p, res = R.register("msq", fixed.array, geom(fixed), moving.array, geom(moving), k, p0, tf,
+                            [dict(shrink=(1, 1, 1), sigma=0.0)],
+                            dict(learning_rate=lr, minimum_step_length=min_step, number_of_iterations=iters,
+                                 scales=sc))
+        cpu_s = time.perf_counter() - t0
+        T0.SetParameters(p)
+        d = T.GetParameters() - p
+        out["cpu_baseline"] = {"seconds_per_registration": cpu_s, "regs_per_s": 1.0 / cpu_s,
+                               "cores": os.cpu_count(), "kind": "port",
+                               "iterations": res[0]["iterations"],
+                               "sample": "one full registration with the FP64 oracle metric and the restated "
+                                         "RegularStep loop (oracle/registration.py)"}
+        out["max_param_diff_gpu_vs_cpu"] = float(np.max(np.abs(d)))
+    return out
+
+
 def run_forms_only(args):
     """The batched and served forms alone (for profiling their kernels)."""
-    t_gen = time.perf_counter()
-    inst = forms_instances(3, FORMS_N, 3000)
-    t_gen = time.perf_counter() - t_gen
+    inst, t_gen = None, 0.0
+    if "batched" in args.forms or "served" in args.forms:
+        t_gen = time.perf_counter()
+        inst = forms_instances(3, FORMS_N, 3000)
+        t_gen = time.perf_counter() - t_gen
     line = {"metric": "batched/served forms", "impl": "gb300"}
+    if "registration" in args.forms:
+        line["registration_64cubed"] = run_plain_registration(args)
     if "batched" in args.forms:
         line["batched"] = run_batched_form(args, inst, t_gen)
     if "served" in args.forms:
@@ -426,7 +505,9 @@ def run_gb300(args):
     }
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(args, fixed, moving, grad, pts, U, args.cpu_seconds)
-    if args.forms and world == 1:
+    if world == 1 and "registration" in args.forms:
+        line["registration_64cubed"] = run_plain_registration(args)
+    if world == 1 and ("batched" in args.forms or "served" in args.forms):
         t_gen = time.perf_counter()
         inst = forms_instances(3, FORMS_N, 3000)
         t_gen = time.perf_counter() - t_gen

@@ -7,11 +7,12 @@
   affine about the image centre (Euler angles U(+-8 deg), translations
   U(+-5 mm), scales U(0.95, 1.05)) plus fresh N(0, 2) noise;
 * multimodal variant: v' = 1000 (max(v, 0) / max)^1.7 + N(0, 5);
-* random sampling: uniform voxel picks with replacement plus N(0, spacing/3)
+* random_points: uniform voxel picks with replacement plus N(0, spacing/3)
   jitter per coordinate, stored as float32 points -- the shape of
   ImageRegistrationMethodv4's RANDOM strategy
-  (Registration/RegistrationMethodsv4/include/itkImageRegistrationMethodv4.hxx:965-1003),
-  drawn from numpy's generator rather than ITK's Mersenne Twister.
+  (Registration/RegistrationMethodsv4/include/itkImageRegistrationMethodv4.hxx:965-1003)
+  from numpy's generator, for tests; itk_gb300.sample_points draws the
+  reference's own points (its Mersenne Twister, bit for bit).
 
 The seed of an instance is 1000 * config + instance.
 """
