@@ -789,10 +789,10 @@ def run_served_form(args, inst):
         "latency_s": {"served_p50": float(np.percentile(lat, 50)), "served_p99": float(np.percentile(lat, 99)),
                       "plain_p50": float(np.percentile(plain_lat, 50)),
                       "plain_p99": float(np.percentile(plain_lat, 99))},
-        "capacity_regs_per_s": capacity,
+        "capacity_regs_per_s": {"served": capacity, "plain_per_call": len(reqs) / float(sum(service))},
         "level_setups": {"count": srv.setups, "seconds_total": srv.setup_seconds,
                          "note": "image upload, device smoothing / shrink / gradient filter, host sample points, "
-                                 "Initialize; on 2 host threads beside the batch"},
+                                 "Initialize; on 4 host threads beside the batch"},
         "results_equal_alone_vs_mixed_arrivals": bool(same),
     }
 

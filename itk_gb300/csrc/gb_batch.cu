@@ -324,11 +324,11 @@ int rebuild_tables(gb_batch* b) {
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem1));
     GB_B_CUDA(cudaFuncSetAttribute(k_batch_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem2));
   }
-  GB_B_CUDA(b->d_eval.alloc(n));
-  GB_B_CUDA(b->d_step.alloc(n));
-  GB_B_CUDA(b->d_clear.alloc(n));
-  GB_B_CUDA(b->d_work.alloc(std::max<size_t>(all.size(), 1)));
-  GB_B_CUDA(b->d_halts.alloc(n + 1));
+  GB_B_CUDA(b->d_eval.alloc_on(b->stream, n));
+  GB_B_CUDA(b->d_step.alloc_on(b->stream, n));
+  GB_B_CUDA(b->d_clear.alloc_on(b->stream, n));
+  GB_B_CUDA(b->d_work.alloc_on(b->stream, std::max<size_t>(all.size(), 1)));
+  GB_B_CUDA(b->d_halts.alloc_on(b->stream, n + 1));
   if (b->h_halts_cap < n + 1) {
     if (b->h_halts) cudaFreeHost(b->h_halts);
     b->h_halts = nullptr;
@@ -383,6 +383,12 @@ extern "C" int gb_batch_destroy(gb_batch* b) {
   cudaSetDevice(b->ctx->device);
   cudaStreamSynchronize(b->stream);
   b->drop_graph();
+  b->d_eval.reset();  // stream-ordered frees, before the stream goes
+  b->d_step.reset();
+  b->d_clear.reset();
+  b->d_work.reset();
+  b->d_halts.reset();
+  cudaStreamSynchronize(b->stream);
   for (cudaEvent_t e : b->ev)
     if (e) cudaEventDestroy(e);
   if (b->h_halts) cudaFreeHost(b->h_halts);

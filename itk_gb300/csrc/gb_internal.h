@@ -27,17 +27,26 @@ struct Geom {
 
 int geom_init(Geom& g, const int64_t size[3], const double spacing[3], const double origin[3], const double dir[9]);
 
-// Owning device buffer (cudaMalloc / cudaFree).
+// Owning device buffer from the stream-ordered allocator: allocated and freed
+// in the order of the stream it is bound to, so growing or dropping a buffer
+// never waits for the whole device (a plain cudaFree does, stalling every other
+// stream -- other registrations' iterations included).  Without a stream:
+// cudaMalloc / cudaFree.
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t st = nullptr;
+  bool ordered = false;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { reset(); }
   void reset() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (ordered) cudaFreeAsync(p, st);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
   }
@@ -45,8 +54,21 @@ struct DevBuf {
   cudaError_t alloc(size_t count) {
     if (count <= n && p) return cudaSuccess;
     reset();
+    ordered = false;
     if (count == 0) return cudaSuccess;
     cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    else p = nullptr;
+    return e;
+  }
+  // stream-ordered: usable on `stream` at once, on other streams once `stream` has been synchronized
+  cudaError_t alloc_on(cudaStream_t stream, size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    reset();
+    st = stream;
+    ordered = true;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(T), stream);
     if (e == cudaSuccess) n = count;
     else p = nullptr;
     return e;
@@ -157,6 +179,8 @@ struct gb_metric {
   bool opt_graphs = true;           // capture each iteration in a CUDA graph
 
   size_t device_bytes() const;  // all device buffers of the handle (gb_metric.cu)
+  void release_buffers();       // frees them in the handle's stream order (gb_metric.cu)
+  size_t h_cap = 0;             // doubles held by h_params and h_out (pinned, reused across levels)
 
   // per-kernel event timing (gb_metric_set_profiling)
   bool profiling = false;

@@ -153,6 +153,13 @@ extern "C" int gb_ctx_create(int device, gb_ctx** out) {
   GB_CUDA(cudaSetDevice(device));
   int sms = 0;
   GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  // this process's stream-ordered pool keeps freed blocks for the next level's
+  // buffers instead of returning them to the driver at every synchronization
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   gb_ctx* c = new gb_ctx;
   c->device = device;
   c->sm_count = sms;
@@ -196,9 +203,19 @@ extern "C" int gb_metric_create(gb_ctx* ctx, int kind, gb_metric** out) {
   return GB_OK;
 }
 
+void gb_metric::release_buffers() {
+  d_fixed.reset(); d_moving.reset(); d_fixed_s.reset(); d_moving_s.reset(); d_grad_in.reset();
+  d_mov4.reset(); d_samples.reset(); d_cache.reset(); d_sup.reset(); d_chunks.reset();
+  d_node_first.reset(); d_node_entries.reset(); d_chunk_part.reset(); d_nodes.reset(); d_params.reset();
+  d_acc.reset(); d_scratch.reset(); d_out.reset(); d_status.reset(); d_pratio.reset(); d_pdf.reset();
+  d_consts.reset(); d_opt.reset(); d_opt_vec.reset();
+}
+
 extern "C" int gb_metric_destroy(gb_metric* m) {
   if (!m) return GB_OK;
   cudaSetDevice(m->ctx->device);
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  m->release_buffers();  // stream-ordered frees, before the stream goes
   if (m->stream) cudaStreamSynchronize(m->stream);
   if (m->h_params) cudaFreeHost(m->h_params);
   if (m->h_out) cudaFreeHost(m->h_out);
@@ -234,7 +251,7 @@ static int set_image_common(gb_metric* m, int which, const float* src, bool devi
   DevBuf<float>& buf = which == GB_IMAGE_FIXED ? m->d_fixed : m->d_moving;
   const size_t n = (size_t)g.voxels();
   buf.reset();
-  GB_CUDA(buf.alloc(n));
+  GB_CUDA(buf.alloc_on(m->stream, n));
   GB_CUDA(cudaMemcpyAsync(buf.p, src, n * sizeof(float), device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                           m->stream));
   GB_CUDA(cudaStreamSynchronize(m->stream));
@@ -271,7 +288,7 @@ extern "C" int gb_metric_set_moving_gradient_image(gb_metric* m, const double* g
   GB_CUDA(cudaSetDevice(m->ctx->device));
   const size_t n = (size_t)m->moving.voxels() * 3;
   m->d_grad_in.reset();
-  GB_CUDA(m->d_grad_in.alloc(n));
+  GB_CUDA(m->d_grad_in.alloc_on(m->stream, n));
   GB_CUDA(cudaMemcpyAsync(m->d_grad_in.p, gradient_xyz, n * sizeof(double), cudaMemcpyHostToDevice, m->stream));
   GB_CUDA(cudaStreamSynchronize(m->stream));
   m->grad_set = true;
@@ -436,8 +453,8 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
       for (int i = 0; i < 3; ++i) sig[i] = m->level_sigma_physical ? m->level_sigma : m->level_sigma * g.spacing[i];
       const int64_t nv = g.voxels();
       DevBuf<float> tmp;
-      GB_CUDA(dst.alloc(nv));
-      GB_CUDA(tmp.alloc(2 * (size_t)nv));
+      GB_CUDA(dst.alloc_on(m->stream, nv));
+      GB_CUDA(tmp.alloc_on(m->stream, 2 * (size_t)nv));
       const int rc = smooth_rg_device(st, src, dst.p, tmp.p, tmp.p + nv, g.size, g.spacing, sig);
       if (rc) return rc;
       GB_CUDA(cudaStreamSynchronize(st));  // tmp is released at the end of this scope
@@ -467,7 +484,7 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
 
   DevBuf<float> d_pts;
   if (sampled) {
-    GB_CUDA(d_pts.alloc(m->h_points.size()));
+    GB_CUDA(d_pts.alloc_on(m->stream, m->h_points.size()));
     GB_CUDA(cudaMemcpyAsync(d_pts.p, m->h_points.data(), m->h_points.size() * sizeof(float), cudaMemcpyHostToDevice, st));
   }
 
@@ -475,7 +492,7 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   const DGeom dfixed = to_dgeom(m->fixed), dvirt = to_dgeom(m->virt);
   if (m->kind == GB_METRIC_MATTES) {
     DevBuf<int> d_mm;
-    GB_CUDA(d_mm.alloc(4));
+    GB_CUDA(d_mm.alloc_on(m->stream, 4));
     int init[4] = {float_to_ordered_host(FLT_MAX), float_to_ordered_host(-FLT_MAX), float_to_ordered_host(FLT_MAX),
                    float_to_ordered_host(-FLT_MAX)};
     GB_CUDA(cudaMemcpyAsync(d_mm.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
@@ -526,12 +543,12 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   DevBuf<uint32_t> vals, vals_sorted;
   DevBuf<float4> recs;
   DevBuf<unsigned long long> d_nvalid;
-  GB_CUDA(keys.alloc(ncand));
-  GB_CUDA(keys_sorted.alloc(ncand));
-  GB_CUDA(vals.alloc(ncand));
-  GB_CUDA(vals_sorted.alloc(ncand));
-  GB_CUDA(recs.alloc(ncand));
-  GB_CUDA(d_nvalid.alloc(1));
+  GB_CUDA(keys.alloc_on(m->stream, ncand));
+  GB_CUDA(keys_sorted.alloc_on(m->stream, ncand));
+  GB_CUDA(vals.alloc_on(m->stream, ncand));
+  GB_CUDA(vals_sorted.alloc_on(m->stream, ncand));
+  GB_CUDA(recs.alloc_on(m->stream, ncand));
+  GB_CUDA(d_nvalid.alloc_on(m->stream, 1));
   GB_CUDA(cudaMemsetAsync(d_nvalid.p, 0, sizeof(unsigned long long), st));
   BuildArgs b{};
   b.points = sampled ? d_pts.p : nullptr;
@@ -547,7 +564,7 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   b.bspline = bspline ? 1 : 0;
   DevBuf<float4> sup;
   if (bspline) {
-    GB_CUDA(sup.alloc(ncand));
+    GB_CUDA(sup.alloc_on(m->stream, ncand));
     for (int i = 0; i < 3; ++i) {
       b.grid[i] = m->grid[i];
       b.g_origin[i] = m->tfixed[3 + i];
@@ -567,9 +584,9 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   GB_CUDA(cudaStreamSynchronize(st));
   m->nsamples = (int64_t)nvalid;
   m->d_samples.reset();
-  GB_CUDA(m->d_samples.alloc(std::max<int64_t>(1, m->nsamples)));
+  GB_CUDA(m->d_samples.alloc_on(m->stream, std::max<int64_t>(1, m->nsamples)));
   m->d_sup.reset();
-  if (bspline) GB_CUDA(m->d_sup.alloc(std::max<int64_t>(1, m->nsamples)));
+  if (bspline) GB_CUDA(m->d_sup.alloc_on(m->stream, std::max<int64_t>(1, m->nsamples)));
   if (m->nsamples > 0)
     k_gather_samples<<<(unsigned)((m->nsamples + kBlock - 1) / kBlock), kBlock, 0, st>>>(
         vals_sorted.p, m->nsamples, recs.p, m->d_samples.p, bspline ? sup.p : nullptr,
@@ -622,10 +639,10 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     m->d_node_first.reset();
     m->d_node_entries.reset();
     m->d_chunk_part.reset();
-    GB_CUDA(m->d_chunks.alloc(std::max<size_t>(1, chunks.size())));
-    GB_CUDA(m->d_node_first.alloc(node_first.size()));
-    GB_CUDA(m->d_node_entries.alloc(std::max<size_t>(1, entries.size())));
-    GB_CUDA(m->d_chunk_part.alloc(std::max<size_t>(1, chunks.size()) * 192));
+    GB_CUDA(m->d_chunks.alloc_on(m->stream, std::max<size_t>(1, chunks.size())));
+    GB_CUDA(m->d_node_first.alloc_on(m->stream, node_first.size()));
+    GB_CUDA(m->d_node_entries.alloc_on(m->stream, std::max<size_t>(1, entries.size())));
+    GB_CUDA(m->d_chunk_part.alloc_on(m->stream, std::max<size_t>(1, chunks.size()) * 192));
     if (!chunks.empty())
       GB_CUDA(cudaMemcpyAsync(m->d_chunks.p, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, st));
     GB_CUDA(cudaMemcpyAsync(m->d_node_first.p, node_first.data(), sizeof(int) * node_first.size(),
@@ -634,7 +651,7 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
       GB_CUDA(cudaMemcpyAsync(m->d_node_entries.p, entries.data(), sizeof(int) * entries.size(),
                               cudaMemcpyHostToDevice, st));
     m->d_nodes.reset();
-    GB_CUDA(m->d_nodes.alloc((size_t)m->nper));
+    GB_CUDA(m->d_nodes.alloc_on(m->stream, (size_t)m->nper));
     GB_CUDA(cudaStreamSynchronize(st));  // the host vectors die here
   }
 
@@ -642,7 +659,7 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   if (m->grad_source == GB_GRADIENT_IMAGE) {
     const int64_t nv = m->moving.voxels();
     m->d_mov4.reset();
-    GB_CUDA(m->d_mov4.alloc(nv));
+    GB_CUDA(m->d_mov4.alloc_on(m->stream, nv));
     k_pack_moving<<<(unsigned)((nv + kBlock - 1) / kBlock), kBlock, 0, st>>>(m->moving_img(), m->d_grad_in.p, nv,
                                                                               m->d_mov4.p);
     GB_CUDA(cudaGetLastError());
@@ -651,7 +668,7 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     // scale, image direction applied (itkImageToImageMetricv4.hxx:488-503)
     const int64_t nv = m->moving.voxels();
     m->d_mov4.reset();
-    GB_CUDA(m->d_mov4.alloc(nv));
+    GB_CUDA(m->d_mov4.alloc_on(m->stream, nv));
     const double sigma = std::max(m->moving.spacing[0], std::max(m->moving.spacing[1], m->moving.spacing[2]));
     const int rc = gradient_rg_device(st, m->moving_img(), m->moving.size, m->moving.spacing, m->moving.dir, sigma,
                                       true, true, m->d_mov4.p, nullptr);
@@ -662,28 +679,32 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   const size_t P = m->tparams.size();
   m->acc_bytes = acc_layout_bytes(m);
   m->d_acc.reset();
-  GB_CUDA(m->d_acc.alloc(m->acc_bytes));
-  GB_CUDA(m->d_scratch.alloc(kScratchDoubles));
-  GB_CUDA(m->d_params.alloc(P));
+  GB_CUDA(m->d_acc.alloc_on(m->stream, m->acc_bytes));
+  GB_CUDA(m->d_scratch.alloc_on(m->stream, kScratchDoubles));
+  GB_CUDA(m->d_params.alloc_on(m->stream, P));
   m->d_out.reset();
-  GB_CUDA(m->d_out.alloc(2 + P));
-  GB_CUDA(m->d_status.alloc(1));
+  GB_CUDA(m->d_out.alloc_on(m->stream, 2 + P));
+  GB_CUDA(m->d_status.alloc_on(m->stream, 1));
   if (m->kind == GB_METRIC_MATTES) {
     m->d_pratio.reset();
-    GB_CUDA(m->d_pratio.alloc((size_t)(m->bins * m->bins)));
+    GB_CUDA(m->d_pratio.alloc_on(m->stream, (size_t)(m->bins * m->bins)));
     m->d_pdf.reset();
-    GB_CUDA(m->d_pdf.alloc((size_t)(m->bins * m->bins)));
+    GB_CUDA(m->d_pdf.alloc_on(m->stream, (size_t)(m->bins * m->bins)));
     GB_CUDA(cudaMemsetAsync(m->d_pdf.p, 0, sizeof(double) * m->bins * m->bins, st));
   }
   m->d_cache.reset();
-  if (m->kind == GB_METRIC_MATTES || bspline) GB_CUDA(m->d_cache.alloc(std::max<int64_t>(1, m->nsamples)));
-  if (m->h_params) cudaFreeHost(m->h_params);
-  if (m->h_out) cudaFreeHost(m->h_out);
-  m->h_params = nullptr;
-  m->h_out = nullptr;
-  GB_CUDA(cudaMallocHost(&m->h_params, sizeof(double) * std::max<size_t>(P, 1)));
-  GB_CUDA(cudaMallocHost(&m->h_out, sizeof(double) * (2 + P)));
-  GB_CUDA(m->d_consts.alloc(1));
+  if (m->kind == GB_METRIC_MATTES || bspline) GB_CUDA(m->d_cache.alloc_on(m->stream, std::max<int64_t>(1, m->nsamples)));
+  if (m->h_cap < 2 + P) {  // pinned staging, reused while large enough (cudaFreeHost waits for the device)
+    if (m->h_params) cudaFreeHost(m->h_params);
+    if (m->h_out) cudaFreeHost(m->h_out);
+    m->h_params = nullptr;
+    m->h_out = nullptr;
+    m->h_cap = 0;
+    GB_CUDA(cudaMallocHost(&m->h_params, sizeof(double) * (2 + P)));
+    GB_CUDA(cudaMallocHost(&m->h_out, sizeof(double) * (2 + P)));
+    m->h_cap = 2 + P;
+  }
+  GB_CUDA(m->d_consts.alloc_on(m->stream, 1));
   if (!m->h_consts) GB_CUDA(cudaMallocHost(&m->h_consts, sizeof(EvalConsts)));
   if (bspline) {
     // the B-spline paths' constants depend only on the fixed initial affine: once, here

@@ -202,8 +202,8 @@ int opt_setup(gb_metric* m, const gb_regular_step_settings* cfg, const double* s
   }
   GB_OPT_CUDA(cudaSetDevice(m->ctx->device));
   cudaStream_t st = m->stream;
-  GB_OPT_CUDA(m->d_opt.alloc(sizeof(OptState)));
-  GB_OPT_CUDA(m->d_opt_vec.alloc((size_t)(4 * P)));
+  GB_OPT_CUDA(m->d_opt.alloc_on(st, sizeof(OptState)));
+  GB_OPT_CUDA(m->d_opt_vec.alloc_on(st, (size_t)(4 * P)));
   if (!m->h_opt) GB_OPT_CUDA(cudaMallocHost(&m->h_opt, sizeof(OptState)));
   if (!m->h_halt) GB_OPT_CUDA(cudaMallocHost(&m->h_halt, 2 * sizeof(int)));
   OptState* S = reinterpret_cast<OptState*>(m->d_opt.p);

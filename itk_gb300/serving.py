@@ -111,7 +111,7 @@ class RegistrationServer:
 
     def __init__(self, hbm_budget_bytes: float = 120e9, max_active: int = 64, iterations_per_tick: int = 8,
                  samples_per_block=(8192, 8192, 8192), device: int = 0, clock=time.perf_counter,
-                 setup_threads: int = 2):
+                 setup_threads: int = 4):
         self.budget = float(hbm_budget_bytes)
         self.max_active = int(max_active)
         self.k = int(iterations_per_tick)
