@@ -472,15 +472,14 @@ def run_gb300(args):
     ktime = float(ktimes[kidx])
     peak, peak_src = measured_peak()
     achieved = kbytes / (ktime / 1e3) / 1e9
-    traffic = None
+    traffic = None  # measured DRAM bytes of this kernel on this workload (profiles/traffic.txt), if captured
     tf = os.path.join(ROOT, "profiles", "traffic.txt")
-    default_size = "192,192,160" if bs else "256,256,200"
-    default_fraction = 0.1 if bs else 0.2
-    if os.path.exists(tf) and args.size == default_size and abs(args.fraction - default_fraction) < 1e-9:
+    wkey = config_dict(args, n)["workload"]
+    if os.path.exists(tf):
         for line in open(tf):
             parts = line.split()
-            if len(parts) == 2 and parts[0] == kname:
-                traffic = int(parts[1])
+            if len(parts) == 3 and parts[0] == wkey and parts[1] == kname:
+                traffic = int(parts[2])
     b_alg = roofline.evaluation_bytes(n, v_touched, nparams=P)
     eval_ms = dev_ms / args.steps
     line = {

@@ -23,7 +23,7 @@
 namespace gb {
 
 constexpr int kChunkLen = 256;     // samples per chunk (at most); also the chunk kernel's block size
-constexpr int kParamsBlock = 256;  // 8 parameters per block in k_bspline_params
+constexpr int kParamsBlock = 256;  // k_bspline_params: 8 nodes per block (warp form) or 1 (block form)
 
 __device__ __forceinline__ void unpack_support(float w, int& sx, int& sy, int& sz, bool& valid) {
   const unsigned u = __float_as_uint(w);
@@ -329,16 +329,18 @@ __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
   griddep_launch_dependents();
 }
 
-// One warp per node n: for its three parameters (n + d * nper), the sum of the
+// For each node n and its three parameters (n + d * nper): the sum of the
 // chunk sums of every cell whose 4x4x4 support holds n, listed at Initialize in
-// node_entries (chunk * 192 + support position).  Lane-strided over the list
-// with compensated FP32 (GB300's FP64 pipe is a small fraction of FP32), a
-// fixed XOR tree across lanes, FP64 only for the metric's scale (1/N for
-// MeanSquares, -1/(binsize N) for Mattes, MeanSquares...Threader.hxx:71-79,
-// Mattes...Threader.hxx:446-457).
-template <bool MATTES>
+// node_entries (chunk * 192 + support position).  Compensated FP32 over the
+// list, fixed XOR trees, FP64 only for the metric's scale (1/N for MeanSquares,
+// -1/(binsize N) for Mattes, MeanSquares...Threader.hxx:71-79,
+// Mattes...Threader.hxx:446-457).  BLOCK = false: one warp per node (lane-strided
+// list); BLOCK = true, for coarse grids whose nodes hold thousands of entries:
+// one block per node (thread-strided list, warps added in fixed order), so the
+// few hundred nodes still spread over every SM.
+template <bool MATTES, bool BLOCK>
 __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
-  const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n = BLOCK ? (int)blockIdx.x : (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   griddep_wait();
   if (halted(a)) return;
@@ -363,14 +365,39 @@ __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
   s0.zero();
   s1.zero();
   s2.zero();
+  const int first = BLOCK ? (int)threadIdx.x : lane;
+  const int step = BLOCK ? (int)blockDim.x : 32;
 #pragma unroll 4
-  for (int e = e0 + lane; e < e1; e += 32) {
+  for (int e = e0 + first; e < e1; e += step) {
     const float* src = a.chunk_part + __ldg(a.node_entries + e);
     s0.add(__ldcg(src));
     s1.add(__ldcg(src + 64));
     s2.add(__ldcg(src + 128));
   }
-  const float t0 = warp_sum(s0.value()), t1 = warp_sum(s1.value()), t2 = warp_sum(s2.value());
+  float t0 = warp_sum(s0.value()), t1 = warp_sum(s1.value()), t2 = warp_sum(s2.value());
+  if (BLOCK) {
+    __shared__ float wsum[kParamsBlock / 32][3];
+    const int w = threadIdx.x >> 5;
+    if (lane == 0) {
+      wsum[w][0] = t0;
+      wsum[w][1] = t1;
+      wsum[w][2] = t2;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    KahanF b0, b1, b2;
+    b0.zero();
+    b1.zero();
+    b2.zero();
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      b0.add(wsum[k][0]);
+      b1.add(wsum[k][1]);
+      b2.add(wsum[k][2]);
+    }
+    t0 = b0.value();
+    t1 = b1.value();
+    t2 = b2.value();
+  }
   if (lane == 0) {
     double scale = 0.0;
     if (st == GB_OK && N > 0) scale = MATTES ? -1.0 / (a.m_bs * (double)N) : 1.0 / (double)N;

@@ -150,6 +150,7 @@ struct gb_metric {
   gb::DevBuf<float> d_chunk_part;  // nchunks x 192 Jacobian partial sums
   gb::DevBuf<float4> d_nodes;    // B-spline coefficients as float4 nodes
   int64_t nchunks = 0;
+  int64_t node_entries_count = 0;  // (node, chunk) pairs: chooses the parameter gather's shape
   int grid[3] = {0, 0, 0};       // B-spline control grid
   double mstate[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 

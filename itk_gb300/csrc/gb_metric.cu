@@ -642,6 +642,7 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     GB_CUDA(m->d_chunks.alloc_on(m->stream, std::max<size_t>(1, chunks.size())));
     GB_CUDA(m->d_node_first.alloc_on(m->stream, node_first.size()));
     GB_CUDA(m->d_node_entries.alloc_on(m->stream, std::max<size_t>(1, entries.size())));
+    m->node_entries_count = (int64_t)entries.size();
     GB_CUDA(m->d_chunk_part.alloc_on(m->stream, std::max<size_t>(1, chunks.size()) * 192));
     if (!chunks.empty())
       GB_CUDA(cudaMemcpyAsync(m->d_chunks.p, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, st));
@@ -859,10 +860,17 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
                    : launch_chain(m, k_bspline_chunks<false>, (unsigned)cblocks, kChunkLen, 0, a));
     m->mark();
   }
-  const int64_t threads = (int64_t)nper * 32;  // one warp per node
-  const unsigned pblocks = (unsigned)((threads + kParamsBlock - 1) / kParamsBlock);
-  GB_CUDA(mattes ? launch_chain(m, k_bspline_params<true>, pblocks, kParamsBlock, 0, a)
-                 : launch_chain(m, k_bspline_params<false>, pblocks, kParamsBlock, 0, a));
+  // one warp per node, or one block per node when the nodes hold many chunk entries
+  const bool per_block = m->node_entries_count >= (int64_t)kParamsBlock * nper;
+  if (per_block) {
+    GB_CUDA(mattes ? launch_chain(m, k_bspline_params<true, true>, (unsigned)nper, kParamsBlock, 0, a)
+                   : launch_chain(m, k_bspline_params<false, true>, (unsigned)nper, kParamsBlock, 0, a));
+  } else {
+    const int64_t threads = (int64_t)nper * 32;
+    const unsigned pblocks = (unsigned)((threads + kParamsBlock - 1) / kParamsBlock);
+    GB_CUDA(mattes ? launch_chain(m, k_bspline_params<true, false>, pblocks, kParamsBlock, 0, a)
+                   : launch_chain(m, k_bspline_params<false, false>, pblocks, kParamsBlock, 0, a));
+  }
   m->mark();
   return GB_OK;
 }
