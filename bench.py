@@ -772,6 +772,11 @@ def run_served_form(args, inst):
                                   r.sampling_percentage, seed)
             plain_loop(m, T, r.iterations[lv], r.learning_rate, r.minimum_step_length, scales=r.scales)
         service.append(time.perf_counter() - t0)
+    # the Mattes MI requests alone: capacity of the server against the plain path
+    mi = [i for i, r in enumerate(reqs) if r.metric == "mattes"]
+    srv_mi = RegistrationServer(hbm_budget_bytes=120e9)
+    _, wall_mi = srv_mi.serve([reqs[i] for i in mi], [0.0] * len(mi))
+    cap_mi = {"served": len(mi) / wall_mi, "plain_per_call": len(mi) / float(sum(service[i] for i in mi))}
     done, plain_lat = 0.0, []
     for a, s in zip(arrivals, service):
         start = max(a, done)
@@ -789,6 +794,8 @@ def run_served_form(args, inst):
                       "plain_p50": float(np.percentile(plain_lat, 50)),
                       "plain_p99": float(np.percentile(plain_lat, 99))},
         "capacity_regs_per_s": {"served": capacity, "plain_per_call": len(reqs) / float(sum(service))},
+        "capacity_mattes_only_regs_per_s": cap_mi,
+        "speedup_capacity_mattes_only": cap_mi["served"] / cap_mi["plain_per_call"],
         "level_setups": {"count": srv.setups, "seconds_total": srv.setup_seconds,
                          "note": "image upload, device smoothing / shrink / gradient filter, host sample points, "
                                  "Initialize; on 4 host threads beside the batch"},

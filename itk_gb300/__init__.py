@@ -15,6 +15,7 @@ from .metrics import (ImageToImageMetricv4, MattesMutualInformationImageToImageM
 from .optimizers import RegularStepGradientDescentOptimizerv4
 from .registration import ImageRegistrationMethodv4, sample_count, sample_points
 from .serving import RegistrationRequest, RegistrationResult, RegistrationServer
+from .transformio import ReadTransform, WriteTransform
 from .transforms import AffineTransform, BSplineTransform, CompositeTransform
 
 __all__ = [
@@ -23,5 +24,5 @@ __all__ = [
     "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
     "RegistrationBatch", "RegistrationRequest", "RegistrationResult", "RegistrationServer",
     "RegularStepGradientDescentOptimizerv4", "ShrinkImageFilter", "SmoothingRecursiveGaussianImageFilter", "context",
-    "lib", "library_path", "sample_count", "sample_points", "shrink_geometry",
+    "ReadTransform", "WriteTransform", "lib", "library_path", "sample_count", "sample_points", "shrink_geometry",
 ]
