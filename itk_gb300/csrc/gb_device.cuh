@@ -289,6 +289,9 @@ __device__ __forceinline__ uint64_t morton_spread(uint64_t v) {
   v = (v | v << 2) & 0x1249249249249249ULL;
   return v;
 }
+// Sample sort keys: B-spline cell above this bit, spatial order below it.
+constexpr int kCellShift = 41;
+
 __device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
   return morton_spread(x) | (morton_spread(y) << 1) | (morton_spread(z) << 2);
 }

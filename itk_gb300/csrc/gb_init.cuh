@@ -209,7 +209,12 @@ __global__ void k_build_samples(BuildArgs b) {
     const uint32_t x = (uint32_t)(vi[0] < 0 ? 0 : vi[0]);
     const uint32_t y = (uint32_t)(vi[1] < 0 ? 0 : vi[1]);
     const uint32_t z = (uint32_t)(vi[2] < 0 ? 0 : vi[2]);
-    key = (morton3(x & 0xfff, y & 0xfff, z & 0xfff) & ((1ull << 36) - 1)) | (cell << 36);
+    // 8 x 2 x 2 bricks of the virtual grid in Morton order, scan order inside a
+    // brick: a warp's samples cover long x runs over few (y, z) rows, so the
+    // trilinear gathers of one load instruction touch few 128-byte lines
+    const uint64_t brick = morton3((x >> 3) & 0xfff, (y >> 1) & 0xfff, (z >> 1) & 0xfff) & ((1ull << 36) - 1);
+    key = (brick << 5) | ((uint64_t)(z & 1) << 4) | ((uint64_t)(y & 1) << 3) | (uint64_t)(x & 7) |
+          (cell << kCellShift);
     atomicAdd(b.nvalid, 1ull);
   }
   b.keys[i] = key;

@@ -604,9 +604,9 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     std::vector<int4> chunks;
     std::vector<int> cell_first((size_t)m->nper + 2, 0);
     for (int64_t i = 0; i < m->nsamples;) {
-      const uint64_t cell = hk[i] >> 36;
+      const uint64_t cell = hk[i] >> kCellShift;
       int64_t j = i + 1;
-      while (j < m->nsamples && (hk[j] >> 36) == cell && j - i < kChunkLen) ++j;
+      while (j < m->nsamples && (hk[j] >> kCellShift) == cell && j - i < kChunkLen) ++j;
       if (cell > 0) {
         chunks.push_back(make_int4((int)i, (int)j, (int)cell, 0));
         ++cell_first[cell + 1];
