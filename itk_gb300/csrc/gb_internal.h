@@ -179,6 +179,11 @@ struct gb_metric {
   int* h_halt = nullptr;            // pinned halt flags, one per batch slot
   bool opt_graphs = true;           // capture each iteration in a CUDA graph
 
+  // the host call's device work as CUDA graphs, [value only, with derivative]
+  cudaGraphExec_t host_exec[2] = {nullptr, nullptr};
+  bool host_graph_tried[2] = {false, false};
+  void drop_host_graphs();
+
   size_t device_bytes() const;  // all device buffers of the handle (gb_metric.cu)
   void release_buffers();       // frees them in the handle's stream order (gb_metric.cu)
   size_t h_cap = 0;             // doubles held by h_params and h_out (pinned, reused across levels)

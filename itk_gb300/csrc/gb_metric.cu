@@ -215,6 +215,7 @@ extern "C" int gb_metric_destroy(gb_metric* m) {
   if (!m) return GB_OK;
   cudaSetDevice(m->ctx->device);
   if (m->stream) cudaStreamSynchronize(m->stream);
+  m->drop_host_graphs();
   m->release_buffers();  // stream-ordered frees, before the stream goes
   if (m->stream) cudaStreamSynchronize(m->stream);
   if (m->h_params) cudaFreeHost(m->h_params);
@@ -419,6 +420,7 @@ static size_t acc_layout_bytes(const gb_metric* m) {
 
 extern "C" int gb_metric_initialize(gb_metric* m) {
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  m->drop_host_graphs();  // they hold this level's buffers and arguments
   if (!m->fixed.set) return fail(GB_ERR_BAD_ARG, "FixedImage is not present");
   if (!m->moving.set) return fail(GB_ERR_BAD_ARG, "MovingImage is not present");
   if (m->tkind < 0) return fail(GB_ERR_BAD_ARG, "MovingTransform is not present");
@@ -945,6 +947,61 @@ extern "C" int gb_metric_get_kernel_times(gb_metric* m, double* ms, int max_kern
   return GB_OK;
 }
 
+// The host call's device work: the constants (affine) or float4 nodes (B-spline)
+// up from pinned memory, the evaluation, value / derivative / status down into
+// pinned memory.
+static int host_chain(gb_metric* m, bool deriv) {
+  cudaStream_t st = m->stream;
+  const size_t P = m->tparams.size();
+  if (is_bspline(m))
+    GB_CUDA(cudaMemcpyAsync(m->d_nodes.p, m->h_params, sizeof(float4) * m->nper, cudaMemcpyHostToDevice, st));
+  else
+    GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
+  int rc = enqueue_eval(m, nullptr, m->d_out.p, deriv, false);
+  if (rc) return rc;
+  GB_CUDA(cudaMemcpyAsync(m->h_out, m->d_out.p, sizeof(double) * (2 + (deriv ? P : 0)), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(m->h_status, m->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  return GB_OK;
+}
+
+void gb_metric::drop_host_graphs() {
+  for (int k = 0; k < 2; ++k) {
+    if (host_exec[k]) cudaGraphExecDestroy(host_exec[k]);
+    host_exec[k] = nullptr;
+    host_graph_tried[k] = false;
+  }
+}
+
+// host_chain as one CUDA graph per form (value only / with derivative), captured on
+// the first call after Initialize: one launch per evaluation instead of about ten
+// API calls.  Direct launches when profiling (per-kernel events), when there is no
+// sample (that path stages its result from host memory), or if capture fails.
+static int run_host_chain(gb_metric* m, bool deriv) {
+  const int k = deriv ? 1 : 0;
+  if (m->profiling || m->nsamples == 0) return host_chain(m, deriv);
+  if (!m->host_exec[k] && !m->host_graph_tried[k]) {
+    m->host_graph_tried[k] = true;
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+    if (ok) {
+      const int rc = host_chain(m, deriv);
+      const cudaError_t e = cudaStreamEndCapture(m->stream, &g);
+      ok = rc == GB_OK && e == cudaSuccess && g != nullptr;
+      if (ok) ok = cudaGraphInstantiate(&m->host_exec[k], g, 0) == cudaSuccess;
+      if (g) cudaGraphDestroy(g);
+    }
+    if (!ok) {
+      (void)cudaGetLastError();  // a failed capture leaves no sticky error
+      m->host_exec[k] = nullptr;
+    }
+  }
+  if (m->host_exec[k]) {
+    GB_CUDA(cudaGraphLaunch(m->host_exec[k], m->stream));
+    return GB_OK;
+  }
+  return host_chain(m, deriv);
+}
+
 static int eval_host(gb_metric* m, double* value, double* derivative, int64_t nparams, bool deriv) {
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
@@ -952,7 +1009,6 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
   if (deriv && (size_t)nparams != P) return fail(GB_ERR_BAD_ARG, "derivative size must equal the number of parameters");
   GB_CUDA(cudaSetDevice(m->ctx->device));
   cudaStream_t st = m->stream;
-  const double* d_params = nullptr;
   if (is_bspline(m)) {
     // float4 coefficient nodes converted here (IEEE round to nearest, as the device
     // conversion of the device-resident call), staged in the pinned parameter buffer
@@ -960,18 +1016,14 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
     const int64_t np = m->nper;
     const double* c = m->tparams.data();
     for (int64_t n = 0; n < np; ++n) hn[n] = make_float4((float)c[n], (float)c[np + n], (float)c[2 * np + n], 0.f);
-    GB_CUDA(cudaMemcpyAsync(m->d_nodes.p, hn, sizeof(float4) * np, cudaMemcpyHostToDevice, st));
   } else {
     // per-evaluation constants in FP64 on the host, uploaded with the parameters
     const bool dense = !m->use_sampled;
     affine_consts(m->tparams.data(), m->tfixed.data(), m->moving.p2i, m->moving.origin, dense ? m->virt.i2p : nullptr,
                   m->virt.origin, *m->h_consts);
-    GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
   }
-  int rc = enqueue_eval(m, d_params, m->d_out.p, deriv, false);
+  int rc = run_host_chain(m, deriv);
   if (rc) return rc;
-  GB_CUDA(cudaMemcpyAsync(m->h_out, m->d_out.p, sizeof(double) * (2 + (deriv ? P : 0)), cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(m->h_status, m->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));
   const int status = *m->h_status;
   m->last_status = status;
