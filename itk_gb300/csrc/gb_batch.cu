@@ -99,43 +99,13 @@ __global__ void __launch_bounds__(kBlock, 4) k_batch_pass2(const EvalArgs* __res
   mattes_pass2_affine_body(sa, VGrid{w.y, w.z});
 }
 
-// AdvanceOneStep of one registration per block, then the NumberOfIterations stop
-// that the reference checks at the top of its next loop pass.
-__global__ void __launch_bounds__(kStepBlock) k_batch_step(const StepArgs* __restrict__ steps) {
+// AdvanceOneStep of one registration per block (step_block), one warp for the
+// 12 affine parameters.
+__global__ void __launch_bounds__(32) k_batch_step(const StepArgs* __restrict__ steps) {
   griddep_wait();
   const StepArgs s = steps[blockIdx.x];
-  OptState* S = s.st;
-  if (__ldcg(&S->halt)) return;
   griddep_launch_dependents();
-  const int status = __ldcg(s.status);
-  const bool err = metric_error(s, status);
-  DD q = {0.0, 0.0}, r = {0.0, 0.0};
-  if (!err)
-    for (long long j = threadIdx.x; j < s.P; j += blockDim.x) {
-      double qq, rr;
-      step_terms(s, j, qq, rr);
-      q = dd_add(q, DD{qq, 0.0});
-      r = dd_add(r, DD{rr, 0.0});
-    }
-  block_dd2(q, r);
-  __shared__ int act, fin_max;
-  if (threadIdx.x == 0) {
-    step_decide(s, S, status, q, r);
-    int fm = 0;
-    if (!S->halt && S->iteration >= s.max_iterations) {
-      S->stop = GB_STOP_MAXIMUM_NUMBER_OF_ITERATIONS;
-      S->halt = 1;
-      fm = 1;
-      if (s.return_best) S->value = S->best_value;
-    }
-    act = S->action;
-    fin_max = fm;
-  }
-  __syncthreads();
-  for (long long j = threadIdx.x; j < s.P; j += blockDim.x) {
-    step_apply(s, S, act, j);
-    if (fin_max && s.return_best) s.params[j] = __ldcg(s.best + j);
-  }
+  step_block<32>(s);
 }
 
 // out[r] = halt word of registration r; out[n] = the number still running.
@@ -252,7 +222,7 @@ int enqueue_iteration(gb_batch* b, bool step) {
                          regs, w + b->goff[kGrpP1CD]));
   if (b->gcnt[kGrpP2])
     GB_B_CUDA(launch_dep(st, k_batch_pass2, (unsigned)b->gcnt[kGrpP2], kBlock, b->smem2, regs, w + b->goff[kGrpP2]));
-  if (step) GB_B_CUDA(launch_dep(st, k_batch_step, n, kStepBlock, 0, (const StepArgs*)b->d_step.p));
+  if (step) GB_B_CUDA(launch_dep(st, k_batch_step, n, 32, 0, (const StepArgs*)b->d_step.p));
   return GB_OK;
 }
 

@@ -97,6 +97,14 @@ __global__ void __launch_bounds__(kStepBlock) k_step_apply(StepArgs s) {
   if (j < s.P) step_apply(s, S, act, j);
 }
 
+// The whole step of a registration with at most 32 parameters in one warp
+// (reduce, decide and apply in one launch).
+__global__ void __launch_bounds__(32) k_step_single(StepArgs s) {
+  griddep_wait();
+  griddep_launch_dependents();
+  step_block<32>(s);
+}
+
 // The loop ran out of iterations without another stop: MAXIMUM_NUMBER_OF_ITERATIONS.
 __global__ void __launch_bounds__(kStepBlock) k_opt_finish(StepArgs s) {
   griddep_wait();
@@ -137,10 +145,24 @@ static cudaError_t launch_dependent(cudaStream_t st, void (*kernel)(KArgs...), u
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
-// One optimizer iteration: the evaluation, then the step.
+// One optimizer iteration: the evaluation, then the step (one warp for at most 32
+// parameters, else the multi-block reduce and apply).
 static int enqueue_iteration(gb_metric* m, const StepArgs& a, unsigned blocks) {
   int rc = enqueue_eval(m, m->d_params.p, m->d_out.p, true, true);
   if (rc) return rc;
+  if (a.P <= 32) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(32);
+    cfg.stream = m->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GB_OPT_CUDA(cudaLaunchKernelEx(&cfg, k_step_single, a));
+    return GB_OK;
+  }
   GB_OPT_CUDA(launch_dependent(m->stream, k_step_reduce, blocks, a));
   GB_OPT_CUDA(launch_dependent(m->stream, k_step_apply, blocks, a));
   return GB_OK;

@@ -77,10 +77,10 @@ __device__ __forceinline__ DD dd_shfl_down(DD v, int off) {
   return {__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
 }
 
-// Sum over a block of kStepBlock threads in a fixed order (lane tree, then warp
-// tree); the result is in thread 0.
+// Sum over a block of NT threads (32 or kStepBlock) in a fixed order (lane tree,
+// then warp tree); the result is in thread 0.
+template <int NT = kStepBlock>
 __device__ __forceinline__ void block_dd2(DD& x, DD& y) {
-  __shared__ DD sx[kStepBlock / 32], sy[kStepBlock / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -90,13 +90,15 @@ __device__ __forceinline__ void block_dd2(DD& x, DD& y) {
       y = dd_add(y, oy);
     }
   }
+  if constexpr (NT == 32) return;
+  __shared__ DD sx[NT / 32], sy[NT / 32];
   if (lane == 0) {
     sx[w] = x;
     sy[w] = y;
   }
   __syncthreads();
   if (w == 0) {
-    constexpr int W = kStepBlock / 32;
+    constexpr int W = NT / 32;
     x = lane < W ? sx[lane] : DD{0.0, 0.0};
     y = lane < W ? sy[lane] : DD{0.0, 0.0};
 #pragma unroll
@@ -189,6 +191,44 @@ __device__ __forceinline__ void step_apply(const StepArgs& s, const OptState* S,
   const double p = __dadd_rn(s.params[j], __dmul_rn(glr, __ldcg(&S->inv_mag)));
   s.params[j] = p;
   if (__ldcg(&S->save_best)) s.best[j] = p;
+}
+
+// One registration's whole step in one block of NT threads: the compensated sums,
+// the decisions, the update, then the NumberOfIterations stop that the reference
+// checks at the top of its next loop pass (itkGradientDescentOptimizerv4.hxx:82-89).
+template <int NT>
+__device__ __forceinline__ void step_block(const StepArgs& s) {
+  OptState* S = s.st;
+  if (__ldcg(&S->halt)) return;
+  const int status = __ldcg(s.status);
+  const bool err = metric_error(s, status);
+  DD q = {0.0, 0.0}, r = {0.0, 0.0};
+  if (!err)
+    for (long long j = threadIdx.x; j < s.P; j += NT) {
+      double qq, rr;
+      step_terms(s, j, qq, rr);
+      q = dd_add(q, DD{qq, 0.0});
+      r = dd_add(r, DD{rr, 0.0});
+    }
+  block_dd2<NT>(q, r);
+  __shared__ int act, fin_max;
+  if (threadIdx.x == 0) {
+    step_decide(s, S, status, q, r);
+    int fm = 0;
+    if (!S->halt && S->iteration >= s.max_iterations) {
+      S->stop = GB_STOP_MAXIMUM_NUMBER_OF_ITERATIONS;
+      S->halt = 1;
+      fm = 1;
+      if (s.return_best) S->value = S->best_value;
+    }
+    act = S->action;
+    fin_max = fm;
+  }
+  __syncthreads();
+  for (long long j = threadIdx.x; j < s.P; j += NT) {
+    step_apply(s, S, act, j);
+    if (fin_max && s.return_best) s.params[j] = __ldcg(s.best + j);
+  }
 }
 
 // Host side (gb_optimizer.cu).  opt_setup: StartOptimization of one registration
