@@ -43,8 +43,9 @@ enum {
   GB_ERR_ADMISSION = 13
 };
 
-/* metric kinds */
-enum { GB_METRIC_MEAN_SQUARES = 0, GB_METRIC_MATTES = 1 };
+/* metric kinds; CORRELATION is CorrelationImageToImageMetricv4 (affine transforms)
+ * (Registration/Metricsv4/include/itkCorrelationImageToImageMetricv4.hxx) */
+enum { GB_METRIC_MEAN_SQUARES = 0, GB_METRIC_MATTES = 1, GB_METRIC_CORRELATION = 2 };
 /* image slots */
 enum { GB_IMAGE_FIXED = 0, GB_IMAGE_MOVING = 1 };
 /* moving transform kinds (flat encodings below) */

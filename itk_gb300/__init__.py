@@ -10,8 +10,8 @@ from .batch import RegistrationBatch
 from .filters import (GradientRecursiveGaussianImageFilter, ShrinkImageFilter, SmoothingRecursiveGaussianImageFilter,
                       shrink_geometry)
 from .image import GradientImage, Image
-from .metrics import (ImageToImageMetricv4, MattesMutualInformationImageToImageMetricv4,
-                      MeanSquaresImageToImageMetricv4, context)
+from .metrics import (CorrelationImageToImageMetricv4, ImageToImageMetricv4,
+                      MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4, context)
 from .optimizers import RegularStepGradientDescentOptimizerv4
 from .registration import ImageRegistrationMethodv4, sample_count, sample_points
 from .serving import RegistrationRequest, RegistrationResult, RegistrationServer
@@ -19,7 +19,8 @@ from .transformio import ReadTransform, WriteTransform
 from .transforms import AffineTransform, BSplineTransform, CompositeTransform
 
 __all__ = [
-    "AffineTransform", "BSplineTransform", "CompositeTransform", "ExceptionObject", "GradientImage",
+    "AffineTransform", "BSplineTransform", "CompositeTransform", "CorrelationImageToImageMetricv4", "ExceptionObject",
+    "GradientImage",
     "GradientRecursiveGaussianImageFilter", "Image", "ImageRegistrationMethodv4", "ImageToImageMetricv4",
     "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
     "RegistrationBatch", "RegistrationRequest", "RegistrationResult", "RegistrationServer",

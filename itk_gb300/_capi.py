@@ -31,6 +31,7 @@ GB_ERR_ADMISSION = 13
 
 GB_METRIC_MEAN_SQUARES = 0
 GB_METRIC_MATTES = 1
+GB_METRIC_CORRELATION = 2
 GB_IMAGE_FIXED = 0
 GB_IMAGE_MOVING = 1
 GB_TRANSFORM_AFFINE = 0

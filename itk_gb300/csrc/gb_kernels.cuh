@@ -413,6 +413,140 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Correlation, affine (CorrelationImageToImageMetricv4), two passes:
+//   pass A: the sums of the fixed and moving values over the valid points; its
+//     last block writes the averages (the helper threader,
+//     itkCorrelationImageToImageMetricv4HelperThreader.hxx:58-169);
+//   pass B: with f1 = f - avg_f, m1 = m - avg_m (the averages as double-float),
+//     fm, f2, m2 and fdm = sum f1 (J^T g), mdm = sum m1 (J^T g); the last block:
+//     value = -fm^2 / (f2 m2), derivative = 2 fm / (f2 m2) (fdm - fm / m2 mdm),
+//     0 when m2 f2 <= epsilon (...GetValueAndDerivativeThreader.hxx:62-130,270-325).
+constexpr int kCorrMaxBlocks = 1024;  // pass B's 27 partials per block fit the scratch
+
+template <int GRAD>
+__device__ __forceinline__ void corr_mean_body(const EvalArgs& a, VGrid vg) {
+  __shared__ EvalConsts K;
+  __shared__ float red[kBlock / 32][2];
+  __shared__ double blk[2], fin[2];
+  griddep_wait();
+  if (halted(a)) return;
+  griddep_launch_dependents();
+  load_consts(a.consts, K);
+  __syncthreads();
+  KahanF acc[2];
+  acc[0].zero();
+  acc[1].zero();
+  unsigned nv = 0;
+  const int64_t stride = (int64_t)vg.n * blockDim.x;
+  for (int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 s = __ldcs(a.samples + i);
+    float m;
+    float3 g;
+    if (!eval_moving<GRAD>(a, map_pos(K.map, s.x, s.y, s.z), false, m, g)) continue;
+    acc[0].add(s.w);
+    acc[1].add(m);
+    ++nv;
+  }
+  block_count(nv, a.acc_n);
+  block_sums<2>(acc, red, blk);
+  if (!grid_sums<2>(blk, a.part, a.grp, a.tickets + kTicketMain, fin, vg)) return;
+  if (threadIdx.x == 0) {
+    const unsigned long long N = __ldcg(a.acc_n);
+    a.marg[2] = N > 0 ? fin[0] / (double)N : 0.0;  // m_AverageFix
+    a.marg[3] = N > 0 ? fin[1] / (double)N : 0.0;  // m_AverageMov
+  }
+}
+
+template <int GRAD>
+__device__ __forceinline__ void corr_body(const EvalArgs& a, VGrid vg) {
+  __shared__ EvalConsts K;
+  __shared__ float red[kBlock / 32][27];
+  __shared__ double blk[27], fin[27];
+  griddep_wait();
+  if (halted(a)) return;
+  griddep_launch_dependents();
+  load_consts(a.consts, K);
+  float afh, afl, amh, aml;
+  split_df(__ldcg(&a.marg[2]), afh, afl);
+  split_df(__ldcg(&a.marg[3]), amh, aml);
+  __syncthreads();
+  KahanF acc[3];  // fm, f2, m2
+#pragma unroll
+  for (int k = 0; k < 3; ++k) acc[k].zero();
+  float d[24];  // fdm (12), mdm (12): plain FP32 per thread (a few samples each)
+#pragma unroll
+  for (int k = 0; k < 24; ++k) d[k] = 0.f;
+  const int64_t stride = (int64_t)vg.n * blockDim.x;
+  for (int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 s = __ldcs(a.samples + i);
+    float m;
+    float3 g;
+    if (!eval_moving<GRAD>(a, map_pos(K.map, s.x, s.y, s.z), a.with_derivative != 0, m, g)) continue;
+    const float f1 = __fsub_rn(__fsub_rn(s.w, afh), afl);
+    const float m1 = __fsub_rn(__fsub_rn(m, amh), aml);
+    acc[0].add(f1 * m1);
+    acc[1].add(f1 * f1);
+    acc[2].add(m1 * m1);
+    if (a.with_derivative) {
+      const float3 v = jac_vec(K, s.x, s.y, s.z);
+      const float gg[3] = {g.x, g.y, g.z}, vv[3] = {v.x, v.y, v.z};
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const float tf = f1 * gg[r], tm = m1 * gg[r];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          d[3 * r + c] = fmaf(tf, vv[c], d[3 * r + c]);
+          d[12 + 3 * r + c] = fmaf(tm, vv[c], d[12 + 3 * r + c]);
+        }
+        d[9 + r] += tf;
+        d[21 + r] += tm;
+      }
+    }
+  }
+  KahanF kacc[27];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) kacc[k] = acc[k];
+#pragma unroll
+  for (int k = 0; k < 24; ++k) {
+    kacc[3 + k].s = d[k];
+    kacc[3 + k].c = 0.f;
+  }
+  block_sums<27>(kacc, red, blk);
+  if (!grid_sums<27>(blk, a.part, a.grp, a.tickets + kTicketPass2, fin, vg)) return;
+  if (threadIdx.x == 0) {
+    const unsigned long long N = __ldcg(a.acc_n);
+    const int P = a.with_derivative ? a.nparams : 0;
+    a.out[1] = (double)N;
+    for (int p = 0; p < P; ++p) a.out[2 + p] = 0.0;
+    if (N == 0) {  // VerifyNumberOfValidPoints: a warning, value max
+      a.out[0] = DBL_MAX;
+      *a.status = GB_ERR_NO_VALID_POINTS;
+      return;
+    }
+    *a.status = GB_OK;
+    const double fm = fin[0], f2 = fin[1], m2 = fin[2];
+    const double m2f2 = m2 * f2;
+    if (m2f2 <= DBL_EPSILON) {
+      a.out[0] = 0.0;
+      return;
+    }
+    a.out[0] = -1.0 * fm * fm / m2f2;
+    const double sc = 2.0 * fm / (f2 * m2), r = fm / m2;
+    for (int p = 0; p < P; ++p) a.out[2 + p] = sc * (fin[3 + p] - r * fin[15 + p]);
+  }
+}
+
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock) k_corr_mean_affine(EvalArgs a) {
+  corr_mean_body<GRAD>(a, hw_grid());
+}
+
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock) k_corr_affine(EvalArgs a) {
+  corr_body<GRAD>(a, hw_grid());
+}
+
+// ---------------------------------------------------------------------------
 // Mattes pass 1, affine: joint histogram (Parzen: box on fixed, cubic B-spline
 // on moving), fixed marginal counts, moving marginal, valid count, per-sample
 // cache.  Histogram weights are 2^26 fixed point: integer adds are

@@ -188,7 +188,8 @@ extern "C" int gb_ctx_info(gb_ctx* ctx, int* sm_count, uint64_t* total_bytes, ui
 
 extern "C" int gb_metric_create(gb_ctx* ctx, int kind, gb_metric** out) {
   if (!ctx || !out) return fail(GB_ERR_BAD_ARG, "null argument");
-  if (kind != GB_METRIC_MEAN_SQUARES && kind != GB_METRIC_MATTES) return fail(GB_ERR_BAD_ARG, "unknown metric kind");
+  if (kind != GB_METRIC_MEAN_SQUARES && kind != GB_METRIC_MATTES && kind != GB_METRIC_CORRELATION)
+    return fail(GB_ERR_BAD_ARG, "unknown metric kind");
   GB_CUDA(cudaSetDevice(ctx->device));
   gb_metric* m = new gb_metric;
   m->ctx = ctx;
@@ -427,6 +428,8 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   if (m->grad_source == GB_GRADIENT_IMAGE && !m->grad_set)
     return fail(GB_ERR_BAD_ARG, "gradient source is a gradient image but none was set");
   const bool bspline = is_bspline(m);
+  if (bspline && m->kind == GB_METRIC_CORRELATION)
+    return fail(GB_ERR_UNSUPPORTED, "the correlation metric runs affine transforms");
   double g_p2i[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   if (bspline) {
     // BSplineTransform fixed parameters: grid size, origin, spacing, direction (itkBSplineTransform.hxx:243-283)
@@ -892,7 +895,7 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
     // no valid fixed sample at all: every point is invalid
     const int code = GB_ERR_NO_VALID_POINTS;
     GB_CUDA(cudaMemcpyAsync(m->d_status.p, &code, sizeof(int), cudaMemcpyHostToDevice, st));
-    const double v[2] = {m->kind == GB_METRIC_MEAN_SQUARES ? DBL_MAX : 0.0, 0.0};
+    const double v[2] = {m->kind != GB_METRIC_MATTES ? DBL_MAX : 0.0, 0.0};
     GB_CUDA(cudaMemcpyAsync(d_out, v, sizeof(v), cudaMemcpyHostToDevice, st));
     if (deriv && !m->tparams.empty()) GB_CUDA(cudaMemsetAsync(d_out + 2, 0, sizeof(double) * m->tparams.size(), st));
     return GB_OK;
@@ -901,6 +904,18 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
   m->nevents = 0;
   m->mark();
   if (is_bspline(m)) return enqueue_eval_bspline(m, a, cd, deriv, device_params);
+  if (m->kind == GB_METRIC_CORRELATION) {
+    // averages, then the value and derivative (at most kCorrMaxBlocks blocks: 27 partials each)
+    GB_CUDA(cd ? launch_wave(m, k_corr_mean_affine<kGradCentralDifference>, 0, a)
+               : launch_wave(m, k_corr_mean_affine<kGradImage>, 0, a));
+    m->mark();
+    const int grid = std::min(kCorrMaxBlocks, cd ? full_wave(m, k_corr_affine<kGradCentralDifference>, 0, m->nsamples)
+                                                 : full_wave(m, k_corr_affine<kGradImage>, 0, m->nsamples));
+    GB_CUDA(cd ? launch_chain(m, k_corr_affine<kGradCentralDifference>, (unsigned)grid, kBlock, 0, a)
+               : launch_chain(m, k_corr_affine<kGradImage>, (unsigned)grid, kBlock, 0, a));
+    m->mark();
+    return GB_OK;
+  }
   if (m->kind == GB_METRIC_MEAN_SQUARES) {
     GB_CUDA(cd ? launch_wave(m, k_msq_affine<kGradCentralDifference>, 0, a)
                : launch_wave(m, k_msq_affine<kGradImage>, 0, a));

@@ -266,7 +266,7 @@ int opt_setup(gb_metric* m, const gb_regular_step_settings* cfg, const double* s
   a.min_step = cfg->minimum_step_length;
   a.grad_tol = cfg->gradient_magnitude_tolerance;
   a.return_best = cfg->return_best_parameters_and_value ? 1 : 0;
-  a.msq = m->kind == GB_METRIC_MEAN_SQUARES ? 1 : 0;
+  a.msq = m->kind != GB_METRIC_MATTES ? 1 : 0;  // MeanSquares, Correlation: no valid point is a warning
   return GB_OK;
 }
 

@@ -56,7 +56,7 @@ struct StepArgs {
   long long max_iterations;  // NumberOfIterations (checked in-kernel by the batched step)
   double learning_rate, relaxation_factor, min_step, grad_tol;
   int return_best;
-  int msq;  // MeanSquares: no valid points is a warning (value max, derivative 0), not an error
+  int msq;  // MeanSquares / Correlation: no valid points is a warning (value max, derivative 0), not an error
 };
 
 // Compensated pair: the sum is hi + lo, |lo| <= ulp(hi) / 2.

@@ -182,7 +182,7 @@ class ImageToImageMetricv4:
     def _handle_status(self, rc):
         if rc == _capi.GB_OK:
             return
-        if rc == _capi.GB_ERR_NO_VALID_POINTS and self._kind == _capi.GB_METRIC_MEAN_SQUARES:
+        if rc == _capi.GB_ERR_NO_VALID_POINTS and self._kind != _capi.GB_METRIC_MATTES:
             warnings.warn(_capi.last_error())
             return
         raise ExceptionObject(rc, _capi.last_error())
@@ -265,6 +265,14 @@ class MeanSquaresImageToImageMetricv4(ImageToImageMetricv4):
     """Mean of squared intensity differences; derivative 2 (f - m) J^T grad m / N."""
 
     _kind = _capi.GB_METRIC_MEAN_SQUARES
+
+
+class CorrelationImageToImageMetricv4(ImageToImageMetricv4):
+    """Normalized cross correlation: value -(sum f1 m1)^2 / (sum f1^2 sum m1^2) with
+    f1, m1 the intensities less their averages over the valid points (affine
+    transforms)."""
+
+    _kind = _capi.GB_METRIC_CORRELATION
 
 
 class MattesMutualInformationImageToImageMetricv4(ImageToImageMetricv4):

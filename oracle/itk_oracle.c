@@ -700,6 +700,169 @@ int orc_msq_value_derivative(const orc_inputs *in, const orc_transform *t, int c
 }
 
 /* ------------------------------------------------------------------ */
+/* Correlation (normalized cross correlation)                          */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+  const orc_inputs *in;
+  const orc_transform *t;
+  int compute_derivative;
+  int64_t begin, end;
+  double avg_f, avg_m;         /* helper pass: inputs of the main pass */
+  double fix_sum, mov_sum;     /* helper pass: outputs */
+  double f, m, f2, m2, fm;     /* main pass */
+  uint64_t nvalid;
+  int64_t nparams;
+  double *fdm, *mdm;
+} corr_job;
+
+/* CorrelationImageToImageMetricv4HelperThreader::ProcessVirtualPoint,
+ * itkCorrelationImageToImageMetricv4HelperThreader.hxx:104-169: sums of the
+ * fixed and moving values over the valid points */
+static void *corr_helper_worker(void *arg)
+{
+  corr_job *j = (corr_job *)arg;
+  point_eval pe;
+  for (int64_t i = j->begin; i < j->end; ++i) {
+    double vp[3];
+    domain_point(j->in, i, vp);
+    if (!evaluate_point(j->in, j->t, vp, 0, &pe)) continue;
+    j->fix_sum += pe.fixed_value;
+    j->mov_sum += pe.moving_value;
+    j->nvalid++;
+  }
+  return NULL;
+}
+
+/* CorrelationImageToImageMetricv4GetValueAndDerivativeThreader::ProcessPoint,
+ * itkCorrelationImageToImageMetricv4GetValueAndDerivativeThreader.hxx:270-325 */
+static void *corr_worker(void *arg)
+{
+  corr_job *j = (corr_job *)arg;
+  point_eval pe;
+  sparse_row row;
+  for (int64_t i = j->begin; i < j->end; ++i) {
+    double vp[3];
+    domain_point(j->in, i, vp);
+    if (!evaluate_point(j->in, j->t, vp, j->compute_derivative, &pe)) continue;
+    const double f1 = pe.fixed_value - j->avg_f;
+    const double m1 = pe.moving_value - j->avg_m;
+    j->f += f1;
+    j->m += m1;
+    j->f2 += f1 * f1;
+    j->m2 += m1 * m1;
+    j->fm += f1 * m1;
+    j->nvalid++;
+    if (!j->compute_derivative) continue;
+    /* one nonzero J(dim, par) per parameter for affine and B-spline rows, so the
+     * row entry is sum_dim g[dim] J(dim, par) */
+    jacobian_product(j->t, &pe, &row);
+    for (int e = 0; e < row.count; ++e) {
+      j->fdm[row.idx[e]] += f1 * row.val[e];
+      j->mdm[row.idx[e]] += m1 * row.val[e];
+    }
+  }
+  return NULL;
+}
+
+static int corr_run(corr_job *jobs, int T, void *(*fn)(void *))
+{
+  pthread_t *th = (pthread_t *)calloc((size_t)T, sizeof(pthread_t));
+  if (!th) return ORC_ERR_OOM;
+  for (int k = 0; k < T; ++k) pthread_create(&th[k], NULL, fn, &jobs[k]);
+  for (int k = 0; k < T; ++k) pthread_join(th[k], NULL);
+  free(th);
+  return ORC_OK;
+}
+
+/* CorrelationImageToImageMetricv4: InitializeForIteration's helper pass for the
+ * averages (itkCorrelationImageToImageMetricv4.hxx:69-116,
+ * ...HelperThreader.hxx:58-100), then the value and derivative
+ * (...GetValueAndDerivativeThreader.hxx:62-130):
+ *   value = -fm^2 / (f2 m2),  derivative = 2 fm / (f2 m2) (fdm - fm / m2 mdm),
+ * value 0 and a zero derivative when m2 f2 <= epsilon; no valid point: the
+ * MeanSquares-style warning (value DBL_MAX, zero derivative). */
+int orc_corr_value_derivative(const orc_inputs *in, const orc_transform *t, int compute_derivative, double *value,
+                              double *derivative, uint64_t *nvalid)
+{
+  const int64_t n = domain_size(in);
+  const int64_t P = orc_transform_nparams(t);
+  if (n < 1) return ORC_ERR_BAD_ARG;
+  const int T = resolve_threads(in->nthreads, n);
+  corr_job *jobs = (corr_job *)calloc((size_t)T, sizeof(corr_job));
+  if (!jobs) return ORC_ERR_OOM;
+  const int64_t chunk = (n + T - 1) / T;
+  int rc = ORC_OK;
+  for (int k = 0; k < T; ++k) {
+    jobs[k].in = in;
+    jobs[k].t = t;
+    jobs[k].compute_derivative = compute_derivative;
+    jobs[k].begin = k * chunk < n ? k * chunk : n;
+    jobs[k].end = (k + 1) * chunk < n ? (k + 1) * chunk : n;
+    jobs[k].nparams = P;
+    if (compute_derivative) {
+      jobs[k].fdm = (double *)calloc((size_t)P, sizeof(double));
+      jobs[k].mdm = (double *)calloc((size_t)P, sizeof(double));
+      if (!jobs[k].fdm || !jobs[k].mdm) rc = ORC_ERR_OOM;
+    }
+  }
+  if (rc == ORC_OK) rc = corr_run(jobs, T, corr_helper_worker);
+  if (compute_derivative)
+    for (int64_t p = 0; p < P; ++p) derivative[p] = 0.0;
+  *value = 0.0;
+  if (rc == ORC_OK) {
+    uint64_t nh = 0;
+    double sum_f = 0.0, sum_m = 0.0;
+    for (int k = 0; k < T; ++k) {
+      nh += jobs[k].nvalid;
+      sum_f += jobs[k].fix_sum;
+      sum_m += jobs[k].mov_sum;
+    }
+    const double avg_f = nh > 0 ? sum_f / (double)nh : 0.0;
+    const double avg_m = nh > 0 ? sum_m / (double)nh : 0.0;
+    for (int k = 0; k < T; ++k) {
+      jobs[k].avg_f = avg_f;
+      jobs[k].avg_m = avg_m;
+      jobs[k].nvalid = 0;
+    }
+    rc = corr_run(jobs, T, corr_worker);
+  }
+  if (rc == ORC_OK) {
+    uint64_t nv = 0;
+    for (int k = 0; k < T; ++k) nv += jobs[k].nvalid;
+    *nvalid = nv;
+    if (nv == 0) {
+      *value = DBL_MAX;
+      rc = ORC_ERR_NO_VALID_POINTS;
+    } else {
+      double fm = 0.0, f2 = 0.0, m2 = 0.0;
+      for (int k = 0; k < T; ++k) {
+        fm += jobs[k].fm;
+        m2 += jobs[k].m2;
+        f2 += jobs[k].f2;
+      }
+      const double m2f2 = m2 * f2;
+      if (m2f2 > DBL_EPSILON) {
+        *value = -1.0 * fm * fm / m2f2;
+        if (compute_derivative) {
+          for (int64_t p = 0; p < P; ++p) {
+            double fd = 0.0, md = 0.0;
+            for (int k = 0; k < T; ++k) {
+              fd += jobs[k].fdm[p];
+              md += jobs[k].mdm[p];
+            }
+            derivative[p] += 2.0 * fm / (f2 * m2) * (fd - fm / m2 * md);
+          }
+        }
+      }
+    }
+  }
+  for (int k = 0; k < T; ++k) { free(jobs[k].fdm); free(jobs[k].mdm); }
+  free(jobs);
+  return rc;
+}
+
+/* ------------------------------------------------------------------ */
 /* Mattes mutual information                                           */
 /* ------------------------------------------------------------------ */
 
@@ -1013,6 +1176,22 @@ int orc_msq_flat_v(const float *fixed, const int64_t fsize[3], const double fgeo
   rc = orc_transform_from_flat(&t, tkind, tparams, nparams, tfixed, nfixed);
   if (rc) return rc;
   return orc_msq_value_derivative(&in, &t, compute_derivative, value, derivative, nvalid);
+}
+
+int orc_corr_flat_v(const float *fixed, const int64_t fsize[3], const double fgeo[15], const float *moving,
+                    const int64_t msize[3], const double mgeo[15], const double *moving_grad, const float *points,
+                    int64_t npoints, int tkind, const double *tparams, int64_t nparams, const double *tfixed,
+                    int64_t nfixed, int nthreads, int compute_derivative, double *value, double *derivative,
+                    uint64_t *nvalid, const int64_t *vsize, const double *vgeo)
+{
+  orc_inputs in;
+  orc_transform t;
+  int rc = inputs_from_flat(&in, fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, nthreads,
+                            vsize, vgeo);
+  if (rc) return rc;
+  rc = orc_transform_from_flat(&t, tkind, tparams, nparams, tfixed, nfixed);
+  if (rc) return rc;
+  return orc_corr_value_derivative(&in, &t, compute_derivative, value, derivative, nvalid);
 }
 
 int orc_mattes_flat(const float *fixed, const int64_t fsize[3], const double fgeo[15], const float *moving,

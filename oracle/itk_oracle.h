@@ -27,6 +27,10 @@
  *       Core/Common/include/itkBSplineKernelFunction.h:152-175
  *       Core/Common/include/itkBSplineDerivativeKernelFunction.h:156-180
  *   - Kahan summation  Core/Common/include/itkCompensatedSummation.hxx:38-48
+ *   - Correlation metric
+ *       Registration/Metricsv4/include/itkCorrelationImageToImageMetricv4.hxx:69-116
+ *       Registration/Metricsv4/include/itkCorrelationImageToImageMetricv4HelperThreader.hxx:58-169
+ *       Registration/Metricsv4/include/itkCorrelationImageToImageMetricv4GetValueAndDerivativeThreader.hxx:62-325
  *
  * All arithmetic is double, as in the reference (TInternalComputationValueType
  * = double); interpolated pixel values are rounded to float where the
@@ -204,6 +208,17 @@ int orc_gradient_recursive_gaussian(const float *in, double *out, const int64_t 
 int orc_shrink_geometry(const int64_t size[3], const double spacing[3], const double origin[3],
                         const double direction[9], const int64_t factors[3], int64_t out_size[3],
                         double out_spacing[3], double out_origin[3]);
+
+/* CorrelationImageToImageMetricv4 (normalized cross correlation): averages over
+ * the valid points, then value -fm^2/(f2 m2) and its derivative; flat inputs as
+ * orc_msq_flat_v */
+int orc_corr_value_derivative(const orc_inputs *in, const orc_transform *t, int compute_derivative, double *value,
+                              double *derivative, uint64_t *nvalid);
+int orc_corr_flat_v(const float *fixed, const int64_t fsize[3], const double fgeo[15], const float *moving,
+                    const int64_t msize[3], const double mgeo[15], const double *moving_grad, const float *points,
+                    int64_t npoints, int tkind, const double *tparams, int64_t nparams, const double *tfixed,
+                    int64_t nfixed, int nthreads, int compute_derivative, double *value, double *derivative,
+                    uint64_t *nvalid, const int64_t *vsize, const double *vgeo);
 
 /* ---- metric sample points (itk_oracle_sampling.c) ---------------------- */
 /* MT19937 32-bit outputs after `skip` draws from a fresh seed */
