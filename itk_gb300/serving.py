@@ -127,6 +127,9 @@ class RegistrationServer:
         self.peak_bytes = 0
         self.setup_seconds = 0.0   # worker-thread time spent setting up levels
         self.setups = 0
+        self.upload_seconds = 0.0  # of which: metric creation and image upload (first level)
+        self.run_seconds = 0.0     # main thread: inside the batch's iterations
+        self.ticks = 0
         self._next = 0
 
     def __del__(self):
@@ -173,6 +176,7 @@ class RegistrationServer:
     def _setup_level_timed(self, job):
         r = job.req
         if job.metric is None:
+            t_up = time.perf_counter()
             m = MeanSquaresImageToImageMetricv4(self.device) if r.metric == "msq" else \
                 MattesMutualInformationImageToImageMetricv4(self.device)
             if r.metric != "msq":
@@ -184,6 +188,7 @@ class RegistrationServer:
             t.SetParameters(r.transform.GetParameters())
             m.SetMovingTransform(t)
             job.metric, job.transform = m, t
+            self.upload_seconds += time.perf_counter() - t_up
         lv = job.level
         shrink = r.shrink_factors[lv]
         shrink = np.full(3, int(shrink)) if np.ndim(shrink) == 0 else np.asarray(shrink)
@@ -251,7 +256,10 @@ class RegistrationServer:
         self._join_ready(block=not running)
         if not any(j.slot is not None for j in self.active.values()):
             return
+        t_run = time.perf_counter()
         self.batch.Run(self.k)
+        self.run_seconds += time.perf_counter() - t_run
+        self.ticks += 1
         for job in list(self.active.values()):
             if job.slot is not None and not self.batch.IsRunning(job.slot):
                 self._finish_level(job)
