@@ -146,10 +146,16 @@ class ImageRegistrationMethodv4:
         self._strategy = strategy
 
     def SetMetricSamplingPercentage(self, p: float):
-        self._percentages = [float(p)] * self._levels
+        self.SetMetricSamplingPercentagePerLevel([float(p)] * self._levels)
 
     def SetMetricSamplingPercentagePerLevel(self, ps):
-        self._percentages = [float(p) for p in ps]
+        """Every percentage must lie in (0, 1]
+        (RegistrationMethodsv4/include/itkImageRegistrationMethodv4.hxx:1266-1283)."""
+        ps = [float(p) for p in ps]
+        if ps != self._percentages:
+            if any(not (0.0 < p <= 1.0) for p in ps):
+                raise ExceptionObject(_capi.GB_ERR_BAD_ARG, "sampling percentage outside expected (0,1] range")
+            self._percentages = ps
 
     def MetricSamplingReinitializeSeed(self, seed=None):
         if seed is None:

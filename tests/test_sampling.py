@@ -93,3 +93,17 @@ def test_seed_sequence_over_levels():
     assert not np.array_equal(a, b)
     c, _ = sample_points(RANDOM, size, sp, org, np.eye(3), 0.1, 40)
     assert np.array_equal(a, c)
+
+
+def test_sampling_percentage_range():
+    # itkImageRegistrationSamplingTest: 0.1 is accepted; -0.1, 0 and 1.1 raise
+    from itk_gb300 import ExceptionObject, ImageRegistrationMethodv4
+    r = ImageRegistrationMethodv4()
+    r.SetMetricSamplingPercentage(0.1)
+    for bad in (-0.1, 0.0, 1.1):
+        with pytest.raises(ExceptionObject):
+            r.SetMetricSamplingPercentage(bad)
+    r.SetNumberOfLevels(3)
+    r.SetMetricSamplingPercentagePerLevel([0.2, 0.5, 1.0])
+    with pytest.raises(ExceptionObject):
+        r.SetMetricSamplingPercentagePerLevel([0.2, 1.5, 1.0])
