@@ -49,7 +49,7 @@ enum { GB_METRIC_MEAN_SQUARES = 0, GB_METRIC_MATTES = 1, GB_METRIC_CORRELATION =
 /* image slots */
 enum { GB_IMAGE_FIXED = 0, GB_IMAGE_MOVING = 1 };
 /* moving transform kinds (flat encodings below) */
-enum { GB_TRANSFORM_AFFINE = 0, GB_TRANSFORM_BSPLINE = 1, GB_TRANSFORM_COMPOSITE = 2 };
+enum { GB_TRANSFORM_AFFINE = 0, GB_TRANSFORM_BSPLINE = 1, GB_TRANSFORM_COMPOSITE = 2, GB_TRANSFORM_DISPLACEMENT_FIELD = 3 };
 /* moving-gradient source */
 enum {
   GB_GRADIENT_IMAGE = 0,              /* caller-supplied gradient image (filter output) */
@@ -145,7 +145,17 @@ int gb_metric_use_sampled_point_set(gb_metric *m, int on);
  *   COMPOSITE params = 3*nper B-spline coefficients (optimized), fixed = 18
  *             B-spline fixed parameters + 12 initial-affine parameters + 3
  *             initial-affine centre -- CompositeTransform [affine, bspline]
- *             with only the B-spline optimized, Core/Transform/include/itkCompositeTransform.hxx:60-70,466-580 */
+ *             with only the B-spline optimized, Core/Transform/include/itkCompositeTransform.hxx:60-70,466-580
+ *   DISPLACEMENT_FIELD params = 3 per field voxel (x, y, z; voxels x fastest),
+ *             fixed = 18 (field size, origin, spacing, direction) --
+ *             DisplacementFieldTransform<double,3>,
+ *             Filtering/DisplacementField/include/itkDisplacementFieldTransform.hxx:67-100,520-570.
+ *             Local support: Initialize requires the field to share the virtual
+ *             domain's grid (Numerics/Optimizersv4/include/itkObjectToObjectMetric.hxx:444-503);
+ *             the derivative is a field too, each point's block added at its
+ *             virtual voxel and not divided by the number of valid points
+ *             (Registration/Metricsv4/include/itkImageToImageMetricv4GetValueAndDerivativeThreaderBase.hxx:128-172,276-327).
+ *             MeanSquares and Mattes only. */
 int gb_metric_set_moving_transform(gb_metric *m, int kind, const double *params, int64_t nparams,
                                    const double *fixed, int64_t nfixed);
 /* SetParameters of the optimized transform (per optimizer iteration). */

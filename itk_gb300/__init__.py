@@ -2,25 +2,26 @@
 
 GetValueAndDerivative of MeanSquaresImageToImageMetricv4 and
 MattesMutualInformationImageToImageMetricv4 on Image<float,3> under affine,
-B-spline and [affine, B-spline] composite transforms, computed by hand-written
+B-spline, [affine, B-spline] composite and displacement-field transforms (and
+CorrelationImageToImageMetricv4 under affine transforms), computed by hand-written
 sm_103a CUDA kernels behind the C ABI in include/itk_gb300.h.
 """
 from ._capi import ExceptionObject, lib, library_path
 from .batch import RegistrationBatch
 from .filters import (GradientRecursiveGaussianImageFilter, ShrinkImageFilter, SmoothingRecursiveGaussianImageFilter,
                       shrink_geometry)
-from .image import GradientImage, Image
+from .image import DisplacementFieldImage, GradientImage, Image
 from .metrics import (CorrelationImageToImageMetricv4, ImageToImageMetricv4,
                       MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4, context)
 from .optimizers import RegularStepGradientDescentOptimizerv4
 from .registration import ImageRegistrationMethodv4, sample_count, sample_points
 from .serving import RegistrationRequest, RegistrationResult, RegistrationServer
 from .transformio import ReadTransform, WriteTransform
-from .transforms import AffineTransform, BSplineTransform, CompositeTransform
+from .transforms import AffineTransform, BSplineTransform, CompositeTransform, DisplacementFieldTransform
 
 __all__ = [
     "AffineTransform", "BSplineTransform", "CompositeTransform", "CorrelationImageToImageMetricv4", "ExceptionObject",
-    "GradientImage",
+    "DisplacementFieldImage", "DisplacementFieldTransform", "GradientImage",
     "GradientRecursiveGaussianImageFilter", "Image", "ImageRegistrationMethodv4", "ImageToImageMetricv4",
     "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
     "RegistrationBatch", "RegistrationRequest", "RegistrationResult", "RegistrationServer",

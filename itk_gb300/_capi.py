@@ -37,6 +37,7 @@ GB_IMAGE_MOVING = 1
 GB_TRANSFORM_AFFINE = 0
 GB_TRANSFORM_BSPLINE = 1
 GB_TRANSFORM_COMPOSITE = 2
+GB_TRANSFORM_DISPLACEMENT_FIELD = 3
 GB_GRADIENT_IMAGE = 0
 GB_GRADIENT_CENTRAL_DIFFERENCE = 1
 GB_GRADIENT_RECURSIVE_GAUSSIAN = 2

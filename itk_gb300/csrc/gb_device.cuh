@@ -269,6 +269,53 @@ __device__ __forceinline__ DFPos df_offset(const DFPos& p, const float* dhi, con
   return r;
 }
 
+// A double as an unevaluated float pair hi + lo by integer operations only (no
+// FP64 instruction): hi is the double truncated to 24 significant bits, lo the
+// remaining 29 bits rounded to float, so hi + lo = x within 2^-47 |x|.
+// |x| < 2^-126 gives 0 (lo is 0 below 2^-74); |x| >= 2^128, inf and NaN give NaN.
+__device__ __forceinline__ void split_double_bits(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned w1 = (unsigned)(b >> 32), w0 = (unsigned)b;
+  const unsigned sign = w1 & 0x80000000u;
+  const int e = (int)((w1 >> 20) & 0x7ffu);  // biased exponent
+  if (e < 897) {
+    hi = 0.f;
+    lo = 0.f;
+    return;
+  }
+  if (e > 1150) {
+    hi = __int_as_float(0x7fc00000);
+    lo = 0.f;
+    return;
+  }
+  hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((w1 & 0xfffffu) << 3) | (w0 >> 29));
+  lo = e < 949 ? 0.f : __uint2float_rn(w0 & 0x1fffffffu) * __uint_as_float(sign | ((unsigned)(e - 948) << 23));
+}
+
+// p + A u for a double-float matrix A and a double-float vector u (products with
+// FMA error terms, sums by two-sum), renormalized.
+__device__ __forceinline__ DFPos df_add_matvec(const DFPos& p, const AffineDF& A, const float uhi[3],
+                                               const float ulo[3]) {
+  DFPos r;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float s = p.hi[k], err = p.lo[k];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float a = A.Ahi[3 * k + j];
+      const float q = __fmul_rn(a, uhi[j]);
+      const float qe = __fmaf_rn(a, uhi[j], -q);  // exact product error
+      float t, e;
+      two_sum(s, q, t, e);
+      s = t;
+      err = __fadd_rn(err, __fadd_rn(e, __fadd_rn(qe, __fmaf_rn(A.Alo[3 * k + j], uhi[j], __fmul_rn(a, ulo[j])))));
+    }
+    r.hi[k] = __fadd_rn(s, err);
+    r.lo[k] = __fsub_rn(err, __fsub_rn(r.hi[k], s));
+  }
+  return r;
+}
+
 // ---------------------------------------------------------------------------
 // Ordered-int encodings of floats for atomic min/max.
 __device__ __forceinline__ int float_to_ordered(float f) {

@@ -102,6 +102,7 @@ struct BuildArgs {
   uint32_t* vals;
   float4* recs;
   float4* sup;  // B-spline support record per candidate (null without a B-spline)
+  uint32_t* voff;  // nearest virtual voxel per candidate, ~0u outside (displacement field on a point set; else null)
   unsigned long long* nvalid;
 };
 
@@ -224,16 +225,26 @@ __global__ void k_build_samples(BuildArgs b) {
   else b.recs[i] = make_float4((float)(i % b.virt.n[0]), (float)((i / b.virt.n[0]) % b.virt.n[1]),
                                (float)(i / (b.virt.n[0] * b.virt.n[1])), aux);
   if (b.sup) b.sup[i] = sup;
+  if (b.voff) {
+    // the derivative block's voxel: TransformPhysicalPointToIndex of the point
+    // (ImageToImageMetricv4GetValueAndDerivativeThreader.hxx:58), with
+    // ComputeParameterOffsetFromVirtualIndex (itkObjectToObjectMetric.hxx:332-343)
+    int64_t vi[3];
+    const bool in = d_nearest_index(b.virt, vp, vi);
+    b.voff[i] = in ? (uint32_t)(vi[0] + b.virt.n[0] * (vi[1] + b.virt.n[1] * vi[2])) : 0xffffffffu;
+  }
 }
 
 __global__ void k_gather_samples(const uint32_t* __restrict__ perm, int64_t n, const float4* __restrict__ recs,
                                  float4* __restrict__ out, const float4* __restrict__ sup_in,
-                                 float4* __restrict__ sup_out) {
+                                 float4* __restrict__ sup_out, const uint32_t* __restrict__ voff_in,
+                                 uint32_t* __restrict__ voff_out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t j = perm[i];
   out[i] = recs[j];
   if (sup_out) sup_out[i] = sup_in[j];
+  if (voff_out) voff_out[i] = voff_in[j];
 }
 
 // min / max over a float buffer (ordered-int atomics): out[0] = min, out[1] = max

@@ -149,6 +149,7 @@ struct gb_metric {
   gb::DevBuf<int> d_node_entries;  // chunk * 192 + support position of each (node, chunk) pair
   gb::DevBuf<float> d_chunk_part;  // nchunks x 192 Jacobian partial sums
   gb::DevBuf<float4> d_nodes;    // B-spline coefficients as float4 nodes
+  gb::DevBuf<uint32_t> d_voff;   // displacement field on a point set: each sample's nearest virtual voxel
   int64_t nchunks = 0;
   int64_t node_entries_count = 0;  // (node, chunk) pairs: chooses the parameter gather's shape
   int grid[3] = {0, 0, 0};       // B-spline control grid

@@ -53,6 +53,9 @@ struct EvalConsts {
   float joff[3];
   float Mg[9];  // B-spline paths: gradient -> (M^T g), M the initial affine of a composite (identity otherwise)
   float Pm[9];  // B-spline paths: physical displacement -> moving index offset, P2I M
+  // displacement-field paths (map = the identity transform's map):
+  AffineDF umap;  // physical displacement -> moving index offset (the moving image's P2I; b unused)
+  AffineDF fmap;  // point set: physical point -> field continuous index
 };
 
 __device__ __forceinline__ float3 jac_vec(const EvalConsts& K, float x, float y, float z) {
@@ -176,6 +179,11 @@ struct EvalArgs {
   // optimizer loop: nonzero once the optimizer has stopped; every evaluation
   // kernel then returns at once (iterations enqueued ahead become no-ops)
   const int* halt;
+  // displacement-field transform (local support)
+  const double* __restrict__ field;   // 3 doubles per virtual voxel: the transform's parameters
+  int vnx, vny, vnz;                  // the virtual grid, which is the field's
+  const unsigned* __restrict__ voff;  // point sets: each sample's nearest virtual voxel (~0u: outside)
+  int field_full;                     // dense, one sample per voxel: every derivative entry is written
 };
 
 // The optimizer's stop flag (read once per block, after the launch dependency).
@@ -547,6 +555,69 @@ __global__ void __launch_bounds__(kBlock) k_corr_affine(EvalArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Sample position in the moving image for each transform form:
+//   kMapAffine       the per-evaluation affine map of the record's coordinates;
+//   kMapFieldDense   the dense virtual grid under a displacement field: the
+//                    identity map plus P2I_moving u, u the field value at the
+//                    record's own voxel (DisplacementFieldTransform::TransformPoint
+//                    at a grid point: the interpolation weight is 1 there);
+//   kMapFieldPoints  a point set under a displacement field: u interpolated
+//                    trilinearly (VectorLinearInterpolateImageFunction, neighbours
+//                    clamped to the buffer), zero outside the field's buffer
+//                    (Filtering/DisplacementField/include/itkDisplacementFieldTransform.hxx:67-100).
+// `voxel` receives the virtual voxel whose derivative block the sample feeds.
+enum { kMapAffine = 0, kMapFieldDense = 1, kMapFieldPoints = 2 };
+
+__device__ __forceinline__ float3 field_interp(const double* __restrict__ f, const Stencil& st, int nx, int ny) {
+  const unsigned sy = (unsigned)nx, sz = (unsigned)nx * (unsigned)ny;
+  const unsigned zs[2] = {st.z0 * sz, st.z1 * sz}, ys[2] = {st.y0 * sy, st.y1 * sy}, xs[2] = {(unsigned)st.x0,
+                                                                                             (unsigned)st.x1};
+  float v[8][3];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const double* q = f + 3ull * (zs[c >> 2] + ys[(c >> 1) & 1] + xs[c & 1]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float h, l;
+      split_double_bits(__ldg(q + k), h, l);
+      v[c][k] = __fadd_rn(h, l);
+    }
+  }
+  float u[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float x00 = lerp(v[0][k], v[1][k], st.dx), x10 = lerp(v[2][k], v[3][k], st.dx);
+    const float x01 = lerp(v[4][k], v[5][k], st.dx), x11 = lerp(v[6][k], v[7][k], st.dx);
+    u[k] = lerp(lerp(x00, x10, st.dy), lerp(x01, x11, st.dy), st.dz);
+  }
+  return make_float3(u[0], u[1], u[2]);
+}
+
+template <int TK>
+__device__ __forceinline__ DFPos sample_pos(const EvalArgs& a, const EvalConsts& K, const float4& s, int64_t i,
+                                            unsigned& voxel) {
+  const DFPos p = map_pos(K.map, s.x, s.y, s.z);
+  if (TK == kMapAffine) return p;
+  float uhi[3], ulo[3];
+  if (TK == kMapFieldDense) {
+    voxel = (unsigned)s.x + (unsigned)a.vnx * ((unsigned)s.y + (unsigned)a.vny * (unsigned)s.z);
+    const double* q = a.field + 3ull * voxel;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) split_double_bits(__ldg(q + k), uhi[k], ulo[k]);
+  } else {
+    voxel = __ldg(a.voff + i);
+    const CIdx c = to_cidx(map_pos(K.fmap, s.x, s.y, s.z));
+    if (!ci_inside(c, a.vnx, a.vny, a.vnz)) return p;
+    const float3 u = field_interp(a.field, make_stencil(c, a.vnx, a.vny, a.vnz), a.vnx, a.vny);
+    uhi[0] = u.x;
+    uhi[1] = u.y;
+    uhi[2] = u.z;
+    ulo[0] = ulo[1] = ulo[2] = 0.f;
+  }
+  return df_add_matvec(p, K.umap, uhi, ulo);
+}
+
+// ---------------------------------------------------------------------------
 // Mattes pass 1, affine: joint histogram (Parzen: box on fixed, cubic B-spline
 // on moving), fixed marginal counts, moving marginal, valid count, per-sample
 // cache.  Histogram weights are 2^26 fixed point: integer adds are
@@ -733,7 +804,7 @@ __device__ __forceinline__ void mattes_value_groups(const EvalArgs& a, VGrid vg 
   }
 }
 
-template <int GRAD>
+template <int GRAD, int TK = kMapAffine>
 __device__ __forceinline__ void mattes_pass1_affine_body(const EvalArgs& a, VGrid vg) {
   extern __shared__ unsigned long long smem_u64[];
   const int B = a.bins;
@@ -766,7 +837,8 @@ __device__ __forceinline__ void mattes_pass1_affine_body(const EvalArgs& a, VGri
     float3 g = make_float3(0.f, 0.f, 0.f);
     bool ok = false;
     if (live) {
-      const DFPos p = map_pos(K.map, s.x, s.y, s.z);
+      unsigned voxel;
+      const DFPos p = sample_pos<TK>(a, K, s, i, voxel);
       ok = eval_moving<GRAD>(a, p, a.with_derivative != 0, m, g);
       // reject moving values outside [MovingImageTrueMin, MovingImageTrueMax], Mattes...Threader.hxx:238-245
       ok = ok && !(m < a.mmin) && !(m > a.mmax);

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "gb_bspline.cuh"
+#include "gb_field.cuh"
 #include "gb_init.cuh"
 #include "gb_internal.h"
 #include "gb_kernels.cuh"
@@ -117,6 +118,8 @@ static bool is_bspline(const gb_metric* m) {
   return m->tkind == GB_TRANSFORM_BSPLINE || m->tkind == GB_TRANSFORM_COMPOSITE;
 }
 
+static bool is_field(const gb_metric* m) { return m->tkind == GB_TRANSFORM_DISPLACEMENT_FIELD; }
+
 // Initial affine of a B-spline path: the composite's first transform ([affine,
 // B-spline] queue, B-spline applied first), the identity for a plain B-spline.
 static void bspline_init_affine(const gb_metric* m, double p[12], double c[3]) {
@@ -207,8 +210,8 @@ extern "C" int gb_metric_create(gb_ctx* ctx, int kind, gb_metric** out) {
 void gb_metric::release_buffers() {
   d_fixed.reset(); d_moving.reset(); d_fixed_s.reset(); d_moving_s.reset(); d_grad_in.reset();
   d_mov4.reset(); d_samples.reset(); d_cache.reset(); d_sup.reset(); d_chunks.reset();
-  d_node_first.reset(); d_node_entries.reset(); d_chunk_part.reset(); d_nodes.reset(); d_params.reset();
-  d_acc.reset(); d_scratch.reset(); d_out.reset(); d_status.reset(); d_pratio.reset(); d_pdf.reset();
+  d_node_first.reset(); d_node_entries.reset(); d_chunk_part.reset(); d_nodes.reset(); d_voff.reset();
+  d_params.reset(); d_acc.reset(); d_scratch.reset(); d_out.reset(); d_status.reset(); d_pratio.reset(); d_pdf.reset();
   d_consts.reset(); d_opt.reset(); d_opt_vec.reset();
 }
 
@@ -362,6 +365,20 @@ extern "C" int gb_metric_set_moving_transform(gb_metric* m, int kind, const doub
     if (nparams != 3 * nper) return fail(GB_ERR_BAD_ARG, "B-spline parameter count must be 3 * grid nodes");
     if (nper > 65536) return fail(GB_ERR_UNSUPPORTED, "B-spline grids above 65536 nodes are not supported");
     m->nper = nper;
+  } else if (kind == GB_TRANSFORM_DISPLACEMENT_FIELD) {
+    // DisplacementFieldTransform fixed parameters: size, origin, spacing, direction
+    // (itkDisplacementFieldTransform.hxx:520-570); the parameters are the field
+    if (nfixed != 18) return fail(GB_ERR_BAD_ARG, "displacement field fixed parameters: size, origin, spacing, direction (18)");
+    int64_t nv = 1;
+    for (int i = 0; i < 3; ++i) {
+      const double g = fixed[i];
+      if (!(g >= 1.0) || g != std::floor(g) || g > 2147483647.0)
+        return fail(GB_ERR_BAD_ARG, "displacement field size must be a positive integer");
+      nv *= (int64_t)g;
+      if (nv > (int64_t)0x7fffffff) return fail(GB_ERR_UNSUPPORTED, "displacement fields above 2^31-1 voxels");
+    }
+    if (nparams != 3 * nv) return fail(GB_ERR_BAD_ARG, "displacement field parameter count must be 3 * field voxels");
+    m->nper = 0;
   } else {
     return fail(GB_ERR_BAD_ARG, "unknown transform kind");
   }
@@ -428,7 +445,8 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   if (m->grad_source == GB_GRADIENT_IMAGE && !m->grad_set)
     return fail(GB_ERR_BAD_ARG, "gradient source is a gradient image but none was set");
   const bool bspline = is_bspline(m);
-  if (bspline && m->kind == GB_METRIC_CORRELATION)
+  const bool field = is_field(m);
+  if ((bspline || field) && m->kind == GB_METRIC_CORRELATION)
     return fail(GB_ERR_UNSUPPORTED, "the correlation metric runs affine transforms");
   double g_p2i[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   if (bspline) {
@@ -479,6 +497,26 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
       const int rc = geom_init(m->virt, sz, sp, org, m->fixed.dir);
       if (rc) return rc;
     }
+  }
+
+  if (field) {
+    // VerifyDisplacementFieldSizeAndPhysicalSpace (itkObjectToObjectMetric.hxx:444-503): the
+    // derivative field is laid out on the virtual grid, so the two grids must coincide
+    const double* f = m->tfixed.data();
+    for (int i = 0; i < 3; ++i)
+      if ((int64_t)f[i] != m->virt.size[i])
+        return fail(GB_ERR_BAD_ARG,
+                    "Virtual domain and moving transform displacement field must have the same size and index for "
+                    "BufferedRegion.");
+    const double ctol = 1.0e-6 * m->virt.spacing[0];
+    bool same = true;
+    for (int i = 0; i < 3; ++i)
+      same = same && std::fabs(f[3 + i] - m->virt.origin[i]) <= ctol && std::fabs(f[6 + i] - m->virt.spacing[i]) <= ctol;
+    for (int i = 0; i < 9; ++i) same = same && std::fabs(f[9 + i] - m->virt.dir[i]) <= 1.0e-6;
+    if (!same)
+      return fail(GB_ERR_BAD_ARG,
+                  "Virtual Domain and DisplacementField do not occupy the same physical space! You may be able to "
+                  "simply call displacementField->CopyInformation( metric->GetVirtualImage() ) to align them.");
   }
 
   const bool sampled = m->use_sampled;
@@ -576,10 +614,14 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     }
     for (int i = 0; i < 9; ++i) b.g_p2i[i] = g_p2i[i];
   }
+  DevBuf<uint32_t> voff;
+  const bool want_voff = field && sampled;
+  if (want_voff) GB_CUDA(voff.alloc_on(m->stream, ncand));
   b.keys = keys.p;
   b.vals = vals.p;
   b.recs = recs.p;
   b.sup = bspline ? sup.p : nullptr;
+  b.voff = want_voff ? voff.p : nullptr;
   b.nvalid = d_nvalid.p;
   k_build_samples<<<(unsigned)((ncand + kBlock - 1) / kBlock), kBlock, 0, st>>>(b);
   GB_CUDA(cudaGetLastError());
@@ -592,10 +634,12 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   GB_CUDA(m->d_samples.alloc_on(m->stream, std::max<int64_t>(1, m->nsamples)));
   m->d_sup.reset();
   if (bspline) GB_CUDA(m->d_sup.alloc_on(m->stream, std::max<int64_t>(1, m->nsamples)));
+  m->d_voff.reset();
+  if (want_voff) GB_CUDA(m->d_voff.alloc_on(m->stream, std::max<int64_t>(1, m->nsamples)));
   if (m->nsamples > 0)
     k_gather_samples<<<(unsigned)((m->nsamples + kBlock - 1) / kBlock), kBlock, 0, st>>>(
         vals_sorted.p, m->nsamples, recs.p, m->d_samples.p, bspline ? sup.p : nullptr,
-        bspline ? m->d_sup.p : nullptr);
+        bspline ? m->d_sup.p : nullptr, want_voff ? voff.p : nullptr, want_voff ? m->d_voff.p : nullptr);
   GB_CUDA(cudaGetLastError());
 
   // ---- B-spline: runs of same-cell samples (at most kChunkLen each) for the
@@ -720,6 +764,25 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
                   *m->h_consts);
     GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
   }
+  if (field) {
+    // the displacement-field constants are geometry only: the identity transform's
+    // map, the moving image's physical-to-index matrix for the displacement and,
+    // for a point set, the physical point -> field continuous index map
+    const double p[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0}, c[3] = {0, 0, 0};
+    EvalConsts& K = *m->h_consts;
+    affine_consts(p, c, m->moving.p2i, m->moving.origin, sampled ? nullptr : m->virt.i2p, m->virt.origin, K);
+    for (int i = 0; i < 9; ++i) split_df(m->moving.p2i[i], K.umap.Ahi[i], K.umap.Alo[i]);
+    for (int r = 0; r < 3; ++r) {
+      K.umap.bhi[r] = K.umap.blo[r] = 0.f;
+      double b = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        split_df(m->virt.p2i[3 * r + k], K.fmap.Ahi[3 * r + k], K.fmap.Alo[3 * r + k]);
+        b = gb::dadd(b, -gb::dmul(m->virt.p2i[3 * r + k], m->virt.origin[k]));
+      }
+      split_df(b, K.fmap.bhi[r], K.fmap.blo[r]);
+    }
+    GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
+  }
   GB_CUDA(cudaStreamSynchronize(st));
   m->initialized = true;
   return GB_OK;
@@ -787,6 +850,14 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
     a.node_first = m->d_node_first.p;
     a.node_entries = m->d_node_entries.p;
     a.chunk_part = m->d_chunk_part.p;
+  }
+  if (is_field(m)) {
+    a.field = d_params ? d_params : m->d_params.p;  // the host call uploads the field to d_params
+    a.vnx = (int)m->virt.size[0];
+    a.vny = (int)m->virt.size[1];
+    a.vnz = (int)m->virt.size[2];
+    a.voff = m->d_voff.p;
+    a.field_full = (!m->use_sampled && m->nsamples == m->virt.voxels()) ? 1 : 0;
   }
 }
 
@@ -880,6 +951,45 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
   return GB_OK;
 }
 
+// Displacement-field evaluation: MeanSquares in one pass; Mattes pass 1, the
+// value, then the per-sample derivative blocks.  The derivative field is
+// cleared first unless every virtual voxel holds a sample (each then stores its
+// own block, zeros when invalid).
+static int enqueue_eval_field(gb_metric* m, const EvalArgs& a, bool cd, bool deriv) {
+  const size_t P = m->tparams.size();
+  if (deriv && !a.field_full) GB_CUDA(cudaMemsetAsync(a.out + 2, 0, sizeof(double) * P, m->stream));
+  const bool pts = m->use_sampled;
+  if (m->kind == GB_METRIC_MEAN_SQUARES) {
+    cudaError_t e;
+    if (pts) e = cd ? launch_wave(m, k_msq_field<kGradCentralDifference, kMapFieldPoints>, 0, a)
+                    : launch_wave(m, k_msq_field<kGradImage, kMapFieldPoints>, 0, a);
+    else e = cd ? launch_wave(m, k_msq_field<kGradCentralDifference, kMapFieldDense>, 0, a)
+                : launch_wave(m, k_msq_field<kGradImage, kMapFieldDense>, 0, a);
+    GB_CUDA(e);
+    m->mark();
+    return GB_OK;
+  }
+  const int B = (int)m->bins;
+  const size_t sh1 = sizeof(unsigned long long) * (B * B + B) + sizeof(unsigned) * B;
+  if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
+  cudaError_t e;
+  if (pts) e = cd ? launch_wave(m, k_mattes_pass1_field<kGradCentralDifference, kMapFieldPoints>, sh1, a)
+                  : launch_wave(m, k_mattes_pass1_field<kGradImage, kMapFieldPoints>, sh1, a);
+  else e = cd ? launch_wave(m, k_mattes_pass1_field<kGradCentralDifference, kMapFieldDense>, sh1, a)
+              : launch_wave(m, k_mattes_pass1_field<kGradImage, kMapFieldDense>, sh1, a);
+  GB_CUDA(e);
+  m->mark();
+  GB_CUDA(launch_chain(m, k_mattes_finalize, (unsigned)mattes_groups(B), kFinalizeThreads, 0, a));
+  m->mark();
+  if (deriv) {
+    const size_t sh2 = sizeof(float) * B * B;
+    GB_CUDA(pts ? launch_wave(m, k_mattes_pass2_field<kMapFieldPoints>, sh2, a)
+                : launch_wave(m, k_mattes_pass2_field<kMapFieldDense>, sh2, a));
+    m->mark();
+  }
+  return GB_OK;
+}
+
 // Enqueues one evaluation; results land in d_out = [value, nvalid, derivative...].
 // device_params: the parameters are in device memory (d_params), so the affine
 // constants or the B-spline nodes are formed on the device; otherwise the host
@@ -889,7 +999,7 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
   EvalArgs a;
   fill_eval_args(m, a, d_params, d_out, deriv);
   GB_CUDA(cudaMemsetAsync(m->d_acc.p, 0, m->acc_bytes, st));
-  if (device_params && !is_bspline(m))
+  if (device_params && !is_bspline(m) && !is_field(m))
     GB_CUDA(launch_chain(m, k_prepare_affine, kConstEntries, 32, 0, a, m->d_consts.p));
   if (m->nsamples == 0) {
     // no valid fixed sample at all: every point is invalid
@@ -904,6 +1014,7 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
   m->nevents = 0;
   m->mark();
   if (is_bspline(m)) return enqueue_eval_bspline(m, a, cd, deriv, device_params);
+  if (is_field(m)) return enqueue_eval_field(m, a, cd, deriv);
   if (m->kind == GB_METRIC_CORRELATION) {
     // averages, then the value and derivative (at most kCorrMaxBlocks blocks: 27 partials each)
     GB_CUDA(cd ? launch_wave(m, k_corr_mean_affine<kGradCentralDifference>, 0, a)
@@ -970,6 +1081,8 @@ static int host_chain(gb_metric* m, bool deriv) {
   const size_t P = m->tparams.size();
   if (is_bspline(m))
     GB_CUDA(cudaMemcpyAsync(m->d_nodes.p, m->h_params, sizeof(float4) * m->nper, cudaMemcpyHostToDevice, st));
+  else if (is_field(m))
+    GB_CUDA(cudaMemcpyAsync(m->d_params.p, m->h_params, sizeof(double) * P, cudaMemcpyHostToDevice, st));
   else
     GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
   int rc = enqueue_eval(m, nullptr, m->d_out.p, deriv, false);
@@ -1031,6 +1144,9 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
     const int64_t np = m->nper;
     const double* c = m->tparams.data();
     for (int64_t n = 0; n < np; ++n) hn[n] = make_float4((float)c[n], (float)c[np + n], (float)c[2 * np + n], 0.f);
+  } else if (is_field(m)) {
+    // the field (the parameters), staged in pinned memory for the upload
+    std::memcpy(m->h_params, m->tparams.data(), sizeof(double) * P);
   } else {
     // per-evaluation constants in FP64 on the host, uploaded with the parameters
     const bool dense = !m->use_sampled;
@@ -1104,7 +1220,8 @@ extern "C" int gb_metric_get_mattes_state(gb_metric* m, double out8[8]) {
 size_t gb_metric::device_bytes() const {
   return d_fixed.bytes() + d_moving.bytes() + d_fixed_s.bytes() + d_moving_s.bytes() + d_grad_in.bytes() +
          d_mov4.bytes() + d_samples.bytes() + d_cache.bytes() + d_sup.bytes() + d_chunks.bytes() +
-         d_node_first.bytes() + d_node_entries.bytes() + d_chunk_part.bytes() + d_nodes.bytes() + d_params.bytes() +
+         d_node_first.bytes() + d_node_entries.bytes() + d_chunk_part.bytes() + d_nodes.bytes() + d_voff.bytes() +
+         d_params.bytes() +
          d_acc.bytes() + d_scratch.bytes() + d_out.bytes() + d_status.bytes() + d_pratio.bytes() + d_pdf.bytes() +
          d_consts.bytes() + d_opt.bytes() + d_opt_vec.bytes();
 }

@@ -208,19 +208,23 @@ int opt_setup(gb_metric* m, const gb_regular_step_settings* cfg, const double* s
                 "Relaxation factor must be less than 1.0. Current value is " + std::to_string(cfg->relaxation_factor));
   // scales (ObjectToObjectOptimizerBase::StartOptimization): > epsilon each; all
   // within 0.01 of 1 means identity, and the gradient is then not rescaled
+  // a displacement field has 3 local parameters per voxel; its scales are per local
+  // parameter and apply to parameter i as scales[i % 3] (ModifyGradientByScalesOverSubRange,
+  // Numerics/Optimizersv4/include/itkGradientDescentOptimizerv4.hxx:204-238)
+  const int64_t nlocal = m->tkind == GB_TRANSFORM_DISPLACEMENT_FIELD ? 3 : P;
   std::vector<double> inv_s((size_t)P, 1.0);
   if (nscales != 0) {
     if (!scales) return fail(GB_ERR_BAD_ARG, "null scales");
-    if (nscales != P)
+    if (nscales != nlocal)
       return fail(GB_ERR_BAD_ARG, "Size of scales (" + std::to_string(nscales) +
-                                      ") must equal number of local parameters (" + std::to_string(P) + ").");
+                                      ") must equal number of local parameters (" + std::to_string(nlocal) + ").");
     bool identity = true;
-    for (int64_t i = 0; i < P; ++i) {
+    for (int64_t i = 0; i < nlocal; ++i) {
       if (!(scales[i] > DBL_EPSILON)) return fail(GB_ERR_BAD_ARG, "m_Scales values must be > epsilon.");
       if (std::fabs(1.0 - scales[i]) > 0.01) identity = false;
     }
     if (!identity)
-      for (int64_t i = 0; i < P; ++i) inv_s[(size_t)i] = 1.0 / scales[i];
+      for (int64_t i = 0; i < P; ++i) inv_s[(size_t)i] = 1.0 / scales[i % nlocal];
   }
   GB_OPT_CUDA(cudaSetDevice(m->ctx->device));
   cudaStream_t st = m->stream;

@@ -20,7 +20,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .image import GradientImage, Image
+from .image import DisplacementFieldImage, GradientImage, Image
 from .transforms import AffineTransform, BSplineTransform, CompositeTransform
 
 
@@ -158,6 +158,28 @@ def random_bspline_coefficients(T: BSplineTransform, seed, max_disp=4.0):
     rng = np.random.default_rng(seed)
     T.SetParameters(rng.uniform(-1.0, 1.0, size=T.GetNumberOfParameters()) * (max_disp / np.sqrt(3.0)))
     return T
+
+
+def smooth_displacement_field(image: Image, seed, max_disp=2.0, mesh_size=(3, 3, 3)):
+    """A smooth field on the image's grid: the displacement of a seeded cubic B-spline
+    (at most max_disp long) at every voxel centre, as a DisplacementFieldImage."""
+    B = random_bspline_coefficients(bspline_over_image(image, mesh_size), seed, max_disp)
+    x = dense_points(image).astype(np.float64)
+    nx, ny, nz = image.GetSize()
+    u = (B.TransformPoint(x) - x).reshape(nz, ny, nx, 3)
+    return DisplacementFieldImage.like(image, u)
+
+
+def unique_voxel_points(image: Image, fraction, seed, jitter=0.4):
+    """A point set with at most one point per voxel: distinct random voxels, each moved by
+    up to `jitter` voxel along each index axis (the nearest voxel stays its own)."""
+    nx, ny, nz = image.GetSize()
+    total = nx * ny * nz
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(total, size=max(1, int(total * fraction)), replace=False))
+    ijk = np.stack([idx % nx, (idx // nx) % ny, idx // (nx * ny)], axis=1).astype(np.float64)
+    ijk += rng.uniform(-jitter, jitter, size=ijk.shape)
+    return (ijk @ image.index_to_physical().T + image.origin).astype(np.float32)
 
 
 def pair_bspline(size_xyz, mesh_size=(8, 8, 8), instance=0, max_disp=4.0, multimodal_map=True, config=2):

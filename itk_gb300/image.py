@@ -67,3 +67,37 @@ class GradientImage:
         if a.ndim != 4 or a.shape[3] != 3:
             raise ValueError("GradientImage expects a (nz, ny, nx, 3) array")
         self.array = np.ascontiguousarray(a)
+
+
+class DisplacementFieldImage:
+    """``Image<Vector<double,3>,3>``: a displacement per voxel, array of shape
+    (nz, ny, nx, 3) with the geometry of a scalar image."""
+
+    def __init__(self, array, spacing=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0), direction=None):
+        a = np.asarray(array, dtype=np.float64)
+        if a.ndim != 4 or a.shape[3] != 3:
+            raise ValueError("DisplacementFieldImage expects a (nz, ny, nx, 3) array")
+        self.array = np.ascontiguousarray(a)
+        self.spacing = np.asarray(spacing, dtype=np.float64).reshape(3)
+        self.origin = np.asarray(origin, dtype=np.float64).reshape(3)
+        self.direction = (np.eye(3) if direction is None else np.asarray(direction, dtype=np.float64)).reshape(3, 3)
+
+    @classmethod
+    def like(cls, image, array=None):
+        """A field on the grid of `image` (zero unless `array` is given)."""
+        nx, ny, nz = image.GetSize()
+        a = np.zeros((nz, ny, nx, 3)) if array is None else array
+        return cls(a, image.spacing, image.origin, image.direction)
+
+    def GetSize(self):
+        nz, ny, nx, _ = self.array.shape
+        return (nx, ny, nz)
+
+    def GetSpacing(self):
+        return tuple(self.spacing)
+
+    def GetOrigin(self):
+        return tuple(self.origin)
+
+    def GetDirection(self):
+        return self.direction.copy()

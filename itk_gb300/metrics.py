@@ -230,6 +230,13 @@ class ImageToImageMetricv4:
     def GetNumberOfParameters(self):
         return self._transform.GetNumberOfParameters()
 
+    def HasLocalSupport(self) -> bool:
+        """True under a displacement field: the derivative is a field over the virtual domain."""
+        return getattr(self._transform, "kind", None) == _capi.GB_TRANSFORM_DISPLACEMENT_FIELD
+
+    def GetNumberOfLocalParameters(self):
+        return 3 if self.HasLocalSupport() else self.GetNumberOfParameters()
+
     def UpdateTransformParameters(self, update, factor=1.0):
         self._transform.UpdateTransformParameters(update, factor)
 

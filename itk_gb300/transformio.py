@@ -17,13 +17,14 @@ import math
 
 import numpy as np
 
-from .transforms import AffineTransform, BSplineTransform, CompositeTransform
+from .transforms import AffineTransform, BSplineTransform, CompositeTransform, DisplacementFieldTransform
 
 HEADER = "#Insight Transform File V1.0"
 _TYPES = {
     "AffineTransform_double_3_3": AffineTransform,
     "BSplineTransform_double_3_3": BSplineTransform,
     "CompositeTransform_double_3_3": CompositeTransform,
+    "DisplacementFieldTransform_double_3_3": DisplacementFieldTransform,
 }
 
 
@@ -71,6 +72,8 @@ def _type_string(t) -> str:
         return "BSplineTransform_double_3_3"
     if isinstance(t, AffineTransform):
         return "AffineTransform_double_3_3"
+    if isinstance(t, DisplacementFieldTransform):
+        return "DisplacementFieldTransform_double_3_3"
     raise TypeError(f"no transform file type for {type(t).__name__}")
 
 
@@ -126,7 +129,8 @@ def transforms_from_text(text: str):
                 if pending_params is not None:
                     cur.SetParameters(pending_params)
                     pending_params = None
-            elif isinstance(cur, BSplineTransform) and cur.GetNumberOfParameters() != vals.size:
+            elif isinstance(cur, (BSplineTransform, DisplacementFieldTransform)) and \
+                    cur.GetNumberOfParameters() != vals.size:
                 pending_params = vals  # the grid comes with the fixed parameters
             else:
                 cur.SetParameters(vals)

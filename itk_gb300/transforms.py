@@ -8,6 +8,11 @@
   coefficients (dimension-major, x fastest), 18 fixed parameters: grid size,
   grid origin, grid spacing, grid direction
   (Core/Transform/include/itkBSplineTransform.hxx:243-330).
+* ``DisplacementFieldTransform`` -- ``DisplacementFieldTransform<double,3>``:
+  y = x + u(x), u linearly interpolated from a vector field and zero outside
+  its buffer; the parameters are the field itself (3 per voxel), 18 fixed
+  parameters: field size, origin, spacing, direction
+  (Filtering/DisplacementField/include/itkDisplacementFieldTransform.hxx:67-100,520-570).
 * ``CompositeTransform`` -- queue applied in reverse
   (Core/Transform/include/itkCompositeTransform.hxx:60-70), the most recently
   added transform optimized; supported queues: [T] and [affine, B-spline].
@@ -17,10 +22,12 @@ from __future__ import annotations
 import numpy as np
 
 from . import _capi
+from .image import DisplacementFieldImage
 
 TRANSFORM_AFFINE = _capi.GB_TRANSFORM_AFFINE
 TRANSFORM_BSPLINE = _capi.GB_TRANSFORM_BSPLINE
 TRANSFORM_COMPOSITE = _capi.GB_TRANSFORM_COMPOSITE
+TRANSFORM_DISPLACEMENT_FIELD = _capi.GB_TRANSFORM_DISPLACEMENT_FIELD
 
 
 class AffineTransform:
@@ -181,6 +188,90 @@ def _bspline3(u):
     s = a * a
     return np.where(a < 1.0, (4.0 - 6.0 * s + 3.0 * s * a) / 6.0,
                     np.where(a < 2.0, (8.0 - 12.0 * a + 6.0 * s - s * a) / 6.0, 0.0))
+
+
+class DisplacementFieldTransform:
+    """Dense displacement field; local support (3 parameters per voxel)."""
+
+    kind = TRANSFORM_DISPLACEMENT_FIELD
+
+    def __init__(self):
+        self.field = None
+
+    def SetDisplacementField(self, field: DisplacementFieldImage):
+        """The transform keeps the field: its parameters are the field's buffer."""
+        if not isinstance(field, DisplacementFieldImage):
+            raise TypeError("SetDisplacementField expects a DisplacementFieldImage")
+        self.field = field
+
+    def GetDisplacementField(self) -> DisplacementFieldImage:
+        return self.field
+
+    def _need_field(self):
+        if self.field is None:
+            raise ValueError("No displacement field is specified.")
+
+    def GetNumberOfLocalParameters(self):
+        return 3
+
+    def GetNumberOfParameters(self):
+        return 0 if self.field is None else self.field.array.size
+
+    def GetParameters(self):
+        self._need_field()
+        return self.field.array.reshape(-1).copy()
+
+    def SetParameters(self, p):
+        self._need_field()
+        p = np.asarray(p, dtype=np.float64).reshape(-1)
+        if p.size != self.field.array.size:
+            raise ValueError("displacement field parameter count must be 3 * field voxels")
+        self.field.array[...] = p.reshape(self.field.array.shape)
+
+    def GetFixedParameters(self):
+        self._need_field()
+        f = self.field
+        return np.concatenate([np.asarray(f.GetSize(), np.float64), f.origin, f.spacing, f.direction.reshape(9)])
+
+    def SetFixedParameters(self, fp):
+        """A zero field of the described grid (SetDisplacementFieldFromFixedParameters)."""
+        fp = np.asarray(fp, dtype=np.float64).reshape(18)
+        nx, ny, nz = (int(v) for v in fp[:3])
+        self.field = DisplacementFieldImage(np.zeros((nz, ny, nx, 3)), fp[6:9], fp[3:6], fp[9:18].reshape(3, 3))
+
+    def UpdateTransformParameters(self, update, factor=1.0):
+        self.SetParameters(self.GetParameters() + np.asarray(update, np.float64) * factor)
+
+    def TransformPoint(self, x):
+        """x + u(x) inside the field's buffer (VectorLinearInterpolateImageFunction:
+        neighbours of floor(cindex) clamped to the buffer), x outside it."""
+        self._need_field()
+        x = np.atleast_2d(np.asarray(x, dtype=np.float64))
+        f = self.field
+        n = np.asarray(f.GetSize(), np.int64)
+        ci = (x - f.origin) @ np.linalg.inv(f.direction @ np.diag(f.spacing)).T
+        inside = np.all((ci >= -0.5) & (ci < n - 0.5), axis=1)
+        base = np.floor(ci).astype(np.int64)
+        dist = ci - base
+        u = np.zeros_like(x)
+        for corner in range(8):
+            w = np.ones(len(x))
+            idx = np.empty_like(base)
+            for d in range(3):
+                if (corner >> d) & 1:
+                    idx[:, d] = np.minimum(base[:, d] + 1, n[d] - 1)
+                    w = w * dist[:, d]
+                else:
+                    idx[:, d] = np.maximum(base[:, d], 0)
+                    w = w * (1.0 - dist[:, d])
+            idx = np.clip(idx, 0, n - 1)
+            u += w[:, None] * f.array[idx[:, 2], idx[:, 1], idx[:, 0]]
+        out = x.copy()
+        out[inside] += u[inside]
+        return out
+
+    def flat(self):
+        return self.kind, self.GetParameters(), self.GetFixedParameters()
 
 
 class CompositeTransform:

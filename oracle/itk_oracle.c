@@ -342,9 +342,82 @@ int orc_composite_init(orc_transform *t, const double ap[12], const double ac[3]
   return ORC_OK;
 }
 
+/* DisplacementFieldTransform fixed parameters: size, origin, spacing, direction
+ * (Filtering/DisplacementField/include/itkDisplacementFieldTransform.hxx:520-570);
+ * the parameters are the field buffer, 3 values per voxel. */
+int orc_displacement_init(orc_transform *t, const double f[18], const double *field)
+{
+  memset(t, 0, sizeof(*t));
+  t->kind = ORC_TRANSFORM_DISPLACEMENT;
+  int64_t size[3];
+  for (int i = 0; i < 3; ++i) {
+    if (!(f[i] >= 1.0) || f[i] != floor(f[i])) return ORC_ERR_BAD_ARG;
+    size[i] = (int64_t)f[i];
+  }
+  int rc = orc_geom_init(&t->fgeom, size, f + 6, f + 3, f + 9);
+  if (rc) return rc;
+  t->nvox = size[0] * size[1] * size[2];
+  t->field = field;
+  return ORC_OK;
+}
+
 int64_t orc_transform_nparams(const orc_transform *t)
 {
+  if (t->kind == ORC_TRANSFORM_DISPLACEMENT) return 3 * t->nvox;
   return t->kind == ORC_TRANSFORM_AFFINE ? 12 : 3 * t->nper;
+}
+
+/* VectorLinearInterpolateImageFunction::EvaluateAtContinuousIndex,
+ * Core/ImageFunction/include/itkVectorLinearInterpolateImageFunction.hxx:35-105:
+ * the 2^3 neighbours of floor(ci), clamped to the buffer, weighted by their
+ * overlap; the loop ends once the overlaps sum to exactly 1. */
+static inline void vector_linear(const orc_geom *g, const double *img, const double ci[3], double out[3])
+{
+  int64_t base[3];
+  double dist[3];
+  for (int d = 0; d < 3; ++d) {
+    base[d] = (int64_t)floor(ci[d]);
+    dist[d] = ci[d] - (double)base[d];
+  }
+  out[0] = out[1] = out[2] = 0.0;
+  double total = 0.0;
+  const int64_t nx = g->size[0], nxy = g->size[0] * g->size[1];
+  for (unsigned counter = 0; counter < 8; ++counter) {
+    double overlap = 1.0;
+    unsigned upper = counter;
+    int64_t nb[3];
+    for (int d = 0; d < 3; ++d) {
+      if (upper & 1) {
+        nb[d] = base[d] + 1 < g->size[d] - 1 ? base[d] + 1 : g->size[d] - 1;
+        overlap *= dist[d];
+      } else {
+        nb[d] = base[d] > 0 ? base[d] : 0;
+        overlap *= 1.0 - dist[d];
+      }
+      upper >>= 1;
+    }
+    if (overlap != 0.0) {
+      const double *px = img + 3 * (nb[0] + nb[1] * nx + nb[2] * nxy);
+      for (int k = 0; k < 3; ++k) out[k] += overlap * px[k];
+      total += overlap;
+    }
+    if (total == 1.0) break;
+  }
+}
+
+/* DisplacementFieldTransform::TransformPoint, itkDisplacementFieldTransform.hxx:67-100:
+ * x + field(x) inside the field's buffer, x outside it. */
+static inline void displacement_apply(const orc_transform *t, const double x[3], double y[3])
+{
+  double ci[3];
+  point_to_cindex(&t->fgeom, x, ci);
+  y[0] = x[0];
+  y[1] = x[1];
+  y[2] = x[2];
+  if (!inside_buffer(&t->fgeom, ci)) return;
+  double u[3];
+  vector_linear(&t->fgeom, t->field, ci, u);
+  for (int k = 0; k < 3; ++k) y[k] += u[k];
 }
 
 static inline void affine_apply(const orc_transform *t, const double x[3], double y[3])
@@ -443,6 +516,8 @@ void orc_transform_point(const orc_transform *t, const double x[3], double y[3])
   int64_t st[3];
   if (t->kind == ORC_TRANSFORM_AFFINE) {
     affine_apply(t, x, y);
+  } else if (t->kind == ORC_TRANSFORM_DISPLACEMENT) {
+    displacement_apply(t, x, y);
   } else if (t->kind == ORC_TRANSFORM_BSPLINE) {
     bspline_apply(t, x, y, w, st);
   } else {
@@ -473,7 +548,7 @@ typedef struct {
   double moving_value; /* MovingImagePixelType */
   double grad[3];
   /* Jacobian support */
-  int jac_kind; /* 0 affine dense 12, 1 bspline sparse, 2 outside b-spline support (zero) */
+  int jac_kind; /* 0 affine dense 12, 1 bspline sparse, 2 outside b-spline support (zero), 3 displacement (local) */
   double v[3];  /* x - centre (affine) */
   double w[64];
   int64_t start[3];
@@ -497,6 +572,8 @@ static inline int evaluate_point(const orc_inputs *in, const orc_transform *t, c
   int inside_bs = 0;
   if (t->kind == ORC_TRANSFORM_AFFINE) {
     affine_apply(t, vp, mp);
+  } else if (t->kind == ORC_TRANSFORM_DISPLACEMENT) {
+    displacement_apply(t, vp, mp);
   } else if (t->kind == ORC_TRANSFORM_BSPLINE) {
     inside_bs = bspline_apply(t, vp, mp, pe->w, pe->start);
   } else {
@@ -517,6 +594,8 @@ static inline int evaluate_point(const orc_inputs *in, const orc_transform *t, c
     if (t->kind == ORC_TRANSFORM_AFFINE) {
       pe->jac_kind = 0;
       for (int k = 0; k < 3; ++k) pe->v[k] = vp[k] - t->center[k];
+    } else if (t->kind == ORC_TRANSFORM_DISPLACEMENT) {
+      pe->jac_kind = 3; /* identity: J^T g = g at the point's own field voxel */
     } else {
       pe->jac_kind = inside_bs ? 1 : 2;
     }
@@ -542,7 +621,7 @@ static inline void jacobian_product(const orc_transform *t, const point_eval *pe
     }
     return;
   }
-  if (pe->jac_kind == 2) return;
+  if (pe->jac_kind == 2 || pe->jac_kind == 3) return; /* 3: local support, handled by the caller */
   double gd[3];
   if (t->kind == ORC_TRANSFORM_COMPOSITE) {
     /* column d of M * J_bs is M[:,d] w_k; its product with g is w_k (M^T g)_d,
@@ -588,6 +667,34 @@ static inline void domain_point(const orc_inputs *in, int64_t i, double vp[3])
   }
 }
 
+/* ComputeParameterOffsetFromVirtualIndex (Numerics/Optimizersv4/include/itkObjectToObjectMetric.hxx:332-343):
+ * the point's virtual index (its own index for the dense domain,
+ * TransformPhysicalPointToIndex for a point set) times 3.  -1 for a point set
+ * point whose nearest index lies outside the virtual grid (the reference
+ * indexes past the derivative there; such points add nothing here). */
+static inline int64_t local_offset(const orc_inputs *in, int64_t i, const double vp[3])
+{
+  if (!in->points) return 3 * i;
+  int64_t idx[3];
+  if (!point_to_index(&in->virtual_geom, vp, idx)) return -1;
+  return 3 * (idx[0] + in->virtual_geom.size[0] * (idx[1] + in->virtual_geom.size[1] * idx[2]));
+}
+
+/* VerifyDisplacementFieldSizeAndPhysicalSpace, itkObjectToObjectMetric.hxx:444-503 */
+static int verify_field_domain(const orc_inputs *in, const orc_transform *t)
+{
+  if (t->kind != ORC_TRANSFORM_DISPLACEMENT) return ORC_OK;
+  const orc_geom *v = &in->virtual_geom, *f = &t->fgeom;
+  for (int i = 0; i < 3; ++i)
+    if (v->size[i] != f->size[i]) return ORC_ERR_BAD_ARG;
+  const double ctol = 1.0e-6 * v->spacing[0];
+  for (int i = 0; i < 3; ++i)
+    if (fabs(v->origin[i] - f->origin[i]) > ctol || fabs(v->spacing[i] - f->spacing[i]) > ctol) return ORC_ERR_BAD_ARG;
+  for (int i = 0; i < 9; ++i)
+    if (fabs(v->direction[i] - f->direction[i]) > 1.0e-6) return ORC_ERR_BAD_ARG;
+  return ORC_OK;
+}
+
 static int resolve_threads(int requested, int64_t n)
 {
   int t = requested > 0 ? requested : 1;
@@ -609,6 +716,8 @@ typedef struct {
   uint64_t nvalid;
   int64_t nparams;
   double *dsum, *dcomp; /* per-thread compensated derivatives */
+  int64_t *loff;        /* local support: per point, the derivative offset (-1: none) */
+  double *lval;         /* local support: per point, 3 local derivatives */
 } msq_job;
 
 /* MeanSquaresImageToImageMetricv4GetValueAndDerivativeThreader::ProcessPoint,
@@ -629,6 +738,13 @@ static void *msq_worker(void *arg)
     j->measure += diffC * diffC;
     j->nvalid++;
     if (!j->compute_derivative) continue;
+    if (j->loff) {
+      /* local support: the point's own derivative block, stored at its offset
+       * afterwards (StorePointDerivativeResult, ThreaderBase.hxx:301-320) */
+      j->loff[i - j->begin] = local_offset(j->in, i, vp);
+      for (int d = 0; d < 3; ++d) j->lval[3 * (i - j->begin) + d] = 2.0 * diffC * pe.grad[d];
+      continue;
+    }
     jacobian_product(j->t, &pe, &row);
     for (int e = 0; e < row.count; ++e) {
       /* localDerivative[par] = sum_dim 2.0 * diff * J(dim,par) * g[dim]; with one
@@ -646,6 +762,8 @@ int orc_msq_value_derivative(const orc_inputs *in, const orc_transform *t, int c
   const int64_t n = domain_size(in);
   const int64_t P = orc_transform_nparams(t);
   if (n < 1) return ORC_ERR_BAD_ARG;
+  if (verify_field_domain(in, t)) return ORC_ERR_BAD_ARG;
+  const int local = t->kind == ORC_TRANSFORM_DISPLACEMENT;
   const int T = resolve_threads(in->nthreads, n);
   msq_job *jobs = (msq_job *)calloc((size_t)T, sizeof(msq_job));
   pthread_t *th = (pthread_t *)calloc((size_t)T, sizeof(pthread_t));
@@ -659,7 +777,13 @@ int orc_msq_value_derivative(const orc_inputs *in, const orc_transform *t, int c
     jobs[k].begin = k * chunk < n ? k * chunk : n;
     jobs[k].end = (k + 1) * chunk < n ? (k + 1) * chunk : n;
     jobs[k].nparams = P;
-    if (compute_derivative) {
+    if (compute_derivative && local) {
+      const int64_t len = jobs[k].end - jobs[k].begin;
+      jobs[k].loff = (int64_t *)malloc(sizeof(int64_t) * (size_t)(len > 0 ? len : 1));
+      jobs[k].lval = (double *)malloc(sizeof(double) * 3 * (size_t)(len > 0 ? len : 1));
+      if (!jobs[k].loff || !jobs[k].lval) rc = ORC_ERR_OOM;
+      for (int64_t q = 0; jobs[k].loff && q < len; ++q) jobs[k].loff[q] = -1;
+    } else if (compute_derivative) {
       jobs[k].dsum = (double *)calloc((size_t)P, sizeof(double));
       jobs[k].dcomp = (double *)calloc((size_t)P, sizeof(double));
       if (!jobs[k].dsum || !jobs[k].dcomp) rc = ORC_ERR_OOM;
@@ -672,7 +796,17 @@ int orc_msq_value_derivative(const orc_inputs *in, const orc_transform *t, int c
     uint64_t nv = 0;
     for (int k = 0; k < T; ++k) nv += jobs[k].nvalid;
     *nvalid = nv;
-    if (compute_derivative) {
+    if (compute_derivative && local) {
+      /* local support: Derivatives[offset + i] += LocalDerivatives[i] in point
+       * order, no averaging (ThreaderBase.hxx:128-172,301-320) */
+      for (int64_t p = 0; p < P; ++p) derivative[p] = 0.0;
+      for (int k = 0; k < T; ++k)
+        for (int64_t q = 0; q < jobs[k].end - jobs[k].begin; ++q) {
+          const int64_t o = jobs[k].loff[q];
+          if (o < 0) continue;
+          for (int d = 0; d < 3; ++d) derivative[o + d] += jobs[k].lval[3 * q + d];
+        }
+    } else if (compute_derivative) {
       for (int64_t p = 0; p < P; ++p) {
         double s = 0.0, c = 0.0;
         for (int k = 0; k < T; ++k) kahan_add(&s, &c, jobs[k].dsum[p]);
@@ -689,11 +823,11 @@ int orc_msq_value_derivative(const orc_inputs *in, const orc_transform *t, int c
       double v = 0.0;
       for (int k = 0; k < T; ++k) v += jobs[k].measure;
       *value = v / (double)nv;
-      if (compute_derivative)
+      if (compute_derivative && !local)
         for (int64_t p = 0; p < P; ++p) derivative[p] /= (double)nv;
     }
   }
-  for (int k = 0; k < T; ++k) { free(jobs[k].dsum); free(jobs[k].dcomp); }
+  for (int k = 0; k < T; ++k) { free(jobs[k].dsum); free(jobs[k].dcomp); free(jobs[k].loff); free(jobs[k].lval); }
   free(jobs);
   free(th);
   return rc;
@@ -788,6 +922,7 @@ int orc_corr_value_derivative(const orc_inputs *in, const orc_transform *t, int 
   const int64_t n = domain_size(in);
   const int64_t P = orc_transform_nparams(t);
   if (n < 1) return ORC_ERR_BAD_ARG;
+  if (t->kind == ORC_TRANSFORM_DISPLACEMENT) return ORC_ERR_BAD_ARG; /* global-support transforms only here */
   const int T = resolve_threads(in->nthreads, n);
   corr_job *jobs = (corr_job *)calloc((size_t)T, sizeof(corr_job));
   if (!jobs) return ORC_ERR_OOM;
@@ -940,6 +1075,9 @@ typedef struct {
   double *pdf;      /* bins*bins */
   double *fmarg;    /* bins */
   double *pdfd;     /* [f][m][P] */
+  int64_t *loff;    /* local support: per point, the derivative offset (-1: none) */
+  int64_t *lidx;    /* local support: per point, JointPdfIndex1D of its first moving bin */
+  double *lval;     /* local support: per point, [bin][d] local derivative by Parzen bin */
 } mattes_job;
 
 /* MattesMutualInformationImageToImageMetricv4GetValueAndDerivativeThreader::ProcessPoint,
@@ -973,17 +1111,31 @@ static void *mattes_worker(void *arg)
     j->fmarg[fidx] += 1;
     double arg = (double)pdfm - mterm;
     double *pdfrow = j->pdf + fidx * bins + pdfm;
-    if (j->compute_derivative) jacobian_product(j->t, &pe, &row);
+    const int64_t q = i - j->begin;
+    if (j->compute_derivative && j->loff) {
+      /* local support (Mattes...Threader.hxx:300-312): the point's offset and joint-PDF index */
+      j->loff[q] = local_offset(j->in, i, vp);
+      j->lidx[q] = pdfm + fidx * bins;
+    } else if (j->compute_derivative) {
+      jacobian_product(j->t, &pe, &row);
+    }
+    int bin = 0;
     while (pdfm <= pdfmax) {
       const double val = orc_bspline3(arg);
       *(pdfrow++) += val;
-      if (j->compute_derivative) {
+      if (j->compute_derivative && j->loff) {
+        /* ComputePDFDerivativesLocalSupportTransform (.hxx:394-412) with the
+         * identity Jacobian: innerProduct = g[mu] */
+        const double dval = orc_bspline3_derivative(arg);
+        for (int d = 0; d < 3; ++d) j->lval[12 * q + 3 * bin + d] = pe.grad[d] * dval;
+      } else if (j->compute_derivative) {
         const double dval = orc_bspline3_derivative(arg);
         double *dst = j->pdfd + (fidx * bins + pdfm) * P;
         for (int e = 0; e < row.count; ++e) dst[row.idx[e]] += row.val[e] * dval;
       }
       arg += 1.0;
       ++pdfm;
+      ++bin;
     }
     j->nvalid++;
   }
@@ -998,9 +1150,11 @@ int orc_mattes_value_derivative(const orc_inputs *in, const orc_mattes_state *st
   const int64_t P = orc_transform_nparams(t);
   const int64_t bins = st->bins;
   if (n < 1) return ORC_ERR_BAD_ARG;
+  if (verify_field_domain(in, t)) return ORC_ERR_BAD_ARG;
+  const int local = t->kind == ORC_TRANSFORM_DISPLACEMENT;
   int T = resolve_threads(in->nthreads, n);
   /* bound the per-thread derivative arrays to ~2 GB in total */
-  if (compute_derivative) {
+  if (compute_derivative && !local) {
     const double per = (double)P * (double)(bins * bins) * 8.0;
     while (T > 1 && per * T > 2.0e9) --T;
   }
@@ -1019,8 +1173,18 @@ int orc_mattes_value_derivative(const orc_inputs *in, const orc_mattes_state *st
     jobs[k].nparams = P;
     jobs[k].pdf = (double *)calloc((size_t)(bins * bins), sizeof(double));
     jobs[k].fmarg = (double *)calloc((size_t)bins, sizeof(double));
-    if (compute_derivative) jobs[k].pdfd = (double *)calloc((size_t)(bins * bins * P), sizeof(double));
-    if (!jobs[k].pdf || !jobs[k].fmarg || (compute_derivative && !jobs[k].pdfd)) rc = ORC_ERR_OOM;
+    if (compute_derivative && local) {
+      const int64_t len = jobs[k].end - jobs[k].begin > 0 ? jobs[k].end - jobs[k].begin : 1;
+      jobs[k].loff = (int64_t *)malloc(sizeof(int64_t) * (size_t)len);
+      jobs[k].lidx = (int64_t *)malloc(sizeof(int64_t) * (size_t)len);
+      jobs[k].lval = (double *)calloc((size_t)(12 * len), sizeof(double));
+      if (!jobs[k].loff || !jobs[k].lidx || !jobs[k].lval) rc = ORC_ERR_OOM;
+      for (int64_t q = 0; jobs[k].loff && q < len; ++q) jobs[k].loff[q] = -1;
+    } else if (compute_derivative) {
+      jobs[k].pdfd = (double *)calloc((size_t)(bins * bins * P), sizeof(double));
+      if (!jobs[k].pdfd) rc = ORC_ERR_OOM;
+    }
+    if (!jobs[k].pdf || !jobs[k].fmarg) rc = ORC_ERR_OOM;
   }
   if (rc == ORC_OK) {
     for (int k = 0; k < T; ++k) pthread_create(&th[k], NULL, mattes_worker, &jobs[k]);
@@ -1039,7 +1203,23 @@ int orc_mattes_value_derivative(const orc_inputs *in, const orc_mattes_state *st
     double jsum = 0.0, jc = 0.0;
     for (int64_t i = 0; i < bins * bins; ++i) kahan_add(&jsum, &jc, pdf[i]);
     double *pdfd = NULL;
-    if (compute_derivative) {
+    double *lbin = NULL;    /* local support: m_LocalDerivativeByParzenBin[4][P] */
+    int64_t *l1d = NULL;    /* local support: m_JointPdfIndex1DArray[P] */
+    if (compute_derivative && local) {
+      /* the points' blocks in point order: by-bin sums add up, the joint-PDF
+       * index is the last point's (Mattes...Threader.hxx:300-312,340-351) */
+      lbin = (double *)calloc((size_t)(4 * P), sizeof(double));
+      l1d = (int64_t *)calloc((size_t)P, sizeof(int64_t));
+      if (!lbin || !l1d) rc = ORC_ERR_OOM;
+      for (int k = 0; rc == ORC_OK && k < T; ++k)
+        for (int64_t q = 0; q < jobs[k].end - jobs[k].begin; ++q) {
+          const int64_t o = jobs[k].loff[q];
+          if (o < 0) continue;
+          for (int b = 0; b < 4; ++b)
+            for (int d = 0; d < 3; ++d) lbin[b * P + o + d] += jobs[k].lval[12 * q + 3 * b + d];
+          for (int d = 0; d < 3; ++d) l1d[o + d] = jobs[k].lidx[q];
+        }
+    } else if (compute_derivative) {
       pdfd = jobs[0].pdfd;
       for (int k = 1; k < T; ++k)
         for (int64_t i = 0; i < bins * bins * P; ++i) pdfd[i] += jobs[k].pdfd[i];
@@ -1049,7 +1229,9 @@ int orc_mattes_value_derivative(const orc_inputs *in, const orc_mattes_state *st
       }
     }
     /* ComputeResults, Mattes...v4.hxx:358-499 */
-    if (nv == 0) {
+    if (rc != ORC_OK) {
+      /* allocation failure above: no result */
+    } else if (nv == 0) {
       rc = ORC_ERR_NO_VALID_POINTS;
     } else if (jsum < DBL_EPSILON) {
       rc = ORC_ERR_JOINT_PDF_SUM_ZERO;
@@ -1069,6 +1251,9 @@ int orc_mattes_value_derivative(const orc_inputs *in, const orc_mattes_state *st
         if (compute_derivative)
           for (int64_t p = 0; p < P; ++p) derivative[p] = 0.0;
         const double closeToZero = DBL_EPSILON;
+        /* local support: m_PRatioArray, zero where a bin is skipped; nFactor = 1 / (binsize N) */
+        double *pra = local && compute_derivative ? (double *)calloc((size_t)(bins * bins), sizeof(double)) : NULL;
+        const double nFactorLocal = 1.0 / (st->moving_bin_size * (double)nv);
         double sum = 0.0;
         for (int64_t f = 0; f < bins; ++f) {
           const double fpdf = fm[f];
@@ -1080,20 +1265,37 @@ int orc_mattes_value_derivative(const orc_inputs *in, const orc_mattes_state *st
             if (mp > closeToZero && jp > closeToZero) {
               const double pRatio = log(jp / mp);
               sum += jp * (pRatio - logf);
-              if (compute_derivative) {
+              if (compute_derivative && local) {
+                if (pra) pra[f * bins + m] = pRatio * nFactorLocal;
+              } else if (compute_derivative) {
                 const double *dp = pdfd + (f * bins + m) * P;
                 for (int64_t p = 0; p < P; ++p) derivative[p] += dp[p] * pRatio;
               }
             }
           }
         }
+        if (compute_derivative && local) {
+          /* Mattes...v4.hxx:478-495: derivative[i] -= LocalDerivativeByParzenBin[bin][i] * PRatio[index1D + bin] */
+          if (!pra) {
+            rc = ORC_ERR_OOM;
+          } else {
+            for (int64_t i = 0; i < P; ++i)
+              for (int b = 0; b < 4; ++b) derivative[i] -= lbin[b * P + i] * pra[l1d[i] + b];
+          }
+          free(pra);
+        }
         *value = -1.0 * sum;
         free(mm);
       }
     }
     if (joint_pdf) memcpy(joint_pdf, pdf, sizeof(double) * (size_t)(bins * bins));
+    free(lbin);
+    free(l1d);
   }
-  for (int k = 0; k < T; ++k) { free(jobs[k].pdf); free(jobs[k].fmarg); free(jobs[k].pdfd); }
+  for (int k = 0; k < T; ++k) {
+    free(jobs[k].pdf); free(jobs[k].fmarg); free(jobs[k].pdfd);
+    free(jobs[k].loff); free(jobs[k].lidx); free(jobs[k].lval);
+  }
   free(jobs);
   free(th);
   return rc;
@@ -1115,6 +1317,12 @@ int orc_transform_from_flat(orc_transform *t, int tkind, const double *tparams, 
     int rc = orc_bspline_init(t, tfixed, tparams);
     if (rc) return rc;
     return nparams == 3 * t->nper ? ORC_OK : ORC_ERR_BAD_ARG;
+  }
+  if (tkind == ORC_TRANSFORM_DISPLACEMENT) {
+    if (nfixed != 18) return ORC_ERR_BAD_ARG;
+    int rc = orc_displacement_init(t, tfixed, tparams);
+    if (rc) return rc;
+    return nparams == 3 * t->nvox ? ORC_OK : ORC_ERR_BAD_ARG;
   }
   if (tkind == ORC_TRANSFORM_COMPOSITE) {
     if (nfixed != 33) return ORC_ERR_BAD_ARG;

@@ -27,6 +27,14 @@
  *       Core/Common/include/itkBSplineKernelFunction.h:152-175
  *       Core/Common/include/itkBSplineDerivativeKernelFunction.h:156-180
  *   - Kahan summation  Core/Common/include/itkCompensatedSummation.hxx:38-48
+ *   - displacement-field transform and the local-support derivative
+ *       Filtering/DisplacementField/include/itkDisplacementFieldTransform.hxx:67-100,520-570
+ *       Filtering/DisplacementField/include/itkDisplacementFieldTransform.h:336-351 (identity Jacobian)
+ *       Core/ImageFunction/include/itkVectorLinearInterpolateImageFunction.hxx:35-105
+ *       Numerics/Optimizersv4/include/itkObjectToObjectMetric.hxx:332-343,444-503
+ *       Registration/Metricsv4/include/itkImageToImageMetricv4GetValueAndDerivativeThreaderBase.hxx:128-172,276-327
+ *       Registration/Metricsv4/include/itkMattesMutualInformationImageToImageMetricv4GetValueAndDerivativeThreader.hxx:139-157,300-351,394-412
+ *       Registration/Metricsv4/include/itkMattesMutualInformationImageToImageMetricv4.hxx:446-495
  *   - Correlation metric
  *       Registration/Metricsv4/include/itkCorrelationImageToImageMetricv4.hxx:69-116
  *       Registration/Metricsv4/include/itkCorrelationImageToImageMetricv4HelperThreader.hxx:58-169
@@ -58,7 +66,7 @@ enum {
   ORC_ERR_OOM = 8
 };
 
-enum { ORC_TRANSFORM_AFFINE = 0, ORC_TRANSFORM_BSPLINE = 1, ORC_TRANSFORM_COMPOSITE = 2 };
+enum { ORC_TRANSFORM_AFFINE = 0, ORC_TRANSFORM_BSPLINE = 1, ORC_TRANSFORM_COMPOSITE = 2, ORC_TRANSFORM_DISPLACEMENT = 3 };
 
 /* Image geometry: x-fastest buffer, start index 0. */
 typedef struct {
@@ -74,7 +82,10 @@ typedef struct {
  * kind BSPLINE: order-3 B-spline over a coefficient grid (3*nper params).
  * kind COMPOSITE: y = affine(bspline(x)); only the B-spline is optimized,
  * which is the [MovingInitialTransform, OutputTransform] queue of
- * ImageRegistrationMethodv4. */
+ * ImageRegistrationMethodv4.
+ * kind DISPLACEMENT: y = x + field(x) (vector linear interpolation, zero
+ * outside the field's buffer); 3 parameters per field voxel, local support:
+ * the derivative is a field over the virtual domain (same geometry). */
 typedef struct {
   int kind;
   /* affine part (active for AFFINE, fixed initial for COMPOSITE) */
@@ -90,6 +101,10 @@ typedef struct {
   double gdir[9];
   double gp2i[9];
   const double *coeff; /* 3*nper, dimension-major, x-fastest inside */
+  /* displacement field */
+  orc_geom fgeom;
+  int64_t nvox;
+  const double *field; /* 3*nvox, voxel-major (x, y, z per voxel), x-fastest voxels */
 } orc_transform;
 
 typedef struct {
@@ -119,6 +134,8 @@ int orc_affine_init(orc_transform *t, const double params12[12], const double ce
 int orc_bspline_init(orc_transform *t, const double fixed18[18], const double *coeff);
 int orc_composite_init(orc_transform *t, const double affine_params12[12], const double affine_center[3],
                        const double fixed18[18], const double *coeff);
+/* fixed18: field size, origin, spacing, direction (row-major) */
+int orc_displacement_init(orc_transform *t, const double fixed18[18], const double *field);
 int64_t orc_transform_nparams(const orc_transform *t);
 /* y = T(x); returns 1 always (identity outside the B-spline valid region) */
 void orc_transform_point(const orc_transform *t, const double x[3], double y[3]);
@@ -146,6 +163,9 @@ int orc_mattes_value_derivative(const orc_inputs *in, const orc_mattes_state *st
  *   COMPOSITE: tparams = 3*nper B-spline coefficients (the optimized part),
  *              tfixed = 18 B-spline fixed parameters, 12 initial-affine
  *              parameters, 3 initial-affine centre (33 values)
+ *   DISPLACEMENT: tparams = 3*voxels field values, tfixed = 18 (field size,
+ *              origin, spacing, direction); the field must share the virtual
+ *              domain's grid (VerifyDisplacementFieldSizeAndPhysicalSpace)
  * Geometry flat encoding (15 doubles): spacing(3), origin(3), direction(9).
  * nthreads: low 16 bits = thread count; bit 16 set = double pixel type
  * (interpolated values are not rounded to float, as for Image<double,N>). */

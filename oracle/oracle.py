@@ -26,6 +26,7 @@ _lib = None
 TRANSFORM_AFFINE = 0
 TRANSFORM_BSPLINE = 1
 TRANSFORM_COMPOSITE = 2
+TRANSFORM_DISPLACEMENT = 3
 
 STATUS_NAMES = {
     0: "OK",
