@@ -10,7 +10,9 @@ in for real volumes.  `--transform bspline` measures the B-spline workload
 instead: [affine, BSplineTransform order 3 over a 4^3 mesh (7^3 control points,
 1029 parameters; `--mesh 5`: 8^3 control points, 1536 parameters)], 192x192x160
 volumes whose moving image carries a seeded smooth displacement (at most 4 mm),
-10 % random sampling.
+10 % random sampling.  `--transform field` measures the local-support path: a
+DisplacementFieldTransform on the dense 192x192x160 virtual grid (5,898,240
+samples, 17.7 M parameters; the derivative is a field of the same size).
 
 Prints one JSON line.  `value` is device-timed throughput with everything
 resident in HBM (CUDA events around each evaluation, L2 flushed between
@@ -44,9 +46,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--transform", default="affine", choices=["affine", "bspline"],
+    ap.add_argument("--transform", default="affine", choices=["affine", "bspline", "field"],
                     help="affine: 256x256x200, 20%% sampling; bspline: [affine, B-spline order 3], "
-                         "192x192x160, 10%% sampling")
+                         "192x192x160, 10%% sampling; field: DisplacementFieldTransform, 192x192x160 dense")
     ap.add_argument("--size", default=None)
     ap.add_argument("--fraction", type=float, default=None)
     ap.add_argument("--mesh", type=int, default=4,
@@ -66,9 +68,9 @@ def parse():
     args = ap.parse_args()
     bs = args.transform == "bspline"
     if args.size is None:
-        args.size = "192,192,160" if bs else "256,256,200"
+        args.size = "192,192,160" if args.transform in ("bspline", "field") else "256,256,200"
     if args.fraction is None:
-        args.fraction = 0.1 if bs else 0.2
+        args.fraction = 1.0 if args.transform == "field" else (0.1 if bs else 0.2)
     return args
 
 
@@ -103,8 +105,22 @@ def itk_points(fixed, fraction, seed):
 
 
 def make_workload(args):
-    from itk_gb300 import BSplineTransform, CompositeTransform, data
+    from itk_gb300 import (BSplineTransform, CompositeTransform, DisplacementFieldImage, DisplacementFieldTransform,
+                           data)
     size = tuple(int(s) for s in args.size.split(","))
+    if args.transform == "field":
+        # dense virtual grid; the field is the generating affine's displacement at every voxel
+        # centre plus a smooth 1 mm perturbation (mid-optimization)
+        fixed, moving, T = data.pair_affine(size, config=1, multimodal_map=(args.metric == "mattes"))
+        grad = data.gradient_image(moving)
+        nx, ny, nz = fixed.GetSize()
+        k = np.arange(nx * ny * nz)
+        x = np.stack([k % nx, (k // nx) % ny, k // (nx * ny)], axis=1) @ fixed.index_to_physical().T + fixed.origin
+        u = (T.TransformPoint(x) - x).reshape(nz, ny, nx, 3)
+        u += data.smooth_displacement_field(fixed, seed=4001, max_disp=1.0).array
+        F = DisplacementFieldTransform()
+        F.SetDisplacementField(DisplacementFieldImage.like(fixed, u))
+        return fixed, moving, grad, None, F
     if args.transform == "bspline":
         # [affine, B-spline] initialised from the generating affine; the B-spline part mid-optimization
         fixed, moving, A, B = data.pair_bspline(size, (args.mesh,) * 3, instance=0,
@@ -133,6 +149,19 @@ def make_workload(args):
 def config_dict(args, n_samples):
     size = [int(s) for s in args.size.split(",")]
     bs = args.transform == "bspline"
+    if args.transform == "field":
+        return {
+            "workload": f"{args.metric}_field_{'x'.join(map(str, size))}_dense_{args.bins}bins",
+            "volume_xyz": size,
+            "samples": int(n_samples),
+            "bins": args.bins if args.metric == "mattes" else None,
+            "sampling": "dense virtual grid (every voxel)",
+            "transform": f"DisplacementFieldTransform<double,3> on the virtual grid ({3 * int(n_samples)} parameters; "
+                         "local support: the derivative is a field)",
+            "gradient": "moving gradient image (packed with the moving image)",
+            "level": "full resolution (shrink 1, sigma 0)",
+            "l2": "flushed between timed steps (256 MiB memset); inputs larger than L2",
+        }
     tname = f"bspline{args.mesh}" if bs else "affine"
     return {
         "workload": f"{args.metric}_{tname}_{'x'.join(map(str, size))}_{int(args.fraction * 100)}pct_{args.bins}bins",
@@ -226,9 +255,15 @@ def cpu_baseline(args, fixed, moving, grad, pts, U, seconds):
     for _ in range(reps):
         run_oracle(kind, fixed, moving, U, gradient=grad, points=pts, bins=args.bins, nthreads=threads)
     dt = time.perf_counter() - t0
-    return {"value": len(pts) * reps / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{reps} full evaluations of the bench workload ({len(pts)} samples each), "
+    n = n_domain(fixed, pts)
+    return {"value": n * reps / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} full evaluations of the bench workload ({n} samples each), "
                       f"{dt:.1f} s, FP64 oracle (oracle/itk_oracle.c), {threads} threads"}
+
+
+def n_domain(fixed, pts):
+    """Samples of one evaluation: the point set, or every voxel of the dense virtual grid."""
+    return fixed.array.size if pts is None else len(pts)
 
 
 def dist_setup():
@@ -260,14 +295,14 @@ def run_reference(args):
     for _ in range(steps):
         run_oracle(kind, fixed, moving, U, gradient=grad, points=pts, bins=args.bins, nthreads=threads)
     dt = time.perf_counter() - t0
-    value = len(pts) * steps / dt / 1e6
+    value = n_domain(fixed, pts) * steps / dt / 1e6
     per["value"] = value
-    per["sample"] = f"{steps} full evaluations ({len(pts)} samples each) after {min(args.warmup, 3)} warm-up, " \
+    per["sample"] = f"{steps} full evaluations ({n_domain(fixed, pts)} samples each) after {min(args.warmup, 3)} warm-up, " \
                     f"FP64 oracle port of the reference algorithm, {threads} threads"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
             "warmup": min(args.warmup, 3), "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict(args, len(pts)), "impl": "reference", "cpu_baseline": per,
+            "config": config_dict(args, n_domain(fixed, pts)), "impl": "reference", "cpu_baseline": per,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -353,6 +388,13 @@ def run_forms_only(args):
     print(json.dumps(line), flush=True)
 
 
+def data_points(fixed):
+    """The dense virtual grid's voxel centres (physical, FP64)."""
+    nx, ny, nz = fixed.GetSize()
+    k = np.arange(nx * ny * nz)
+    return np.stack([k % nx, (k // nx) % ny, k // (nx * ny)], axis=1) @ fixed.index_to_physical().T + fixed.origin
+
+
 def run_gb300(args):
     world, rank, local, dist = dist_setup()
     if args.only_forms:
@@ -372,8 +414,9 @@ def run_gb300(args):
     m.SetMovingImageGradientImage(grad)
     if args.metric == "mattes":
         m.SetNumberOfHistogramBins(args.bins)
-    m.SetVirtualSampledPointSet(pts)
-    m.SetUseSampledPointSet(True)
+    if pts is not None:
+        m.SetVirtualSampledPointSet(pts)
+        m.SetUseSampledPointSet(True)
     t_init = time.perf_counter()
     m.Initialize()
     init_s = time.perf_counter() - t_init
@@ -448,11 +491,21 @@ def run_gb300(args):
         ktimes.append(m.kernel_times_ms())
     m.set_profiling(False)
     ktimes = np.mean(np.array(ktimes), axis=0)
+    field = args.transform == "field"
     # the affine path's constant kernel runs before the first profiling mark
-    kernels_per_eval = len(ktimes) + (0 if bs else 1)
-    v_touched = roofline.touched_voxels(pts, U, moving)
+    kernels_per_eval = len(ktimes) + (0 if (bs or field) else 1)
+    v_touched = roofline.touched_voxels(data_points(fixed) if pts is None else pts, U, moving)
     nodes = (args.mesh + 3) ** 3
-    if bs:
+    if field:
+        # kernel order: MeanSquares; or Mattes pass 1, the value, the derivative blocks
+        kidx = 0
+        if args.metric == "mattes":
+            kbytes = roofline.mattes_pass1_field_bytes(n, v_touched)
+            kname = "k_mattes_pass1_field"
+        else:
+            kbytes = roofline.msq_field_bytes(n, v_touched)
+            kname = "k_msq_field"
+    elif bs:
         # kernel order of the device-resident call: nodes, pass 1 (or MeanSquares), chunks, params
         kidx = 1
         if args.metric == "mattes":
@@ -480,7 +533,7 @@ def run_gb300(args):
             parts = line.split()
             if len(parts) == 3 and parts[0] == wkey and parts[1] == kname:
                 traffic = int(parts[2])
-    b_alg = roofline.evaluation_bytes(n, v_touched, nparams=P)
+    b_alg = roofline.evaluation_bytes(n, v_touched, sparse=pts is not None, nparams=P)
     eval_ms = dev_ms / args.steps
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

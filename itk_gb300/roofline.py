@@ -61,3 +61,23 @@ def mattes_pass1_bytes(n_samples, v_touched):
 def msq_bytes(n_samples, v_touched):
     """Minimal DRAM traffic of the MeanSquares kernel: sample records (16 B) + touched voxels (16 B)."""
     return n_samples * 16 + v_touched * 16
+
+
+def mattes_pass1_field_bytes(n_samples, v_touched):
+    """Minimal DRAM traffic of the Mattes pass-1 kernel under a dense displacement field: the
+    sample record (16 B) and the sample's field value (3 doubles, 24 B) read, the per-sample cache
+    written (16 B), each touched (value, gradient) voxel once (16 B)."""
+    return n_samples * 56 + v_touched * 16
+
+
+def msq_field_bytes(n_samples, v_touched):
+    """Minimal DRAM traffic of the MeanSquares kernel under a dense displacement field: sample
+    record (16 B) and field value (24 B) read, the derivative block (3 doubles, 24 B) written,
+    touched voxels once (16 B)."""
+    return n_samples * 64 + v_touched * 16
+
+
+def mattes_pass2_field_bytes(n_samples):
+    """Minimal DRAM traffic of the Mattes derivative-block kernel under a dense displacement field:
+    cache and sample record read (16 B each), the derivative block written (24 B)."""
+    return n_samples * 56
