@@ -3,8 +3,11 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/itk_gb300.h"
@@ -92,6 +95,34 @@ void shrink_geometry(const int64_t size[3], const double spacing[3], const doubl
                      const int64_t factors[3], int64_t out_size[3], double out_spacing[3], double out_origin[3]);
 
 struct OptState;  // device optimizer state (gb_optimizer.cu)
+
+// body(k0, k1) over [0, n) split across the host's threads (at most 16, at least
+// `grain` items each); the caller's thread runs whatever no new thread could take.
+template <typename F>
+void parallel_ranges(int64_t n, F body, int64_t grain = 16384) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const int64_t T = std::max<int64_t>(1, std::min<int64_t>(hw, n / grain));
+  if (T == 1) {
+    body(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  int64_t started = 0;
+  try {
+    for (; started < T; ++started) th.emplace_back(body, n * started / T, n * (started + 1) / T);
+  } catch (...) {  // no more threads: the rest runs here
+  }
+  for (std::thread& x : th) x.join();
+  if (started < T) body(n * started / T, n);
+}
+
+// memcpy split across the host's threads for large buffers (a displacement
+// field's parameters and derivative are tens to hundreds of MB per call).
+inline void copy_parallel(void* dst, const void* src, size_t bytes) {
+  parallel_ranges((int64_t)bytes, [&](int64_t a, int64_t b) {
+    std::memcpy(static_cast<char*>(dst) + a, static_cast<const char*>(src) + a, (size_t)(b - a));
+  }, (int64_t)4 << 20);
+}
 
 }  // namespace gb
 

@@ -393,7 +393,7 @@ extern "C" int gb_metric_set_parameters(gb_metric* m, const double* params, int6
   if (!m || !params) return fail(GB_ERR_BAD_ARG, "null argument");
   if (m->tkind < 0) return fail(GB_ERR_BAD_ARG, "no moving transform set");
   if ((size_t)nparams != m->tparams.size()) return fail(GB_ERR_BAD_ARG, "parameter count mismatch");
-  std::copy(params, params + nparams, m->tparams.begin());
+  copy_parallel(m->tparams.data(), params, sizeof(double) * (size_t)nparams);
   return GB_OK;
 }
 
@@ -412,7 +412,7 @@ extern "C" int gb_metric_update_transform_parameters(gb_metric* m, const double*
 extern "C" int gb_metric_get_parameters(gb_metric* m, double* params, int64_t nparams) {
   if (!m || !params) return fail(GB_ERR_BAD_ARG, "null argument");
   if ((size_t)nparams != m->tparams.size()) return fail(GB_ERR_BAD_ARG, "parameter count mismatch");
-  std::copy(m->tparams.begin(), m->tparams.end(), params);
+  copy_parallel(params, m->tparams.data(), sizeof(double) * m->tparams.size());
   return GB_OK;
 }
 
@@ -1146,7 +1146,7 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
     for (int64_t n = 0; n < np; ++n) hn[n] = make_float4((float)c[n], (float)c[np + n], (float)c[2 * np + n], 0.f);
   } else if (is_field(m)) {
     // the field (the parameters), staged in pinned memory for the upload
-    std::memcpy(m->h_params, m->tparams.data(), sizeof(double) * P);
+    copy_parallel(m->h_params, m->tparams.data(), sizeof(double) * P);
   } else {
     // per-evaluation constants in FP64 on the host, uploaded with the parameters
     const bool dense = !m->use_sampled;
@@ -1160,8 +1160,7 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
   m->last_status = status;
   m->last_nvalid = (uint64_t)m->h_out[1];
   if (value) *value = m->h_out[0];
-  if (deriv)
-    for (size_t p = 0; p < P; ++p) derivative[p] = m->h_out[2 + p];
+  if (deriv) copy_parallel(derivative, m->h_out + 2, sizeof(double) * P);
   if (status == GB_ERR_NO_VALID_POINTS) {
     if (m->kind == GB_METRIC_MATTES)
       return fail(status,

@@ -61,25 +61,6 @@ struct PointMaker {
   }
 };
 
-// body(k0, k1) over [0, n) split across the host's threads (at most 16).
-template <typename F>
-void parallel_ranges(int64_t n, F body) {
-  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const int64_t T = std::max<int64_t>(1, std::min<int64_t>(hw, n / 16384));
-  if (T == 1) {
-    body(0, n);
-    return;
-  }
-  std::vector<std::thread> th;
-  int64_t started = 0;
-  try {
-    for (; started < T; ++started) th.emplace_back(body, n * started / T, n * (started + 1) / T);
-  } catch (...) {  // no more threads: the rest runs here
-  }
-  for (std::thread& x : th) x.join();
-  if (started < T) body(n * started / T, n);
-}
-
 }  // namespace
 
 }  // namespace gb

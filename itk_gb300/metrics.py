@@ -174,7 +174,8 @@ class ImageToImageMetricv4:
 
     # ---- evaluation
     def _sync_params(self):
-        p = f64(self._transform.GetParameters())
+        view = getattr(self._transform, "parameters_view", None)  # a displacement field: no copy
+        p = view() if view is not None else f64(self._transform.GetParameters())
         if p.size != self._nparams:
             raise ExceptionObject(_capi.GB_ERR_BAD_ARG, "transform parameter count changed; call Initialize()")
         check(self._L.gb_metric_set_parameters(self._h, ptr(p), p.size))
@@ -191,7 +192,7 @@ class ImageToImageMetricv4:
         """Returns (value, derivative) like GetValueAndDerivative(value, derivative)."""
         self._sync_params()
         value = np.zeros(1)
-        deriv = np.zeros(self._nparams)
+        deriv = np.empty(self._nparams)  # every entry is written by the call
         rc = self._L.gb_metric_get_value_and_derivative(self._h, ptr(value), ptr(deriv), self._nparams)
         self._handle_status(rc)
         self._value = float(value[0])

@@ -221,6 +221,11 @@ class DisplacementFieldTransform:
         self._need_field()
         return self.field.array.reshape(-1).copy()
 
+    def parameters_view(self):
+        """The field's buffer as the flat parameter array, without a copy."""
+        self._need_field()
+        return self.field.array.reshape(-1)
+
     def SetParameters(self, p):
         self._need_field()
         p = np.asarray(p, dtype=np.float64).reshape(-1)
@@ -307,6 +312,10 @@ class CompositeTransform:
 
     def GetParameters(self):
         return self.active.GetParameters()
+
+    @property
+    def parameters_view(self):
+        return getattr(self.active, "parameters_view", None)
 
     def SetParameters(self, p):
         self.active.SetParameters(p)
