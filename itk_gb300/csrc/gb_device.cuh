@@ -292,18 +292,6 @@ __device__ __forceinline__ void split_double_bits(double x, float& hi, float& lo
   lo = e < 949 ? 0.f : __uint2float_rn(w0 & 0x1fffffffu) * __uint_as_float(sign | ((unsigned)(e - 948) << 23));
 }
 
-// float -> double by integer operations (exact, as the conversion instruction,
-// which GB300 issues on its slow FP64 pipe): the exponent rebiased, the mantissa
-// widened.  Subnormal floats take the conversion instruction.
-__device__ __forceinline__ double f2d_bits(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
-  if (e == 0u) return (b & 0x7fffffu) ? (double)f : __hiloint2double((int)(b & 0x80000000u), 0);
-  const unsigned m = b & 0x7fffffu;
-  const unsigned ed = e == 255u ? 0x7ffu : e + 896u;
-  return __hiloint2double((int)((b & 0x80000000u) | (ed << 20) | (m >> 3)), (int)(m << 29));
-}
-
 // p + A u for a double-float matrix A and a double-float vector u (products with
 // FMA error terms, sums by two-sum), renormalized.
 __device__ __forceinline__ DFPos df_add_matvec(const DFPos& p, const AffineDF& A, const float uhi[3],

@@ -31,17 +31,16 @@ namespace gb {
 template <int TK>
 __device__ __forceinline__ void field_store(const EvalArgs& a, unsigned voxel, bool ok, float c, float3 g) {
   double* d = a.out + 2 + 3ull * voxel;
-  // FP32 products widened by integer operations (f2d_bits), not on the FP64 pipe
   if (TK == kMapFieldDense) {
     if (!ok && !a.field_full) return;
-    d[0] = f2d_bits(ok ? c * g.x : 0.f);
-    d[1] = f2d_bits(ok ? c * g.y : 0.f);
-    d[2] = f2d_bits(ok ? c * g.z : 0.f);
+    d[0] = ok ? (double)(c * g.x) : 0.0;
+    d[1] = ok ? (double)(c * g.y) : 0.0;
+    d[2] = ok ? (double)(c * g.z) : 0.0;
   } else {
     if (!ok || voxel == ~0u) return;
-    atomicAdd(d, f2d_bits(c * g.x));
-    atomicAdd(d + 1, f2d_bits(c * g.y));
-    atomicAdd(d + 2, f2d_bits(c * g.z));
+    atomicAdd(d, (double)(c * g.x));
+    atomicAdd(d + 1, (double)(c * g.y));
+    atomicAdd(d + 2, (double)(c * g.z));
   }
 }
 
@@ -117,7 +116,10 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass2_field(EvalArgs a) {
     coef = N > 0 ? (float)(-1.0 / (a.m_bs * (double)N)) : 0.f;  // -nFactor, Mattes...v4.hxx:415
   }
   __syncthreads();
-  auto one = [&](int64_t i, const float4& cc, const float4& s) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 cc = __ldcs(a.cache + i);
+    const float4 s = __ldcs(a.samples + i);
     const unsigned voxel = TK == kMapFieldDense
                                ? (unsigned)s.x + (unsigned)a.vnx * ((unsigned)s.y + (unsigned)a.vny * (unsigned)s.z)
                                : __ldg(a.voff + i);
@@ -132,19 +134,6 @@ __global__ void __launch_bounds__(kBlock) k_mattes_pass2_field(EvalArgs a) {
       w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
     }
     field_store<TK>(a, voxel, ok, coef * w, make_float3(cc.y, cc.z, cc.w));
-  };
-  // two samples per thread and step: both records' loads in flight together
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += 2 * stride) {
-    const int64_t j = i + stride;
-    const float4 c0 = __ldcs(a.cache + i), s0 = __ldcs(a.samples + i);
-    float4 c1 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = c1;
-    if (j < a.n) {
-      c1 = __ldcs(a.cache + j);
-      s1 = __ldcs(a.samples + j);
-    }
-    one(i, c0, s0);
-    if (j < a.n) one(j, c1, s1);
   }
 }
 
