@@ -45,7 +45,7 @@ enum {
 
 /* metric kinds; CORRELATION is CorrelationImageToImageMetricv4 (affine transforms)
  * (Registration/Metricsv4/include/itkCorrelationImageToImageMetricv4.hxx) */
-enum { GB_METRIC_MEAN_SQUARES = 0, GB_METRIC_MATTES = 1, GB_METRIC_CORRELATION = 2 };
+enum { GB_METRIC_MEAN_SQUARES = 0, GB_METRIC_MATTES = 1, GB_METRIC_CORRELATION = 2, GB_METRIC_JOINT_HISTOGRAM_MI = 3 };
 /* image slots */
 enum { GB_IMAGE_FIXED = 0, GB_IMAGE_MOVING = 1 };
 /* moving transform kinds (flat encodings below) */
@@ -84,6 +84,10 @@ int gb_metric_destroy(gb_metric *m);
 /* SetNumberOfHistogramBins, clamped to >= 5
  * (itkMattesMutualInformationImageToImageMetricv4.h:146). */
 int gb_metric_set_number_of_histogram_bins(gb_metric *m, uint64_t bins);
+/* JointHistogramMutualInformationImageToImageMetricv4::SetVarianceForJointPDFSmoothing
+ * (default 1.5; <= 0: no smoothing), Registration/Metricsv4/include/itkJointHistogramMutualInformationImageToImageMetricv4.h:141.
+ * The joint-histogram metric takes affine transforms and 6 to 64 bins (default 20). */
+int gb_metric_set_joint_pdf_smoothing_variance(gb_metric *m, double variance);
 
 /* SetFixedImage / SetMovingImage (itkImageToImageMetricv4.h SetFixedImage /
  * SetMovingImage): float voxels, x fastest, size[3] = (nx, ny, nz), start

@@ -3,7 +3,8 @@
 GetValueAndDerivative of MeanSquaresImageToImageMetricv4 and
 MattesMutualInformationImageToImageMetricv4 on Image<float,3> under affine,
 B-spline, [affine, B-spline] composite and displacement-field transforms (and
-CorrelationImageToImageMetricv4 under affine transforms), computed by hand-written
+CorrelationImageToImageMetricv4 and JointHistogramMutualInformationImageToImageMetricv4
+under affine transforms), computed by hand-written
 sm_103a CUDA kernels behind the C ABI in include/itk_gb300.h.
 """
 from ._capi import ExceptionObject, lib, library_path
@@ -12,6 +13,7 @@ from .filters import (GradientRecursiveGaussianImageFilter, ShrinkImageFilter, S
                       shrink_geometry)
 from .image import DisplacementFieldImage, GradientImage, Image
 from .metrics import (CorrelationImageToImageMetricv4, ImageToImageMetricv4,
+                      JointHistogramMutualInformationImageToImageMetricv4,
                       MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4, context)
 from .optimizers import RegularStepGradientDescentOptimizerv4
 from .registration import ImageRegistrationMethodv4, sample_count, sample_points
@@ -23,6 +25,7 @@ __all__ = [
     "AffineTransform", "BSplineTransform", "CompositeTransform", "CorrelationImageToImageMetricv4", "ExceptionObject",
     "DisplacementFieldImage", "DisplacementFieldTransform", "GradientImage",
     "GradientRecursiveGaussianImageFilter", "Image", "ImageRegistrationMethodv4", "ImageToImageMetricv4",
+    "JointHistogramMutualInformationImageToImageMetricv4",
     "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
     "RegistrationBatch", "RegistrationRequest", "RegistrationResult", "RegistrationServer",
     "RegularStepGradientDescentOptimizerv4", "ShrinkImageFilter", "SmoothingRecursiveGaussianImageFilter", "context",

@@ -32,6 +32,7 @@ GB_ERR_ADMISSION = 13
 GB_METRIC_MEAN_SQUARES = 0
 GB_METRIC_MATTES = 1
 GB_METRIC_CORRELATION = 2
+GB_METRIC_JOINT_HISTOGRAM_MI = 3
 GB_IMAGE_FIXED = 0
 GB_IMAGE_MOVING = 1
 GB_TRANSFORM_AFFINE = 0
@@ -86,6 +87,7 @@ SIGNATURES = {
     "gb_metric_create": [_P, _I, _P],
     "gb_metric_destroy": [_P],
     "gb_metric_set_number_of_histogram_bins": [_P, _U64],
+    "gb_metric_set_joint_pdf_smoothing_variance": [_P, _D],
     "gb_metric_set_image": [_P, _I, _P, _P, _P, _P, _P],
     "gb_metric_set_image_device": [_P, _I, _P, _P, _P, _P, _P],
     "gb_metric_set_gradient_source": [_P, _I],

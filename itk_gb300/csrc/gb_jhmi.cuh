@@ -1,0 +1,322 @@
+// gb_jhmi.cuh -- JointHistogramMutualInformationImageToImageMetricv4, affine transforms.
+//
+// Reference (paths under ITK's Modules/Registration/Metricsv4/include/):
+//   Initialize (true min / max over the whole images, joint-PDF geometry)
+//                                  itkJointHistogramMutualInformationImageToImageMetricv4.hxx:70-190
+//   joint histogram, smoothing, marginals (InitializeForIteration)          .hxx:207-303
+//   value (ComputeValue, MI in bits)                                        .hxx:340-378
+//   joint-PDF point                                                         .hxx:389-401
+//   histogram point     itkJointHistogramMutualInformationComputeJointPDFThreaderBase.hxx:57-150
+//   derivative point    itkJointHistogramMutualInformationGetValueAndDerivativeThreader.hxx:41-277
+//
+// Three kernels per evaluation:
+//   k_jhmi_pass1    per sample: moving value (and gradient, cached for pass 2), the
+//                   joint bin of (f, m), an integer count in a shared-memory
+//                   histogram, flushed with 64-bit atomics (order-free, so exact);
+//   k_jhmi_finalize one block: the normalized PDF, the discrete-Gaussian smoothing
+//                   (separable, zero-flux border, moving axis first), the marginals
+//                   by compensated sums, the value; FP32 tables for pass 2;
+//   k_jhmi_pass2    per sample: bilinear PDF value and moving-axis slope, the
+//                   marginal and its slope, the clamped log-slope difference times
+//                   J^T g, fixed-order sums; the last block divides by the count.
+// A joint bin is floor((p - origin) / spacing + 0.5) of p = (v - min) / (max - min):
+// computed in FP32, and again in FP64 exactly as the reference does where the FP32
+// result lies within 1e-4 of a rounding boundary, so every sample lands in the
+// reference's bin.
+#pragma once
+
+#include "gb_kernels.cuh"
+
+namespace gb {
+
+constexpr int kJhmiMaxBins = 64;  // the finalize block keeps two bins^2 FP64 planes in shared memory
+
+// Joint-PDF constants (host-computed in FP64 at Initialize).
+struct JhmiConsts {
+  double fmin, fmax, mmin, mmax;  // true min / max of the whole fixed and moving images
+  double origin, inv_spacing;     // joint-PDF geometry: origin -2 s, 1 / s, s = 1 / (bins - 5)
+  double spacing;
+  float fmin_f, finv_f, mmin_f, minv_f;  // FP32 twins: min, 1 / (max - min)
+  float origin_f, inv_spacing_f, spacing_f;
+  int radius;                            // discrete Gaussian radius (0: no smoothing)
+  double kernel[65];                     // 2 radius + 1 coefficients
+};
+
+// Joint bin along one axis: TransformPhysicalPointToIndex (round half up) of the
+// joint-PDF point; -1 outside [0, bins).
+__device__ __forceinline__ int jhmi_bin(float v, float vmin_f, float vinv_f, double vmin, double vmax,
+                                        const JhmiConsts& C, int B) {
+  const float p = (v - vmin_f) * vinv_f;
+  const float t = fmaf(p - C.origin_f, C.inv_spacing_f, 0.5f);
+  float fl = floorf(t);
+  if (fabsf(t - rintf(t)) < 1e-4f || !(t == t)) {
+    // near a boundary: the reference's FP64 arithmetic
+    const double pd = ((double)v - vmin) / (vmax - vmin);
+    fl = (float)floor((pd - C.origin) * C.inv_spacing + 0.5);
+    if (!(pd == pd)) return -1;
+  }
+  const int b = (int)fl;
+  return (b >= 0 && b < B) ? b : -1;
+}
+
+// k_jhmi_pass1: histogram counts in shared memory (u32), the cache (m, g) for pass 2.
+template <int GRAD>
+__device__ __forceinline__ void jhmi_pass1_body(const EvalArgs& a, const JhmiConsts* __restrict__ gC, VGrid vg) {
+  extern __shared__ unsigned hist_s[];
+  __shared__ EvalConsts K;
+  __shared__ JhmiConsts C;
+  const int B = a.bins;
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) hist_s[k] = 0u;
+  griddep_wait();
+  if (halted(a)) return;
+  griddep_launch_dependents();
+  load_consts(a.consts, K);
+  {
+    const unsigned* src = reinterpret_cast<const unsigned*>(gC);
+    unsigned* dst = reinterpret_cast<unsigned*>(&C);
+    for (int k = threadIdx.x; k < (int)(sizeof(JhmiConsts) / 4); k += blockDim.x) dst[k] = __ldg(src + k);
+  }
+  __syncthreads();
+  unsigned nv = 0;
+  const int64_t stride = (int64_t)vg.n * blockDim.x;
+  for (int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 s = __ldcs(a.samples + i);
+    float m = 0.f;
+    float3 g = make_float3(0.f, 0.f, 0.f);
+    const bool ok = eval_moving<GRAD>(a, map_pos(K.map, s.x, s.y, s.z), a.with_derivative != 0, m, g);
+    if (a.with_derivative)
+      __stcs(a.cache + i, ok ? make_float4(m, g.x, g.y, g.z) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f));
+    if (!ok) continue;
+    const int fb = jhmi_bin(s.w, C.fmin_f, C.finv_f, C.fmin, C.fmax, C, B);
+    const int mb = jhmi_bin(m, C.mmin_f, C.minv_f, C.mmin, C.mmax, C, B);
+    if (fb < 0 || mb < 0) continue;
+    atomicAdd(&hist_s[fb + B * mb], 1u);
+    ++nv;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) {
+    const unsigned h = hist_s[k];
+    if (h) atomicAdd(&a.hist[k], (unsigned long long)h);
+  }
+  block_count(nv, a.acc_n);
+}
+
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock) k_jhmi_pass1(EvalArgs a, const JhmiConsts* C) {
+  jhmi_pass1_body<GRAD>(a, C, hw_grid());
+}
+
+// One thread per output: out[x] = sum_k c[k] in[clamp(x + k - r)] along `dir`
+// (0: the fixed index, contiguous; 1: the moving index), ZeroFluxNeumann border.
+__device__ __forceinline__ void jhmi_gauss_pass(const double* in, double* out, int B, int dir, const JhmiConsts& C) {
+  const int r = C.radius;
+  for (int q = threadIdx.x; q < B * B; q += blockDim.x) {
+    const int i = q % B, j = q / B;
+    double s = 0.0;
+    for (int k = 0; k <= 2 * r; ++k) {
+      int t = (dir == 0 ? i : j) + k - r;
+      t = t < 0 ? 0 : (t > B - 1 ? B - 1 : t);
+      s += C.kernel[k] * (dir == 0 ? in[t + B * j] : in[i + B * t]);
+    }
+    out[q] = s;
+  }
+}
+
+__device__ __forceinline__ void kahan_d(double& s, double& c, double x) {
+  const double y = x - c;
+  const double t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// k_jhmi_finalize: one block.  Writes the smoothed PDF (FP64, pdf_out; FP32 and the
+// FP32 moving marginal into the pratio table), the value, the count and the status.
+__global__ void __launch_bounds__(kBlock) k_jhmi_finalize(EvalArgs a, const JhmiConsts* gC) {
+  extern __shared__ double plane[];  // 2 B^2 doubles, then 2 B (marginals)
+  __shared__ JhmiConsts C;
+  __shared__ double red[kBlock];
+  griddep_wait();
+  if (halted(a)) return;
+  griddep_launch_dependents();
+  const int B = a.bins;
+  {
+    const unsigned* src = reinterpret_cast<const unsigned*>(gC);
+    unsigned* dst = reinterpret_cast<unsigned*>(&C);
+    for (int k = threadIdx.x; k < (int)(sizeof(JhmiConsts) / 4); k += blockDim.x) dst[k] = __ldg(src + k);
+  }
+  double* p0 = plane;
+  double* p1 = plane + B * B;
+  double* fm = plane + 2 * B * B;
+  double* mm = fm + B;
+  const unsigned long long N = __ldcg(a.acc_n);
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x)
+    p0[k] = N > 0 ? (double)__ldcg(&a.hist[k]) / (double)N : 0.0;
+  __syncthreads();
+  double* pdf = p0;
+  if (C.radius > 0) {  // DiscreteGaussianImageFilter: the moving axis, then the fixed axis
+    jhmi_gauss_pass(p0, p1, B, 1, C);
+    __syncthreads();
+    jhmi_gauss_pass(p1, p0, B, 0, C);
+    __syncthreads();
+  }
+  // marginals: moving = sum over the fixed index, fixed = sum over the moving index
+  for (int t = threadIdx.x; t < 2 * B; t += blockDim.x) {
+    double s = 0.0, c = 0.0;
+    if (t < B) {
+      for (int i = 0; i < B; ++i) kahan_d(s, c, pdf[i + B * t]);
+      mm[t] = s;
+    } else {
+      const int i = t - B;
+      for (int j = 0; j < B; ++j) kahan_d(s, c, pdf[i + B * j]);
+      fm[i] = s;
+    }
+  }
+  __syncthreads();
+  // the value: per-thread compensated partials over a fixed bin order, then a fixed-order sum
+  double s = 0.0, c = 0.0;
+  for (int q = threadIdx.x; q < B * B; q += blockDim.x) {
+    const int i = q % B, j = q / B;
+    const double denom = fm[i] * mm[j];
+    const double pxy = pdf[q];
+    double local = 0.0;
+    if (fabs(denom) > DBL_EPSILON && pxy / denom > DBL_EPSILON) local = pxy * log(pxy / denom);
+    kahan_d(s, c, local);
+    a.pdf_out[q] = pxy;
+    a.pratio[q] = (float)pxy;
+  }
+  red[threadIdx.x] = s;
+  for (int j = threadIdx.x; j < B; j += blockDim.x) a.pratio[B * B + j] = (float)mm[j];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0, tc = 0.0;
+    for (int k = 0; k < (int)blockDim.x; ++k) kahan_d(t, tc, red[k]);
+    a.out[1] = (double)N;
+    if (N == 0) {  // GetValue: VerifyNumberOfValidPoints, a warning and the maximum value
+      a.out[0] = DBL_MAX;
+      *a.status = GB_ERR_NO_VALID_POINTS;
+    } else {
+      a.out[0] = -1.0 * t / 0.69314718055994530942;  // / log(2): bits
+      *a.status = GB_OK;
+    }
+  }
+}
+
+// Bilinear value of the FP32 PDF table at a continuous index (LinearInterpolateImageFunction, 2-D).
+__device__ __forceinline__ float jhmi_interp2(const float* t, int B, float cx, float cy) {
+  int x0 = (int)floorf(cx), y0 = (int)floorf(cy);
+  x0 = x0 < 0 ? 0 : x0;
+  y0 = y0 < 0 ? 0 : y0;
+  float dx = cx - (float)x0, dy = cy - (float)y0;
+  int x1 = x0 + 1 <= B - 1 ? x0 + 1 : x0, y1 = y0 + 1 <= B - 1 ? y0 + 1 : y0;
+  if (!(dx > 0.f)) { dx = 0.f; x1 = x0; }
+  if (!(dy > 0.f)) { dy = 0.f; y1 = y0; }
+  const float v00 = t[x0 + B * y0], v10 = t[x1 + B * y0], v01 = t[x0 + B * y1], v11 = t[x1 + B * y1];
+  return lerp(lerp(v00, v10, dx), lerp(v01, v11, dx), dy);
+}
+
+__device__ __forceinline__ float jhmi_interp1(const float* t, int B, float c) {
+  int x0 = (int)floorf(c);
+  x0 = x0 < 0 ? 0 : x0;
+  float d = c - (float)x0;
+  const int x1 = x0 + 1 <= B - 1 ? x0 + 1 : x0;
+  if (!(d > 0.f)) return t[x0];
+  return lerp(t[x0], t[x1], d);
+}
+
+// k_jhmi_pass2: the derivative.  Dynamic shared memory: the B^2 + B FP32 tables.
+template <int GRAD>
+__device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiConsts* __restrict__ gC, VGrid vg) {
+  extern __shared__ float tab[];
+  __shared__ EvalConsts K;
+  __shared__ JhmiConsts C;
+  __shared__ float red[kBlock / 32][13];
+  __shared__ double blk[13], fin[13];
+  const int B = a.bins;
+  griddep_wait();
+  if (halted(a)) return;
+  griddep_launch_dependents();
+  for (int k = threadIdx.x; k < B * B + B; k += blockDim.x) tab[k] = __ldcg(&a.pratio[k]);
+  load_consts(a.consts, K);
+  {
+    const unsigned* src = reinterpret_cast<const unsigned*>(gC);
+    unsigned* dst = reinterpret_cast<unsigned*>(&C);
+    for (int k = threadIdx.x; k < (int)(sizeof(JhmiConsts) / 4); k += blockDim.x) dst[k] = __ldg(src + k);
+  }
+  __syncthreads();
+  const float* pdf = tab;
+  const float* mm = tab + B * B;
+  const float sp = C.spacing_f;
+  const float max_slope = (float)(36.841361487904734 / C.spacing);  // -log(1e-16) / spacing
+  const float inv_scale = (float)(1.0 / (0.69314718055994530942 * (C.mmax - C.mmin)));
+  float acc[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) acc[k] = 0.f;
+  unsigned nv = 0;
+  const int64_t stride = (int64_t)vg.n * blockDim.x;
+  for (int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 cc = __ldcs(a.cache + i);
+    const float m = cc.x;
+    if (!(m == m)) continue;                                  // invalid sample
+    if (m < (float)C.mmin || m > (float)C.mmax) continue;     // outside the moving range
+    const float4 s = __ldcs(a.samples + i);
+    const float pa = (s.w - C.fmin_f) * C.finv_f, pb = (m - C.mmin_f) * C.minv_f;
+    const float ca = (pa - C.origin_f) * C.inv_spacing_f, cb = (pb - C.origin_f) * C.inv_spacing_f;
+    if (!(ca >= -0.5f && ca < (float)B - 0.5f && cb >= -0.5f && cb < (float)B - 0.5f)) continue;
+    const float jv = jhmi_interp2(pdf, B, ca, cb);
+    float l = pb - 0.5f * sp, r = pb + 0.5f * sp;
+    l = fminf(fmaxf(l, sp), 1.f);
+    r = fminf(fmaxf(r, sp), 1.f);
+    float dj = 0.f, dm = 0.f;
+    const float delta = r - l;
+    if (delta > 0.f) {
+      const float cl = (l - C.origin_f) * C.inv_spacing_f, cr = (r - C.origin_f) * C.inv_spacing_f;
+      dj = (jhmi_interp2(pdf, B, ca, cr) - jhmi_interp2(pdf, B, ca, cl)) / delta;
+      dm = (jhmi_interp1(mm, B, cr) - jhmi_interp1(mm, B, cl)) / delta;
+    }
+    const float mv = jhmi_interp1(mm, B, cb);
+    float sf = 0.f;
+    if (jv > 1e-16f && mv > 1e-16f) {
+      const float t1 = fminf(fmaxf(dj / jv, -max_slope), max_slope);
+      const float t2 = fminf(fmaxf(dm / mv, -max_slope), max_slope);
+      sf = (t1 - t2) * inv_scale;
+    }
+    ++nv;
+    const float3 v = jac_vec(K, s.x, s.y, s.z);
+    const float t0 = sf * cc.y, t1 = sf * cc.z, t2 = sf * cc.w;
+    acc[0] = fmaf(t0, v.x, acc[0]); acc[1] = fmaf(t0, v.y, acc[1]); acc[2] = fmaf(t0, v.z, acc[2]);
+    acc[3] = fmaf(t1, v.x, acc[3]); acc[4] = fmaf(t1, v.y, acc[4]); acc[5] = fmaf(t1, v.z, acc[5]);
+    acc[6] = fmaf(t2, v.x, acc[6]); acc[7] = fmaf(t2, v.y, acc[7]); acc[8] = fmaf(t2, v.z, acc[8]);
+    acc[9] += t0; acc[10] += t1; acc[11] += t2;
+  }
+  KahanF kacc[13];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    kacc[k].s = acc[k];
+    kacc[k].c = 0.f;
+  }
+  // the valid count rides along as the 13th sum (exact in FP32 per thread, FP64 across blocks)
+  kacc[12].s = (float)nv;
+  kacc[12].c = 0.f;
+  block_sums<13>(kacc, red, blk);
+  if (!grid_sums<13>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin, vg)) return;
+  if (threadIdx.x == 0) {
+    const double N = fin[12];
+    const int P = a.nparams;
+    a.out[1] = N;
+    if (N == 0.0) {  // VerifyNumberOfValidPoints: a warning, value max, zero derivative
+      a.out[0] = DBL_MAX;
+      for (int p = 0; p < P; ++p) a.out[2 + p] = 0.0;
+      *a.status = GB_ERR_NO_VALID_POINTS;
+      return;
+    }
+    *a.status = GB_OK;
+    for (int p = 0; p < P; ++p) a.out[2 + p] = fin[p] / N;
+  }
+}
+
+template <int GRAD>
+__global__ void __launch_bounds__(kBlock) k_jhmi_pass2(EvalArgs a, const JhmiConsts* C) {
+  jhmi_pass2_body<GRAD>(a, C, hw_grid());
+}
+
+}  // namespace gb

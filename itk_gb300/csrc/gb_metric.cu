@@ -13,6 +13,7 @@
 
 #include "gb_bspline.cuh"
 #include "gb_field.cuh"
+#include "gb_jhmi.cuh"
 #include "gb_init.cuh"
 #include "gb_internal.h"
 #include "gb_kernels.cuh"
@@ -120,6 +121,80 @@ static bool is_bspline(const gb_metric* m) {
 
 static bool is_field(const gb_metric* m) { return m->tkind == GB_TRANSFORM_DISPLACEMENT_FIELD; }
 
+// Modified Bessel functions of the first kind: Abramowitz & Stegun 9.8.1-9.8.4 for
+// orders 0 and 1, Miller's downward recurrence normalized by I0 for n >= 2 (the
+// published algorithm GaussianOperator uses, Core/Common/include/itkGaussianOperator.hxx:60-180).
+static double bessel_i0(double y) {
+  const double d = std::fabs(y);
+  if (d < 3.75) {
+    double t = y / 3.75;
+    t *= t;
+    return 1.0 + t * (3.5156229 + t * (3.0899424 + t * (1.2067492 + t * (0.2659732 + t * (0.0360768 + t * 0.0045813)))));
+  }
+  const double t = 3.75 / d;
+  return (std::exp(d) / std::sqrt(d)) *
+         (0.39894228 + t * (0.01328592 + t * (0.00225319 + t * (-0.00157565 + t * (0.00916281 +
+          t * (-0.02057706 + t * (0.02635537 + t * (-0.01647633 + t * 0.00392377))))))));
+}
+
+static double bessel_i1(double y) {
+  const double d = std::fabs(y);
+  double r;
+  if (d < 3.75) {
+    double t = y / 3.75;
+    t *= t;
+    r = d * (0.5 + t * (0.87890594 + t * (0.51498869 + t * (0.15084934 + t * (0.02658733 +
+                                                                               t * (0.00301532 + t * 0.00032411))))));
+  } else {
+    const double t = 3.75 / d;
+    double q = 0.02282967 + t * (-0.02895312 + t * (0.01787654 - t * 0.00420059));
+    q = 0.39894228 + t * (-0.03988024 + t * (-0.00362018 + t * (0.00163801 + t * (-0.01031555 + t * q))));
+    r = q * (std::exp(d) / std::sqrt(d));
+  }
+  return y < 0.0 ? -r : r;
+}
+
+static double bessel_in(int n, double y) {
+  if (y == 0.0) return 0.0;
+  const double tox = 2.0 / std::fabs(y);
+  double bip = 0.0, bi = 1.0, ans = 0.0;
+  for (int j = 2 * (n + (int)std::sqrt(40.0 * n)); j > 0; j--) {
+    const double bim = bip + j * tox * bi;
+    bip = bi;
+    bi = bim;
+    if (std::fabs(bi) > 1.0e10) {
+      ans *= 1.0e-10;
+      bi *= 1.0e-10;
+      bip *= 1.0e-10;
+    }
+    if (j == n) ans = bip;
+  }
+  ans *= bessel_i0(y) / bi;
+  return (y < 0.0 && (n & 1)) ? -ans : ans;
+}
+
+// GaussianOperator::GenerateCoefficients (itkGaussianOperator.hxx:27-57): e^-v I_k(v)
+// until the two-sided sum reaches 1 - max_error or the width limit, normalized,
+// mirrored into c[0, 2r]; returns r (at most 32).
+static int discrete_gaussian_kernel(double variance, double max_error, int max_width, double c[65]) {
+  double half[34];
+  const double et = std::exp(-variance);
+  int n = 0;
+  half[n++] = et * bessel_i0(variance);
+  double sum = half[0];
+  half[n++] = et * bessel_i1(variance);
+  sum += half[1] * 2.0;
+  for (int i = 2; sum < 1.0 - max_error && n < 34; ++i) {
+    half[n++] = et * bessel_in(i, variance);
+    sum += half[i] * 2.0;
+    if (half[i] <= 0.0 || n > max_width) break;
+  }
+  for (int i = 0; i < n; ++i) half[i] /= sum;
+  const int r = n - 1;
+  for (int i = 0; i <= r; ++i) c[r + i] = c[r - i] = half[i];
+  return r;
+}
+
 // Initial affine of a B-spline path: the composite's first transform ([affine,
 // B-spline] queue, B-spline applied first), the identity for a plain B-spline.
 static void bspline_init_affine(const gb_metric* m, double p[12], double c[3]) {
@@ -191,12 +266,14 @@ extern "C" int gb_ctx_info(gb_ctx* ctx, int* sm_count, uint64_t* total_bytes, ui
 
 extern "C" int gb_metric_create(gb_ctx* ctx, int kind, gb_metric** out) {
   if (!ctx || !out) return fail(GB_ERR_BAD_ARG, "null argument");
-  if (kind != GB_METRIC_MEAN_SQUARES && kind != GB_METRIC_MATTES && kind != GB_METRIC_CORRELATION)
+  if (kind != GB_METRIC_MEAN_SQUARES && kind != GB_METRIC_MATTES && kind != GB_METRIC_CORRELATION &&
+      kind != GB_METRIC_JOINT_HISTOGRAM_MI)
     return fail(GB_ERR_BAD_ARG, "unknown metric kind");
   GB_CUDA(cudaSetDevice(ctx->device));
   gb_metric* m = new gb_metric;
   m->ctx = ctx;
   m->kind = kind;
+  if (kind == GB_METRIC_JOINT_HISTOGRAM_MI) m->bins = 20;  // the joint-histogram metric's default
   cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost(&m->h_status, sizeof(int) * 4);
   if (e != cudaSuccess) {
@@ -211,7 +288,7 @@ void gb_metric::release_buffers() {
   d_fixed.reset(); d_moving.reset(); d_fixed_s.reset(); d_moving_s.reset(); d_grad_in.reset();
   d_mov4.reset(); d_samples.reset(); d_cache.reset(); d_sup.reset(); d_chunks.reset();
   d_node_first.reset(); d_node_entries.reset(); d_chunk_part.reset(); d_nodes.reset(); d_voff.reset();
-  d_params.reset(); d_acc.reset(); d_scratch.reset(); d_out.reset(); d_status.reset(); d_pratio.reset(); d_pdf.reset();
+  d_jhmi.reset(); d_params.reset(); d_acc.reset(); d_scratch.reset(); d_out.reset(); d_status.reset(); d_pratio.reset(); d_pdf.reset();
   d_consts.reset(); d_opt.reset(); d_opt_vec.reset();
 }
 
@@ -232,6 +309,14 @@ extern "C" int gb_metric_destroy(gb_metric* m) {
     if (m->events[i]) cudaEventDestroy(m->events[i]);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
+  return GB_OK;
+}
+
+extern "C" int gb_metric_set_joint_pdf_smoothing_variance(gb_metric* m, double variance) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  if (!(variance == variance)) return fail(GB_ERR_BAD_ARG, "variance is NaN");
+  m->jhmi_variance = variance;
+  m->initialized = false;
   return GB_OK;
 }
 
@@ -432,7 +517,7 @@ static size_t acc_offset_hist() { return 8 + (sizeof(unsigned) * kTicketCount + 
 static size_t acc_offset_fmarg(int64_t B) { return acc_offset_hist() + 8 * (size_t)(B * B); }
 static size_t acc_offset_colsum(int64_t B) { return acc_offset_fmarg(B) + 8 * (size_t)B; }
 static size_t acc_layout_bytes(const gb_metric* m) {
-  const int64_t B = m->kind == GB_METRIC_MATTES ? m->bins : 0;
+  const int64_t B = (m->kind == GB_METRIC_MATTES || m->kind == GB_METRIC_JOINT_HISTOGRAM_MI) ? m->bins : 0;
   return acc_offset_colsum(B) + 8 * (size_t)B;
 }
 
@@ -448,6 +533,11 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   const bool field = is_field(m);
   if ((bspline || field) && m->kind == GB_METRIC_CORRELATION)
     return fail(GB_ERR_UNSUPPORTED, "the correlation metric runs affine transforms");
+  const bool jhmi = m->kind == GB_METRIC_JOINT_HISTOGRAM_MI;
+  if (jhmi && m->tkind != GB_TRANSFORM_AFFINE)
+    return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric runs affine transforms");
+  if (jhmi && (m->bins < 6 || m->bins > kJhmiMaxBins))
+    return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric takes 6 to 64 bins");
   double g_p2i[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   if (bspline) {
     // BSplineTransform fixed parameters: grid size, origin, spacing, direction (itkBSplineTransform.hxx:243-283)
@@ -579,6 +669,46 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     m->mstate[6] = fmin / m->mstate[4] - padding;
     m->mstate[5] = (mmax - mmin) / (double)(m->bins - 2 * 2);
     m->mstate[7] = mmin / m->mstate[5] - padding;
+  }
+
+  // ---- joint-histogram MI: true min / max over the whole level images, joint-PDF
+  // geometry, smoothing kernel (itkJointHistogramMutualInformationImageToImageMetricv4.hxx:70-190)
+  if (jhmi) {
+    DevBuf<int> d_mm;
+    GB_CUDA(d_mm.alloc_on(m->stream, 4));
+    int init[4] = {float_to_ordered_host(FLT_MAX), float_to_ordered_host(-FLT_MAX), float_to_ordered_host(FLT_MAX),
+                   float_to_ordered_host(-FLT_MAX)};
+    GB_CUDA(cudaMemcpyAsync(d_mm.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    k_minmax<<<grid_for(m, m->fixed.voxels(), 4), kBlock, 0, st>>>(m->fixed_img(), m->fixed.voxels(), d_mm.p);
+    k_minmax<<<grid_for(m, m->moving.voxels(), 4), kBlock, 0, st>>>(m->moving_img(), m->moving.voxels(), d_mm.p + 2);
+    GB_CUDA(cudaGetLastError());
+    int res[4];
+    GB_CUDA(cudaMemcpyAsync(res, d_mm.p, sizeof(res), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    JhmiConsts C;
+    std::memset(&C, 0, sizeof(C));
+    C.fmin = (double)ordered_to_float_host(res[0]);
+    C.fmax = (double)ordered_to_float_host(res[1]);
+    C.mmin = (double)ordered_to_float_host(res[2]);
+    C.mmax = (double)ordered_to_float_host(res[3]);
+    C.spacing = 1.0 / (double)(m->bins - 2 * 2 - 1);
+    C.origin = C.spacing * 2.0 * -1.0;
+    C.inv_spacing = 1.0 / C.spacing;
+    C.fmin_f = (float)C.fmin;
+    C.finv_f = (float)(1.0 / (C.fmax - C.fmin));
+    C.mmin_f = (float)C.mmin;
+    C.minv_f = (float)(1.0 / (C.mmax - C.mmin));
+    C.origin_f = (float)C.origin;
+    C.inv_spacing_f = (float)C.inv_spacing;
+    C.spacing_f = (float)C.spacing;
+    C.radius = m->jhmi_variance > 0.0 ? discrete_gaussian_kernel(m->jhmi_variance, 0.01, 32, C.kernel) : 0;
+    m->mstate[0] = C.fmin;
+    m->mstate[1] = C.fmax;
+    m->mstate[2] = C.mmin;
+    m->mstate[3] = C.mmax;
+    GB_CUDA(m->d_jhmi.alloc_on(m->stream, sizeof(JhmiConsts)));
+    GB_CUDA(cudaMemcpyAsync(m->d_jhmi.p, &C, sizeof(C), cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaStreamSynchronize(st));  // C lives on this stack frame
   }
 
   // ---- sample list: fixed values / bins in FP64, spatial sort
@@ -735,15 +865,16 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   m->d_out.reset();
   GB_CUDA(m->d_out.alloc_on(m->stream, 2 + P));
   GB_CUDA(m->d_status.alloc_on(m->stream, 1));
-  if (m->kind == GB_METRIC_MATTES) {
-    m->d_pratio.reset();
-    GB_CUDA(m->d_pratio.alloc_on(m->stream, (size_t)(m->bins * m->bins)));
+  if (m->kind == GB_METRIC_MATTES || jhmi) {
+    m->d_pratio.reset();  // log(p / pm) table; the joint-histogram metric: FP32 PDF and moving marginal
+    GB_CUDA(m->d_pratio.alloc_on(m->stream, (size_t)(m->bins * m->bins + m->bins)));
     m->d_pdf.reset();
     GB_CUDA(m->d_pdf.alloc_on(m->stream, (size_t)(m->bins * m->bins)));
     GB_CUDA(cudaMemsetAsync(m->d_pdf.p, 0, sizeof(double) * m->bins * m->bins, st));
   }
   m->d_cache.reset();
-  if (m->kind == GB_METRIC_MATTES || bspline) GB_CUDA(m->d_cache.alloc_on(m->stream, std::max<int64_t>(1, m->nsamples)));
+  if (m->kind == GB_METRIC_MATTES || jhmi || bspline)
+    GB_CUDA(m->d_cache.alloc_on(m->stream, std::max<int64_t>(1, m->nsamples)));
   if (m->h_cap < 2 + P) {  // pinned staging, reused while large enough (cudaFreeHost waits for the device)
     if (m->h_params) cudaFreeHost(m->h_params);
     if (m->h_out) cudaFreeHost(m->h_out);
@@ -885,11 +1016,11 @@ static cudaError_t launch_chain(gb_metric* m, void (*kernel)(KArgs...), unsigned
 }
 
 // Grid-stride evaluation kernel with `smem` bytes of dynamic shared memory, one full wave.
-template <typename K>
-static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalArgs& a) {
+template <typename K, typename... Extra>
+static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalArgs& a, Extra... extra) {
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  return launch_chain(m, kernel, (unsigned)full_wave(m, kernel, smem, m->nsamples), kBlock, smem, a);
+  return launch_chain(m, kernel, (unsigned)full_wave(m, kernel, smem, m->nsamples), kBlock, smem, a, extra...);
 }
 
 // B-spline / composite evaluation: node conversion (large grids), the per-sample
@@ -990,6 +1121,28 @@ static int enqueue_eval_field(gb_metric* m, const EvalArgs& a, bool cd, bool der
   return GB_OK;
 }
 
+// Joint-histogram MI: the histogram pass, the one-block PDF / value kernel, the
+// derivative pass.
+static int enqueue_eval_jhmi(gb_metric* m, const EvalArgs& a, bool cd, bool deriv) {
+  const int B = (int)m->bins;
+  const JhmiConsts* C = reinterpret_cast<const JhmiConsts*>(m->d_jhmi.p);
+  const size_t sh1 = sizeof(unsigned) * B * B;
+  GB_CUDA(cd ? launch_wave(m, k_jhmi_pass1<kGradCentralDifference>, sh1, a, C)
+             : launch_wave(m, k_jhmi_pass1<kGradImage>, sh1, a, C));
+  m->mark();
+  const size_t shf = sizeof(double) * (2 * B * B + 2 * B);
+  GB_CUDA(cudaFuncSetAttribute(k_jhmi_finalize, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shf));
+  GB_CUDA(launch_chain(m, k_jhmi_finalize, 1, kBlock, shf, a, C));
+  m->mark();
+  if (deriv) {
+    const size_t sh2 = sizeof(float) * (B * B + B);
+    GB_CUDA(cd ? launch_wave(m, k_jhmi_pass2<kGradCentralDifference>, sh2, a, C)
+               : launch_wave(m, k_jhmi_pass2<kGradImage>, sh2, a, C));
+    m->mark();
+  }
+  return GB_OK;
+}
+
 // Enqueues one evaluation; results land in d_out = [value, nvalid, derivative...].
 // device_params: the parameters are in device memory (d_params), so the affine
 // constants or the B-spline nodes are formed on the device; otherwise the host
@@ -1015,6 +1168,7 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
   m->mark();
   if (is_bspline(m)) return enqueue_eval_bspline(m, a, cd, deriv, device_params);
   if (is_field(m)) return enqueue_eval_field(m, a, cd, deriv);
+  if (m->kind == GB_METRIC_JOINT_HISTOGRAM_MI) return enqueue_eval_jhmi(m, a, cd, deriv);
   if (m->kind == GB_METRIC_CORRELATION) {
     // averages, then the value and derivative (at most kCorrMaxBlocks blocks: 27 partials each)
     GB_CUDA(cd ? launch_wave(m, k_corr_mean_affine<kGradCentralDifference>, 0, a)
@@ -1200,7 +1354,8 @@ extern "C" int gb_metric_get_number_of_domain_points(gb_metric* m, uint64_t* n) 
 
 extern "C" int gb_metric_get_joint_pdf(gb_metric* m, double* out, int64_t n) {
   if (!m || !out) return fail(GB_ERR_BAD_ARG, "null argument");
-  if (m->kind != GB_METRIC_MATTES) return fail(GB_ERR_BAD_ARG, "joint PDF exists for the Mattes metric only");
+  if (m->kind != GB_METRIC_MATTES && m->kind != GB_METRIC_JOINT_HISTOGRAM_MI)
+    return fail(GB_ERR_BAD_ARG, "joint PDF exists for the Mattes and joint-histogram metrics only");
   if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
   if (n != m->bins * m->bins) return fail(GB_ERR_BAD_ARG, "joint PDF size must be bins*bins");
   GB_CUDA(cudaSetDevice(m->ctx->device));
@@ -1220,6 +1375,7 @@ size_t gb_metric::device_bytes() const {
   return d_fixed.bytes() + d_moving.bytes() + d_fixed_s.bytes() + d_moving_s.bytes() + d_grad_in.bytes() +
          d_mov4.bytes() + d_samples.bytes() + d_cache.bytes() + d_sup.bytes() + d_chunks.bytes() +
          d_node_first.bytes() + d_node_entries.bytes() + d_chunk_part.bytes() + d_nodes.bytes() + d_voff.bytes() +
+         d_jhmi.bytes() +
          d_params.bytes() +
          d_acc.bytes() + d_scratch.bytes() + d_out.bytes() + d_status.bytes() + d_pratio.bytes() + d_pdf.bytes() +
          d_consts.bytes() + d_opt.bytes() + d_opt_vec.bytes();

@@ -283,6 +283,43 @@ class CorrelationImageToImageMetricv4(ImageToImageMetricv4):
     _kind = _capi.GB_METRIC_CORRELATION
 
 
+class JointHistogramMutualInformationImageToImageMetricv4(ImageToImageMetricv4):
+    """Joint-histogram mutual information (value -MI in bits): counts of (fixed, moving)
+    intensity bins over the valid points, normalized and smoothed by a discrete
+    Gaussian; the derivative from the smoothed PDF's slope along the moving axis
+    (affine transforms; default 20 bins, variance 1.5)."""
+
+    _kind = _capi.GB_METRIC_JOINT_HISTOGRAM_MI
+
+    def __init__(self, device: int = 0):
+        super().__init__(device)
+        self._bins = 20
+        self._variance = 1.5
+
+    def SetNumberOfHistogramBins(self, bins: int):
+        self._bins = max(int(bins), 5)  # itkSetClampMacro(..., 5, max)
+
+    def GetNumberOfHistogramBins(self):
+        return self._bins
+
+    def SetVarianceForJointPDFSmoothing(self, variance: float):
+        self._variance = float(variance)
+
+    def GetVarianceForJointPDFSmoothing(self):
+        return self._variance
+
+    def _pre_initialize(self):
+        check(self._L.gb_metric_set_number_of_histogram_bins(self._h, self._bins))
+        check(self._L.gb_metric_set_joint_pdf_smoothing_variance(self._h, self._variance))
+
+    def GetJointPDF(self):
+        """The smoothed joint PDF of the last evaluation as the reference's image buffer
+        (fixed bin fastest): out[moving bin, fixed bin]."""
+        out = np.zeros((self._bins, self._bins))
+        check(self._L.gb_metric_get_joint_pdf(self._h, ptr(out), out.size))
+        return out
+
+
 class MattesMutualInformationImageToImageMetricv4(ImageToImageMetricv4):
     """Mattes mutual information with cubic B-spline Parzen windows (default 50 bins)."""
 

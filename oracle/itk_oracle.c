@@ -1474,3 +1474,434 @@ int orc_central_difference_flat(const float *img, const int64_t size[3], const d
   for (int64_t i = 0; i < n; ++i) orc_central_difference(&g, img, points + 3 * i, grads + 3 * i);
   return ORC_OK;
 }
+
+/* ------------------------------------------------------------------ */
+/* JointHistogramMutualInformationImageToImageMetricv4                 */
+/* ------------------------------------------------------------------ */
+
+/* Modified Bessel functions of the first kind for the discrete Gaussian kernel
+ * (GaussianOperator, Core/Common/include/itkGaussianOperator.hxx:27-180): the
+ * polynomial approximations of Abramowitz & Stegun 9.8.1-9.8.4 for orders 0
+ * and 1, and Miller's downward recurrence (normalized by I0) for order n >= 2,
+ * as published in Numerical Recipes (bessi, accuracy parameter 40, rescaling
+ * at 1e10). */
+static double bessel_i0(double y)
+{
+  const double d = fabs(y);
+  if (d < 3.75) {
+    double t = y / 3.75;
+    t *= t;
+    return 1.0 + t * (3.5156229 + t * (3.0899424 + t * (1.2067492 + t * (0.2659732 + t * (0.0360768 + t * 0.0045813)))));
+  }
+  const double t = 3.75 / d;
+  return (exp(d) / sqrt(d)) *
+         (0.39894228 + t * (0.01328592 + t * (0.00225319 + t * (-0.00157565 + t * (0.00916281 +
+          t * (-0.02057706 + t * (0.02635537 + t * (-0.01647633 + t * 0.00392377))))))));
+}
+
+static double bessel_i1(double y)
+{
+  const double d = fabs(y);
+  double r;
+  if (d < 3.75) {
+    double t = y / 3.75;
+    t *= t;
+    r = d * (0.5 + t * (0.87890594 + t * (0.51498869 + t * (0.15084934 + t * (0.02658733 + t * (0.00301532 +
+                                                                                               t * 0.00032411))))));
+  } else {
+    const double t = 3.75 / d;
+    double q = 0.02282967 + t * (-0.02895312 + t * (0.01787654 - t * 0.00420059));
+    q = 0.39894228 + t * (-0.03988024 + t * (-0.00362018 + t * (0.00163801 + t * (-0.01031555 + t * q))));
+    r = q * (exp(d) / sqrt(d));
+  }
+  return y < 0.0 ? -r : r;
+}
+
+static double bessel_in(int n, double y)
+{
+  if (y == 0.0) return 0.0;
+  const double tox = 2.0 / fabs(y);
+  double bip = 0.0, bi = 1.0, ans = 0.0;
+  for (int j = 2 * (n + (int)sqrt(40.0 * n)); j > 0; j--) {
+    const double bim = bip + j * tox * bi;
+    bip = bi;
+    bi = bim;
+    if (fabs(bi) > 1.0e10) {
+      ans *= 1.0e-10;
+      bi *= 1.0e-10;
+      bip *= 1.0e-10;
+    }
+    if (j == n) ans = bip;
+  }
+  ans *= bessel_i0(y) / bi;
+  return (y < 0.0 && (n & 1)) ? -ans : ans;
+}
+
+/* GaussianOperator::GenerateCoefficients: e^-v I_k(v) for k = 0, 1, ... until the
+ * two-sided sum reaches 1 - max_error (or the width limit), normalized by that
+ * sum, mirrored.  Returns the radius; c holds 2 r + 1 coefficients. */
+int orc_gaussian_kernel(double variance, double max_error, int max_width, double *c, int cap)
+{
+  double half[64];
+  const double et = exp(-variance);
+  int n = 0;
+  half[n++] = et * bessel_i0(variance);
+  double sum = half[0];
+  half[n++] = et * bessel_i1(variance);
+  sum += half[1] * 2.0;
+  const double limit = 1.0 - max_error;
+  for (int i = 2; sum < limit && n < 64; ++i) {
+    half[n++] = et * bessel_in(i, variance);
+    sum += half[i] * 2.0;
+    if (half[i] <= 0.0) break;
+    if (n > max_width) break;
+  }
+  for (int i = 0; i < n; ++i) half[i] /= sum;
+  const int r = n - 1;
+  if (2 * r + 1 > cap) return -1;
+  for (int i = 0; i <= r; ++i) {
+    c[r + i] = half[i];
+    c[r - i] = half[i];
+  }
+  return r;
+}
+
+/* One separable pass of DiscreteGaussianImageFilter over a bins x bins image
+ * along axis `dir` (0: the fixed index, x fastest; 1: the moving index), zero-flux
+ * Neumann boundary (ZeroFluxNeumannBoundaryCondition: indices clamped), the
+ * neighbourhood inner product in operator order. */
+static void gauss_pass(const double *in, double *out, int64_t B, int dir, const double *c, int r)
+{
+  for (int64_t j = 0; j < B; ++j)
+    for (int64_t i = 0; i < B; ++i) {
+      double s = 0.0;
+      for (int k = 0; k <= 2 * r; ++k) {
+        int64_t q = (dir == 0 ? i : j) + k - r;
+        q = q < 0 ? 0 : (q > B - 1 ? B - 1 : q);
+        s += c[k] * (dir == 0 ? in[q + B * j] : in[i + B * q]);
+      }
+      out[i + B * j] = s;
+    }
+}
+
+/* LinearInterpolateImageFunction on the bins x bins joint PDF (2-D path) and the
+ * 1-D marginal, at a continuous index; neighbours clamped as in 3-D. */
+static double interp2(const double *img, int64_t B, const double ci[2])
+{
+  int64_t b0[2], b1[2];
+  double d[2];
+  for (int k = 0; k < 2; ++k) {
+    int64_t f = (int64_t)floor(ci[k]);
+    if (f < 0) f = 0;
+    double dist = ci[k] - (double)f;
+    b0[k] = f;
+    b1[k] = f + 1 <= B - 1 ? f + 1 : f;
+    if (!(dist > 0.0)) { dist = 0.0; b1[k] = f; }
+    d[k] = dist;
+  }
+  const double v00 = img[b0[0] + B * b0[1]], v10 = img[b1[0] + B * b0[1]];
+  const double v01 = img[b0[0] + B * b1[1]], v11 = img[b1[0] + B * b1[1]];
+  if (d[0] <= 0.0 && d[1] <= 0.0) return v00;
+  const double x0 = v00 + (v10 - v00) * d[0];
+  const double x1 = v01 + (v11 - v01) * d[0];
+  return x0 + (x1 - x0) * d[1];
+}
+
+static double interp1(const double *v, int64_t B, double ci)
+{
+  int64_t f = (int64_t)floor(ci);
+  if (f < 0) f = 0;
+  double dist = ci - (double)f;
+  int64_t g = f + 1 <= B - 1 ? f + 1 : f;
+  if (!(dist > 0.0)) return v[f];
+  return v[f] + (v[g] - v[f]) * dist;
+}
+
+/* Initialize: true min / max over the whole fixed and moving images
+ * (itkJointHistogramMutualInformationImageToImageMetricv4.hxx:70-135), joint PDF
+ * geometry: spacing 1 / (bins - 2 padding - 1), origin -padding * spacing
+ * (.hxx:147-163). */
+int orc_jhmi_initialize(const orc_inputs *in, int64_t bins, double variance, orc_jhmi_state *st)
+{
+  if (bins < 6) return ORC_ERR_BAD_ARG;
+  st->bins = bins;
+  st->variance = variance;
+  double fmin = (double)FLT_MAX, fmax = -(double)FLT_MAX, mmin = (double)FLT_MAX, mmax = -(double)FLT_MAX;
+  const int64_t nf = in->fixed_geom.size[0] * in->fixed_geom.size[1] * in->fixed_geom.size[2];
+  for (int64_t i = 0; i < nf; ++i) {
+    const double v = (double)in->fixed[i];
+    fmin = v < fmin ? v : fmin;
+    fmax = v > fmax ? v : fmax;
+  }
+  const int64_t nm = in->moving_geom.size[0] * in->moving_geom.size[1] * in->moving_geom.size[2];
+  for (int64_t i = 0; i < nm; ++i) {
+    const double v = (double)in->moving[i];
+    mmin = v < mmin ? v : mmin;
+    mmax = v > mmax ? v : mmax;
+  }
+  st->fmin = fmin;
+  st->fmax = fmax;
+  st->mmin = mmin;
+  st->mmax = mmax;
+  st->spacing = 1.0 / (double)(bins - 2 * 2 - 1);
+  st->origin = st->spacing * 2.0 * -1.0;
+  st->inv_spacing = 1.0 / st->spacing; /* PhysicalPointToIndex of the diagonal joint-PDF geometry */
+  return ORC_OK;
+}
+
+/* ComputeJointPDFPoint (.hxx:389-401) */
+static inline void jhmi_point(const orc_jhmi_state *st, double f, double m, double p[2])
+{
+  p[0] = (f - st->fmin) / (st->fmax - st->fmin);
+  p[1] = (m - st->mmin) / (st->mmax - st->mmin);
+}
+
+typedef struct {
+  const orc_inputs *in;
+  const orc_transform *t;
+  const orc_jhmi_state *st;
+  int64_t begin, end;
+  /* pass 1 */
+  uint64_t *hist;
+  uint64_t count;
+  /* pass 2 */
+  const double *pdf, *mmarg;
+  double *dsum, *dcomp;
+  uint64_t nvalid;
+  int64_t nparams;
+} jhmi_job;
+
+/* JointHistogramMutualInformationComputeJointPDFThreaderBase::ProcessPoint
+ * (...ComputeJointPDFThreaderBase.hxx:57-104): valid fixed and moving values,
+ * TransformPhysicalPointToIndex on the joint histogram, count inside it. */
+static void *jhmi_hist_worker(void *arg)
+{
+  jhmi_job *j = (jhmi_job *)arg;
+  const int64_t B = j->st->bins;
+  point_eval pe;
+  for (int64_t i = j->begin; i < j->end; ++i) {
+    double vp[3];
+    domain_point(j->in, i, vp);
+    if (!evaluate_point(j->in, j->t, vp, 0, &pe)) continue;
+    double p[2];
+    jhmi_point(j->st, pe.fixed_value, pe.moving_value, p);
+    int64_t idx[2];
+    int inside = 1;
+    for (int k = 0; k < 2; ++k) {
+      const double s = (p[k] - j->st->origin) * j->st->inv_spacing;
+      idx[k] = (int64_t)floor(s + 0.5);
+      if (!(s == s) || idx[k] < 0 || idx[k] >= B) inside = 0;
+    }
+    if (!inside) continue;
+    j->hist[idx[0] + B * idx[1]]++;
+    j->count++;
+  }
+  return NULL;
+}
+
+/* JointHistogramMutualInformationGetValueAndDerivativeThreader::ProcessPoint and
+ * its PDF derivatives (...GetValueAndDerivativeThreader.hxx:94-277). */
+static void *jhmi_deriv_worker(void *arg)
+{
+  jhmi_job *j = (jhmi_job *)arg;
+  const orc_jhmi_state *st = j->st;
+  const int64_t B = st->bins;
+  const double s = st->spacing, eps = 1.0e-16;
+  const double max_slope = -log(eps) / s;
+  const double mrange = st->mmax - st->mmin;
+  const double log2 = log(2.0);
+  point_eval pe;
+  sparse_row row;
+  for (int64_t i = j->begin; i < j->end; ++i) {
+    double vp[3];
+    domain_point(j->in, i, vp);
+    if (!evaluate_point(j->in, j->t, vp, 1, &pe)) continue;
+    if (pe.moving_value < st->mmin || pe.moving_value > st->mmax) continue;
+    double p[2];
+    jhmi_point(st, pe.fixed_value, pe.moving_value, p);
+    double ci[2];
+    int inside = 1;
+    for (int k = 0; k < 2; ++k) {
+      ci[k] = (p[k] - st->origin) * st->inv_spacing;
+      if (!(ci[k] >= -0.5 && ci[k] < (double)B - 0.5)) inside = 0;
+    }
+    if (!inside) continue;
+    const double jv = interp2(j->pdf, B, ci);
+    /* ComputeJointPDFDerivative along the moving axis: +-0.5 spacing, clamped to [spacing, 1] */
+    double l = p[1] - 0.5 * s, r = p[1] + 0.5 * s;
+    l = l < s ? s : (l > 1.0 ? 1.0 : l);
+    r = r < s ? s : (r > 1.0 ? 1.0 : r);
+    double dj = 0.0;
+    if (r - l > 0.0) {
+      const double cl[2] = {ci[0], (l - st->origin) * st->inv_spacing};
+      const double cr[2] = {ci[0], (r - st->origin) * st->inv_spacing};
+      dj = (interp2(j->pdf, B, cr) - interp2(j->pdf, B, cl)) / (r - l);
+    }
+    const double mv = interp1(j->mmarg, B, ci[1]);
+    double dm = 0.0;
+    if (r - l > 0.0)
+      dm = (interp1(j->mmarg, B, (r - st->origin) * st->inv_spacing) -
+            interp1(j->mmarg, B, (l - st->origin) * st->inv_spacing)) / (r - l);
+    double sf = 0.0;
+    if (jv > eps && mv > eps) {
+      double t1 = dj / jv, t2 = dm / mv;
+      t1 = t1 < -max_slope ? -max_slope : (t1 > max_slope ? max_slope : t1);
+      t2 = t2 < -max_slope ? -max_slope : (t2 > max_slope ? max_slope : t2);
+      sf = (t1 - t2) / (log2 * mrange);
+    }
+    j->nvalid++;
+    jacobian_product(j->t, &pe, &row);
+    for (int e = 0; e < row.count; ++e) kahan_add(&j->dsum[row.idx[e]], &j->dcomp[row.idx[e]], sf * row.val[e]);
+  }
+  return NULL;
+}
+
+int orc_jhmi_value_derivative(const orc_inputs *in, const orc_jhmi_state *st, const orc_transform *t,
+                              int compute_derivative, double *value, double *derivative, uint64_t *nvalid,
+                              double *joint_pdf)
+{
+  const int64_t n = domain_size(in);
+  const int64_t P = orc_transform_nparams(t);
+  const int64_t B = st->bins;
+  if (n < 1) return ORC_ERR_BAD_ARG;
+  if (t->kind == ORC_TRANSFORM_DISPLACEMENT) return ORC_ERR_BAD_ARG; /* global-support transforms only here */
+  const int T = resolve_threads(in->nthreads, n);
+  jhmi_job *jobs = (jhmi_job *)calloc((size_t)T, sizeof(jhmi_job));
+  pthread_t *th = (pthread_t *)calloc((size_t)T, sizeof(pthread_t));
+  double *pdf = (double *)calloc((size_t)(B * B), sizeof(double));
+  double *tmp = (double *)calloc((size_t)(B * B), sizeof(double));
+  double *fmarg = (double *)calloc((size_t)B, sizeof(double));
+  double *mmarg = (double *)calloc((size_t)B, sizeof(double));
+  int rc = (jobs && th && pdf && tmp && fmarg && mmarg) ? ORC_OK : ORC_ERR_OOM;
+  const int64_t chunk = (n + T - 1) / T;
+  for (int k = 0; rc == ORC_OK && k < T; ++k) {
+    jobs[k].in = in;
+    jobs[k].t = t;
+    jobs[k].st = st;
+    jobs[k].begin = k * chunk < n ? k * chunk : n;
+    jobs[k].end = (k + 1) * chunk < n ? (k + 1) * chunk : n;
+    jobs[k].nparams = P;
+    jobs[k].hist = (uint64_t *)calloc((size_t)(B * B), sizeof(uint64_t));
+    if (!jobs[k].hist) rc = ORC_ERR_OOM;
+  }
+  uint64_t count = 0;
+  if (rc == ORC_OK) {
+    /* InitializeForIteration (.hxx:207-303): the joint histogram, normalized ... */
+    for (int k = 0; k < T; ++k) pthread_create(&th[k], NULL, jhmi_hist_worker, &jobs[k]);
+    for (int k = 0; k < T; ++k) pthread_join(th[k], NULL);
+    for (int k = 0; k < T; ++k) count += jobs[k].count;
+    if (count > 0)
+      for (int64_t q = 0; q < B * B; ++q) {
+        uint64_t h = 0;
+        for (int k = 0; k < T; ++k) h += jobs[k].hist[q];
+        pdf[q] = (double)h / (double)count;
+      }
+    /* ... smoothed by DiscreteGaussianImageFilter (variance, maximum error 0.01, no
+     * image spacing; the moving axis first, then the fixed axis) ... */
+    if (st->variance > 0.0) {
+      double c[129];
+      const int r = orc_gaussian_kernel(st->variance, 0.01, 32, c, 129);
+      if (r < 0) {
+        rc = ORC_ERR_BAD_ARG;
+      } else {
+        gauss_pass(pdf, tmp, B, 1, c, r);
+        gauss_pass(tmp, pdf, B, 0, c, r);
+      }
+    }
+    /* ... and its marginals by compensated sums: the moving marginal over the fixed
+     * index, the fixed marginal over the moving index */
+    for (int64_t jj = 0; jj < B; ++jj) {
+      double s = 0.0, cc = 0.0;
+      for (int64_t ii = 0; ii < B; ++ii) kahan_add(&s, &cc, pdf[ii + B * jj]);
+      mmarg[jj] = s;
+    }
+    for (int64_t ii = 0; ii < B; ++ii) {
+      double s = 0.0, cc = 0.0;
+      for (int64_t jj = 0; jj < B; ++jj) kahan_add(&s, &cc, pdf[ii + B * jj]);
+      fmarg[ii] = s;
+    }
+  }
+  /* ComputeValue (.hxx:340-378) */
+  double mi = 0.0;
+  if (rc == ORC_OK) {
+    const double eps = DBL_EPSILON;
+    double s = 0.0, cc = 0.0;
+    for (int64_t ii = 0; ii < B; ++ii) {
+      const double px = fmarg[ii];
+      for (int64_t jj = 0; jj < B; ++jj) {
+        const double py = mmarg[jj];
+        const double denom = px * py;
+        const double pxy = pdf[ii + B * jj];
+        double local = 0.0;
+        if (fabs(denom) > eps && pxy / denom > eps) local = pxy * log(pxy / denom);
+        kahan_add(&s, &cc, local);
+      }
+    }
+    mi = -1.0 * s / log(2.0);
+  }
+  if (rc == ORC_OK && !compute_derivative) {
+    /* GetValue (.hxx:309-330): the histogram count is the number of valid points */
+    *nvalid = count;
+    if (count == 0) {
+      *value = DBL_MAX;
+      rc = ORC_ERR_NO_VALID_POINTS;
+    } else {
+      *value = mi;
+    }
+  } else if (rc == ORC_OK) {
+    for (int k = 0; k < T && rc == ORC_OK; ++k) {
+      jobs[k].pdf = pdf;
+      jobs[k].mmarg = mmarg;
+      jobs[k].dsum = (double *)calloc((size_t)P, sizeof(double));
+      jobs[k].dcomp = (double *)calloc((size_t)P, sizeof(double));
+      if (!jobs[k].dsum || !jobs[k].dcomp) rc = ORC_ERR_OOM;
+    }
+    if (rc == ORC_OK) {
+      for (int k = 0; k < T; ++k) pthread_create(&th[k], NULL, jhmi_deriv_worker, &jobs[k]);
+      for (int k = 0; k < T; ++k) pthread_join(th[k], NULL);
+      uint64_t nv = 0;
+      for (int k = 0; k < T; ++k) nv += jobs[k].nvalid;
+      *nvalid = nv;
+      for (int64_t p = 0; p < P; ++p) {
+        double s = 0.0, cc = 0.0;
+        for (int k = 0; k < T; ++k) kahan_add(&s, &cc, jobs[k].dsum[p]);
+        derivative[p] = nv > 0 ? s / (double)nv : 0.0;
+      }
+      if (nv == 0) {
+        *value = DBL_MAX; /* VerifyNumberOfValidPoints: a warning, value max, zero derivative */
+        rc = ORC_ERR_NO_VALID_POINTS;
+      } else {
+        *value = mi;
+      }
+    }
+  }
+  if (joint_pdf && pdf) memcpy(joint_pdf, pdf, sizeof(double) * (size_t)(B * B));
+  for (int k = 0; jobs && k < T; ++k) { free(jobs[k].hist); free(jobs[k].dsum); free(jobs[k].dcomp); }
+  free(jobs);
+  free(th);
+  free(pdf);
+  free(tmp);
+  free(fmarg);
+  free(mmarg);
+  return rc;
+}
+
+int orc_jhmi_flat_v(const float *fixed, const int64_t fsize[3], const double fgeo[15], const float *moving,
+                    const int64_t msize[3], const double mgeo[15], const double *moving_grad, const float *points,
+                    int64_t npoints, int tkind, const double *tparams, int64_t nparams, const double *tfixed,
+                    int64_t nfixed, int64_t bins, double variance, int nthreads, int compute_derivative,
+                    double *value, double *derivative, uint64_t *nvalid, double *joint_pdf, const int64_t *vsize,
+                    const double *vgeo)
+{
+  orc_inputs in;
+  orc_transform t;
+  orc_jhmi_state st;
+  int rc = inputs_from_flat(&in, fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, nthreads,
+                            vsize, vgeo);
+  if (rc) return rc;
+  rc = orc_transform_from_flat(&t, tkind, tparams, nparams, tfixed, nfixed);
+  if (rc) return rc;
+  rc = orc_jhmi_initialize(&in, bins, variance, &st);
+  if (rc) return rc;
+  return orc_jhmi_value_derivative(&in, &st, &t, compute_derivative, value, derivative, nvalid, joint_pdf);
+}

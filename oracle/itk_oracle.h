@@ -35,6 +35,12 @@
  *       Registration/Metricsv4/include/itkImageToImageMetricv4GetValueAndDerivativeThreaderBase.hxx:128-172,276-327
  *       Registration/Metricsv4/include/itkMattesMutualInformationImageToImageMetricv4GetValueAndDerivativeThreader.hxx:139-157,300-351,394-412
  *       Registration/Metricsv4/include/itkMattesMutualInformationImageToImageMetricv4.hxx:446-495
+ *   - JointHistogram mutual information
+ *       Registration/Metricsv4/include/itkJointHistogramMutualInformationImageToImageMetricv4.hxx:70-401
+ *       Registration/Metricsv4/include/itkJointHistogramMutualInformationComputeJointPDFThreaderBase.hxx:57-150
+ *       Registration/Metricsv4/include/itkJointHistogramMutualInformationGetValueAndDerivativeThreader.hxx:41-277
+ *       Core/Common/include/itkGaussianOperator.hxx:27-180 (kernel; Abramowitz & Stegun 9.8.1-9.8.4 Bessel
+ *       approximations, Numerical Recipes' downward recurrence), Filtering/Smoothing/include/itkDiscreteGaussianImageFilter.hxx:152-300
  *   - Correlation metric
  *       Registration/Metricsv4/include/itkCorrelationImageToImageMetricv4.hxx:69-116
  *       Registration/Metricsv4/include/itkCorrelationImageToImageMetricv4HelperThreader.hxx:58-169
@@ -239,6 +245,29 @@ int orc_corr_flat_v(const float *fixed, const int64_t fsize[3], const double fge
                     int64_t npoints, int tkind, const double *tparams, int64_t nparams, const double *tfixed,
                     int64_t nfixed, int nthreads, int compute_derivative, double *value, double *derivative,
                     uint64_t *nvalid, const int64_t *vsize, const double *vgeo);
+
+/* JointHistogramMutualInformationImageToImageMetricv4: joint histogram of
+ * (fixed, moving) bins, normalized, smoothed by a discrete Gaussian, MI in bits;
+ * derivative from the smoothed PDF's moving-axis slope (flat inputs as
+ * orc_msq_flat_v; joint_pdf = the smoothed bins x bins PDF, fixed index fastest,
+ * or NULL).  Global-support transforms. */
+typedef struct {
+  int64_t bins;
+  double variance;
+  double fmin, fmax, mmin, mmax;
+  double spacing, origin, inv_spacing;
+} orc_jhmi_state;
+int orc_gaussian_kernel(double variance, double max_error, int max_width, double *c, int cap);
+int orc_jhmi_initialize(const orc_inputs *in, int64_t bins, double variance, orc_jhmi_state *st);
+int orc_jhmi_value_derivative(const orc_inputs *in, const orc_jhmi_state *st, const orc_transform *t,
+                              int compute_derivative, double *value, double *derivative, uint64_t *nvalid,
+                              double *joint_pdf);
+int orc_jhmi_flat_v(const float *fixed, const int64_t fsize[3], const double fgeo[15], const float *moving,
+                    const int64_t msize[3], const double mgeo[15], const double *moving_grad, const float *points,
+                    int64_t npoints, int tkind, const double *tparams, int64_t nparams, const double *tfixed,
+                    int64_t nfixed, int64_t bins, double variance, int nthreads, int compute_derivative,
+                    double *value, double *derivative, uint64_t *nvalid, double *joint_pdf, const int64_t *vsize,
+                    const double *vgeo);
 
 /* ---- metric sample points (itk_oracle_sampling.c) ---------------------- */
 /* MT19937 32-bit outputs after `skip` draws from a fresh seed */

@@ -65,6 +65,9 @@ def lib():
         L.orc_msq_flat_v.argtypes = L.orc_msq_flat.argtypes + [P, P]
         L.orc_corr_flat_v.argtypes = L.orc_msq_flat_v.argtypes
         L.orc_mattes_flat_v.argtypes = L.orc_mattes_flat.argtypes + [P, P]
+        L.orc_jhmi_flat_v.argtypes = [P, P, P, P, P, P, P, P, i64, ctypes.c_int, P, i64, P, i64, i64,
+                                      ctypes.c_double, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]
+        L.orc_gaussian_kernel.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, P, ctypes.c_int]
         L.orc_transform_point_flat.argtypes = [ctypes.c_int, P, i64, P, i64, P, i64, P]
         L.orc_interpolate_flat.argtypes = [P, P, P, P, i64, P, P]
         L.orc_central_difference_flat.argtypes = [P, P, P, P, i64, P]
@@ -179,6 +182,37 @@ def correlation(fixed, fgeom, moving, mgeom, transform, moving_grad=None, points
                            _threads(nthreads, pixel_double), int(compute_derivative), _p(value), _p(deriv),
                            _p(nvalid), _p(vs), _p(vg))
     return rc, float(value[0]), deriv, int(nvalid[0])
+
+
+def joint_histogram_mi(fixed, fgeom, moving, mgeom, transform, bins=20, variance=1.5, moving_grad=None, points=None,
+                       nthreads=None, compute_derivative=True, pixel_double=False, virtual_geom=None):
+    """JointHistogramMutualInformationImageToImageMetricv4.  Returns (status, value,
+    derivative, nvalid, smoothed joint PDF [moving bin, fixed bin])."""
+    L = lib()
+    fixed, moving = _img(fixed), _img(moving)
+    mg, pts = _grad(moving_grad), _pts(points)
+    tp = np.ascontiguousarray(transform.params, dtype=np.float64)
+    tf = np.ascontiguousarray(transform.fixed, dtype=np.float64)
+    value = np.zeros(1, np.float64)
+    deriv = np.zeros(tp.size, np.float64)
+    nvalid = np.zeros(1, np.uint64)
+    pdf = np.zeros((bins, bins), np.float64)
+    fs, fg, ms, mgeo = fgeom.size_array(), fgeom.flat(), mgeom.size_array(), mgeom.flat()
+    vs, vg = _vgeom(virtual_geom)
+    rc = L.orc_jhmi_flat_v(_p(fixed), _p(fs), _p(fg), _p(moving), _p(ms), _p(mgeo), _p(mg), _p(pts),
+                           0 if pts is None else pts.shape[0], transform.kind, _p(tp), tp.size, _p(tf), tf.size,
+                           int(bins), float(variance), _threads(nthreads, pixel_double), int(compute_derivative),
+                           _p(value), _p(deriv), _p(nvalid), _p(pdf), _p(vs), _p(vg))
+    return rc, float(value[0]), deriv, int(nvalid[0]), pdf
+
+
+def gaussian_kernel(variance, max_error=0.01, max_width=32):
+    """GaussianOperator coefficients (2 r + 1 values)."""
+    c = np.zeros(129, np.float64)
+    r = lib().orc_gaussian_kernel(float(variance), float(max_error), int(max_width), _p(c), 129)
+    if r < 0:
+        raise ValueError("kernel too wide")
+    return c[:2 * r + 1].copy()
 
 
 def mattes(fixed, fgeom, moving, mgeom, transform, bins=50, moving_grad=None, points=None, nthreads=None,
