@@ -36,6 +36,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Mattes-MI value+deriv Msamples/s"
+
+
+def metric_name(args):
+    """The headline metric for Mattes; the same throughput named for the other metrics."""
+    return {"mattes": METRIC, "msq": "MeanSquares value+deriv Msamples/s",
+            "jhmi": "JointHistogram-MI value+deriv Msamples/s"}[args.metric]
 UNIT = "Msamples/s"
 L2_FLUSH_BYTES = 256 << 20
 
@@ -54,8 +60,9 @@ def parse():
     ap.add_argument("--mesh", type=int, default=4,
                     help="B-spline mesh size per axis: 4 = 7^3 control points (1029 parameters), "
                          "5 = 8^3 control points (1536 parameters)")
-    ap.add_argument("--bins", type=int, default=50)
-    ap.add_argument("--metric", default="mattes", choices=["mattes", "msq"])
+    ap.add_argument("--bins", type=int, default=None, help="histogram bins: 50 for Mattes, 20 for jhmi")
+    ap.add_argument("--metric", default="mattes", choices=["mattes", "msq", "jhmi"],
+                    help="jhmi: JointHistogramMutualInformationImageToImageMetricv4 (affine transform only)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms-paths", default="plain,loop",
@@ -67,6 +74,10 @@ def parse():
                          "'' to skip")
     args = ap.parse_args()
     bs = args.transform == "bspline"
+    if args.bins is None:
+        args.bins = 20 if args.metric == "jhmi" else 50
+    if args.metric == "jhmi" and args.transform != "affine":
+        ap.error("--metric jhmi runs the affine transform")
     if args.size is None:
         args.size = "192,192,160" if args.transform in ("bspline", "field") else "256,256,200"
     if args.fraction is None:
@@ -111,7 +122,7 @@ def make_workload(args):
     if args.transform == "field":
         # dense virtual grid; the field is the generating affine's displacement at every voxel
         # centre plus a smooth 1 mm perturbation (mid-optimization)
-        fixed, moving, T = data.pair_affine(size, config=1, multimodal_map=(args.metric == "mattes"))
+        fixed, moving, T = data.pair_affine(size, config=1, multimodal_map=(args.metric in ("mattes", "jhmi")))
         grad = data.gradient_image(moving)
         nx, ny, nz = fixed.GetSize()
         k = np.arange(nx * ny * nz)
@@ -124,7 +135,7 @@ def make_workload(args):
     if args.transform == "bspline":
         # [affine, B-spline] initialised from the generating affine; the B-spline part mid-optimization
         fixed, moving, A, B = data.pair_bspline(size, (args.mesh,) * 3, instance=0,
-                                                multimodal_map=(args.metric == "mattes"))
+                                                multimodal_map=(args.metric in ("mattes", "jhmi")))
         grad = data.gradient_image(moving)
         pts = itk_points(fixed, args.fraction, 2001)
         Bm = BSplineTransform()
@@ -134,7 +145,7 @@ def make_workload(args):
         U.AddTransform(A)
         U.AddTransform(Bm)
         return fixed, moving, grad, pts, U
-    fixed, moving, T = data.pair_affine(size, config=1, multimodal_map=(args.metric == "mattes"))
+    fixed, moving, T = data.pair_affine(size, config=1, multimodal_map=(args.metric in ("mattes", "jhmi")))
     grad = data.gradient_image(moving)
     pts = itk_points(fixed, args.fraction, 1001)
     # evaluate at a transform near (not at) the truth, as mid-optimization
@@ -154,7 +165,7 @@ def config_dict(args, n_samples):
             "workload": f"{args.metric}_field_{'x'.join(map(str, size))}_dense_{args.bins}bins",
             "volume_xyz": size,
             "samples": int(n_samples),
-            "bins": args.bins if args.metric == "mattes" else None,
+            "bins": args.bins if args.metric in ("mattes", "jhmi") else None,
             "sampling": "dense virtual grid (every voxel)",
             "transform": f"DisplacementFieldTransform<double,3> on the virtual grid ({3 * int(n_samples)} parameters; "
                          "local support: the derivative is a field)",
@@ -167,7 +178,7 @@ def config_dict(args, n_samples):
         "workload": f"{args.metric}_{tname}_{'x'.join(map(str, size))}_{int(args.fraction * 100)}pct_{args.bins}bins",
         "volume_xyz": size,
         "samples": int(n_samples),
-        "bins": args.bins if args.metric == "mattes" else None,
+        "bins": args.bins if args.metric in ("mattes", "jhmi") else None,
         "sampling": f"RANDOM {args.fraction:.0%}, ImageRegistrationMethodv4's points (seeded Mersenne Twister)",
         "transform": (f"CompositeTransform [AffineTransform, BSplineTransform order 3, mesh {args.mesh}^3 "
                       f"({(args.mesh + 3) ** 3} nodes, {3 * (args.mesh + 3) ** 3} parameters)]")
@@ -246,7 +257,7 @@ def cpu_baseline(args, fixed, moving, grad, pts, U, seconds):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from cases import run_oracle
     threads = os.cpu_count() or 1
-    kind = "mattes" if args.metric == "mattes" else "msq"
+    kind = args.metric
     t0 = time.perf_counter()
     run_oracle(kind, fixed, moving, U, gradient=grad, points=pts, bins=args.bins, nthreads=threads)
     one = time.perf_counter() - t0
@@ -286,7 +297,7 @@ def run_reference(args):
     # steps of the reference arm: a bounded number of full evaluations
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from cases import run_oracle
-    kind = "mattes" if args.metric == "mattes" else "msq"
+    kind = args.metric
     threads = os.cpu_count() or 1
     for _ in range(min(args.warmup, 3)):
         run_oracle(kind, fixed, moving, U, gradient=grad, points=pts, bins=args.bins, nthreads=threads)
@@ -299,7 +310,7 @@ def run_reference(args):
     per["value"] = value
     per["sample"] = f"{steps} full evaluations ({n_domain(fixed, pts)} samples each) after {min(args.warmup, 3)} warm-up, " \
                     f"FP64 oracle port of the reference algorithm, {threads} threads"
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+    line = {"metric": metric_name(args), "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
             "warmup": min(args.warmup, 3), "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_dict(args, n_domain(fixed, pts)), "impl": "reference", "cpu_baseline": per,
@@ -401,18 +412,20 @@ def run_gb300(args):
         return run_forms_only(args) if rank == 0 else None
     import torch
 
-    from itk_gb300 import (MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4, context,
+    from itk_gb300 import (JointHistogramMutualInformationImageToImageMetricv4,
+                           MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4, context,
                            roofline)
     torch.cuda.set_device(local)
     context(local)
     fixed, moving, grad, pts, U = workload(args)
-    cls = MattesMutualInformationImageToImageMetricv4 if args.metric == "mattes" else MeanSquaresImageToImageMetricv4
+    cls = {"mattes": MattesMutualInformationImageToImageMetricv4, "msq": MeanSquaresImageToImageMetricv4,
+           "jhmi": JointHistogramMutualInformationImageToImageMetricv4}[args.metric]
     m = cls(device=local)
     m.SetFixedImage(fixed)
     m.SetMovingImage(moving)
     m.SetMovingTransform(U)
     m.SetMovingImageGradientImage(grad)
-    if args.metric == "mattes":
+    if args.metric in ("mattes", "jhmi"):
         m.SetNumberOfHistogramBins(args.bins)
     if pts is not None:
         m.SetVirtualSampledPointSet(pts)
@@ -516,7 +529,10 @@ def run_gb300(args):
             kname = "k_msq_bspline"
     else:
         kidx = 0
-        if args.metric == "mattes":
+        if args.metric == "jhmi":
+            kbytes = roofline.jhmi_pass1_bytes(n, v_touched)
+            kname = "k_jhmi_pass1"
+        elif args.metric == "mattes":
             kbytes = roofline.mattes_pass1_bytes(n, v_touched)
             kname = "k_mattes_pass1_affine"
         else:
@@ -536,7 +552,7 @@ def run_gb300(args):
     b_alg = roofline.evaluation_bytes(n, v_touched, sparse=pts is not None, nparams=P)
     eval_ms = dev_ms / args.steps
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": metric_name(args), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": eval_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args, n),
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",

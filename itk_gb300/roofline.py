@@ -81,3 +81,9 @@ def mattes_pass2_field_bytes(n_samples):
     """Minimal DRAM traffic of the Mattes derivative-block kernel under a dense displacement field:
     cache and sample record read (16 B each), the derivative block written (24 B)."""
     return n_samples * 56
+
+
+def jhmi_pass1_bytes(n_samples, v_touched):
+    """Minimal DRAM traffic of the joint-histogram MI pass 1: sample records (16 B) read, the
+    per-sample cache (moving value and gradient, 16 B) written, touched voxels once (16 B)."""
+    return n_samples * 32 + v_touched * 16

@@ -22,9 +22,14 @@ def oracle_transform(t):
 
 def run_oracle(metric_kind, fixed, moving, transform, gradient=None, points=None, bins=50, nthreads=None,
                compute_derivative=True, pixel_double=False):
-    """metric_kind: 'msq' or 'mattes'.  Returns dict(status, value, derivative, nvalid[, pdf, state])."""
+    """metric_kind: 'msq', 'mattes' or 'jhmi' (variance 1.5).  Returns dict(status, value, derivative, nvalid[, pdf, state])."""
     g = None if gradient is None else gradient.array
     T = oracle_transform(transform)
+    if metric_kind == "jhmi":
+        rc, v, d, nv, pdf = O.joint_histogram_mi(fixed.array, geom(fixed), moving.array, geom(moving), T,
+                                                 bins=bins, moving_grad=g, points=points, nthreads=nthreads,
+                                                 compute_derivative=compute_derivative, pixel_double=pixel_double)
+        return dict(status=rc, value=v, derivative=d, nvalid=nv, pdf=pdf)
     if metric_kind == "msq":
         rc, v, d, nv = O.mean_squares(fixed.array, geom(fixed), moving.array, geom(moving), T, moving_grad=g,
                                       points=points, nthreads=nthreads, compute_derivative=compute_derivative,
