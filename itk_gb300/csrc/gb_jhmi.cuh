@@ -134,7 +134,7 @@ __device__ __forceinline__ void kahan_d(double& s, double& c, double x) {
 __global__ void __launch_bounds__(kBlock) k_jhmi_finalize(EvalArgs a, const JhmiConsts* gC) {
   extern __shared__ double plane[];  // 2 B^2 doubles, then 2 B (marginals)
   __shared__ JhmiConsts C;
-  __shared__ double red[kBlock];
+  __shared__ double red[kBlock / 32];
   griddep_wait();
   if (halted(a)) return;
   griddep_launch_dependents();
@@ -172,24 +172,26 @@ __global__ void __launch_bounds__(kBlock) k_jhmi_finalize(EvalArgs a, const Jhmi
     }
   }
   __syncthreads();
-  // the value: per-thread compensated partials over a fixed bin order, then a fixed-order sum
-  double s = 0.0, c = 0.0;
+  // the value: per-thread sums over a fixed bin order, a fixed XOR tree per warp, the
+  // warps in order (short FP64 dependency chains: GB300's FP64 pipe is slow)
+  double s = 0.0;
   for (int q = threadIdx.x; q < B * B; q += blockDim.x) {
     const int i = q % B, j = q / B;
     const double denom = fm[i] * mm[j];
     const double pxy = pdf[q];
     double local = 0.0;
     if (fabs(denom) > DBL_EPSILON && pxy / denom > DBL_EPSILON) local = pxy * log(pxy / denom);
-    kahan_d(s, c, local);
+    s += local;
     a.pdf_out[q] = pxy;
     a.pratio[q] = (float)pxy;
   }
-  red[threadIdx.x] = s;
+  s = warp_sum_d(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
   for (int j = threadIdx.x; j < B; j += blockDim.x) a.pratio[B * B + j] = (float)mm[j];
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0, tc = 0.0;
-    for (int k = 0; k < (int)blockDim.x; ++k) kahan_d(t, tc, red[k]);
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
     a.out[1] = (double)N;
     if (N == 0) {  // GetValue: VerifyNumberOfValidPoints, a warning and the maximum value
       a.out[0] = DBL_MAX;
@@ -248,6 +250,7 @@ __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiCon
   const float sp = C.spacing_f;
   const float max_slope = (float)(36.841361487904734 / C.spacing);  // -log(1e-16) / spacing
   const float inv_scale = (float)(1.0 / (0.69314718055994530942 * (C.mmax - C.mmin)));
+  const float mlo = (float)C.mmin, mhi = (float)C.mmax;  // exact: the true min / max are float values
   float acc[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k] = 0.f;
@@ -257,7 +260,7 @@ __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiCon
     const float4 cc = __ldcs(a.cache + i);
     const float m = cc.x;
     if (!(m == m)) continue;                                  // invalid sample
-    if (m < (float)C.mmin || m > (float)C.mmax) continue;     // outside the moving range
+    if (m < mlo || m > mhi) continue;                         // outside the moving range
     const float4 s = __ldcs(a.samples + i);
     const float pa = (s.w - C.fmin_f) * C.finv_f, pb = (m - C.mmin_f) * C.minv_f;
     const float ca = (pa - C.origin_f) * C.inv_spacing_f, cb = (pb - C.origin_f) * C.inv_spacing_f;
