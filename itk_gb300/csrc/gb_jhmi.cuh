@@ -13,7 +13,7 @@
 //   k_jhmi_pass1    per sample: moving value (and gradient, cached for pass 2), the
 //                   joint bin of (f, m), an integer count in a shared-memory
 //                   histogram, flushed with 64-bit atomics (order-free, so exact);
-//   k_jhmi_finalize one block: the normalized PDF, the discrete-Gaussian smoothing
+//   k_jhmi_finalize a few blocks: the normalized PDF, the discrete-Gaussian smoothing
 //                   (separable, zero-flux border, moving axis first), the marginals
 //                   by compensated sums, the value; FP32 tables for pass 2;
 //   k_jhmi_pass2    per sample: bilinear PDF value and moving-axis slope, the
@@ -29,7 +29,8 @@
 
 namespace gb {
 
-constexpr int kJhmiMaxBins = 64;  // the finalize block keeps two bins^2 FP64 planes in shared memory
+constexpr int kJhmiMaxBins = 64;  // the finalize blocks keep two bins^2 FP64 planes in shared memory
+constexpr int kJhmiFinalizeBlocks = 8;
 
 // Joint-PDF constants (host-computed in FP64 at Initialize).
 struct JhmiConsts {
@@ -129,7 +130,7 @@ __device__ __forceinline__ void kahan_d(double& s, double& c, double x) {
   s = t;
 }
 
-// k_jhmi_finalize: one block.  Writes the smoothed PDF (FP64, pdf_out; FP32 and the
+// k_jhmi_finalize (kJhmiFinalizeBlocks blocks).  Writes the smoothed PDF (FP64, pdf_out; FP32 and the
 // FP32 moving marginal into the pratio table), the value, the count and the status.
 __global__ void __launch_bounds__(kBlock) k_jhmi_finalize(EvalArgs a, const JhmiConsts* gC) {
   extern __shared__ double plane[];  // 2 B^2 doubles, then 2 B (marginals)
@@ -172,10 +173,14 @@ __global__ void __launch_bounds__(kBlock) k_jhmi_finalize(EvalArgs a, const Jhmi
     }
   }
   __syncthreads();
-  // the value: per-thread sums over a fixed bin order, a fixed XOR tree per warp, the
-  // warps in order (short FP64 dependency chains: GB300's FP64 pipe is slow)
+  // the value over this block's share of the bins: per-thread sums in a fixed bin
+  // order, a fixed XOR tree per warp, the warps in order; the blocks' partials are
+  // added in block order by the last block.  Each block repeats the (small) PDF,
+  // smoothing and marginals so the FP64 logs spread over kJhmiFinalizeBlocks SMs.
+  const int q0 = (int)((long long)B * B * blockIdx.x / gridDim.x);
+  const int q1 = (int)((long long)B * B * (blockIdx.x + 1) / gridDim.x);
   double s = 0.0;
-  for (int q = threadIdx.x; q < B * B; q += blockDim.x) {
+  for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
     const int i = q % B, j = q / B;
     const double denom = fm[i] * mm[j];
     const double pxy = pdf[q];
@@ -187,11 +192,18 @@ __global__ void __launch_bounds__(kBlock) k_jhmi_finalize(EvalArgs a, const Jhmi
   }
   s = warp_sum_d(s);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  for (int j = threadIdx.x; j < B; j += blockDim.x) a.pratio[B * B + j] = (float)mm[j];
+  if (blockIdx.x == 0)
+    for (int j = threadIdx.x; j < B; j += blockDim.x) a.pratio[B * B + j] = (float)mm[j];
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    a.part[blockIdx.x] = t;
+  }
+  if (!last_block(a.tickets + kTicketFinalize)) return;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)gridDim.x; ++k) t += __ldcg(&a.part[k]);
     a.out[1] = (double)N;
     if (N == 0) {  // GetValue: VerifyNumberOfValidPoints, a warning and the maximum value
       a.out[0] = DBL_MAX;

@@ -1132,7 +1132,7 @@ static int enqueue_eval_jhmi(gb_metric* m, const EvalArgs& a, bool cd, bool deri
   m->mark();
   const size_t shf = sizeof(double) * (2 * B * B + 2 * B);
   GB_CUDA(cudaFuncSetAttribute(k_jhmi_finalize, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shf));
-  GB_CUDA(launch_chain(m, k_jhmi_finalize, 1, kBlock, shf, a, C));
+  GB_CUDA(launch_chain(m, k_jhmi_finalize, (unsigned)kJhmiFinalizeBlocks, kBlock, shf, a, C));
   m->mark();
   if (deriv) {
     const size_t sh2 = sizeof(float) * (B * B + B);
