@@ -15,7 +15,7 @@
 //                   histogram, flushed with 64-bit atomics (order-free, so exact);
 //   k_jhmi_finalize a few blocks: the normalized PDF, the discrete-Gaussian smoothing
 //                   (separable, zero-flux border, moving axis first), the marginals
-//                   by compensated sums, the value; FP32 tables for pass 2;
+//                   and the value (fixed-order trees); FP32 tables for pass 2;
 //   k_jhmi_pass2    per sample: bilinear PDF value and moving-axis slope, the
 //                   marginal and its slope, the clamped log-slope difference times
 //                   J^T g, fixed-order sums; the last block divides by the count.
@@ -123,13 +123,6 @@ __device__ __forceinline__ void jhmi_gauss_pass(const double* in, double* out, i
   }
 }
 
-__device__ __forceinline__ void kahan_d(double& s, double& c, double x) {
-  const double y = x - c;
-  const double t = s + y;
-  c = (t - s) - y;
-  s = t;
-}
-
 // k_jhmi_finalize (kJhmiFinalizeBlocks blocks).  Writes the smoothed PDF (FP64, pdf_out; FP32 and the
 // FP32 moving marginal into the pratio table), the value, the count and the status.
 __global__ void __launch_bounds__(kBlock) k_jhmi_finalize(EvalArgs a, const JhmiConsts* gC) {
@@ -150,8 +143,8 @@ __global__ void __launch_bounds__(kBlock) k_jhmi_finalize(EvalArgs a, const Jhmi
   double* fm = plane + 2 * B * B;
   double* mm = fm + B;
   const unsigned long long N = __ldcg(a.acc_n);
-  for (int k = threadIdx.x; k < B * B; k += blockDim.x)
-    p0[k] = N > 0 ? (double)__ldcg(&a.hist[k]) / (double)N : 0.0;
+  const double invN = N > 0 ? 1.0 / (double)N : 0.0;
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) p0[k] = (double)__ldcg(&a.hist[k]) * invN;
   __syncthreads();
   double* pdf = p0;
   if (C.radius > 0) {  // DiscreteGaussianImageFilter: the moving axis, then the fixed axis
@@ -160,16 +153,19 @@ __global__ void __launch_bounds__(kBlock) k_jhmi_finalize(EvalArgs a, const Jhmi
     jhmi_gauss_pass(p1, p0, B, 0, C);
     __syncthreads();
   }
-  // marginals: moving = sum over the fixed index, fixed = sum over the moving index
-  for (int t = threadIdx.x; t < 2 * B; t += blockDim.x) {
-    double s = 0.0, c = 0.0;
-    if (t < B) {
-      for (int i = 0; i < B; ++i) kahan_d(s, c, pdf[i + B * t]);
-      mm[t] = s;
-    } else {
-      const int i = t - B;
-      for (int j = 0; j < B; ++j) kahan_d(s, c, pdf[i + B * j]);
-      fm[i] = s;
+  // marginals: moving = sum over the fixed index, fixed = sum over the moving index;
+  // one warp per marginal bin: lane-strided loads, a fixed XOR tree (short FP64 chains)
+  {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int t = warp; t < 2 * B; t += nw) {
+      double s = 0.0;
+      if (t < B) {
+        for (int i = lane; i < B; i += 32) s += pdf[i + B * t];
+      } else {
+        for (int j = lane; j < B; j += 32) s += pdf[(t - B) + B * j];
+      }
+      s = warp_sum_d(s);
+      if (lane == 0) (t < B ? mm[t] : fm[t - B]) = s;
     }
   }
   __syncthreads();
