@@ -98,10 +98,18 @@ struct OptState;  // device optimizer state (gb_optimizer.cu)
 
 // body(k0, k1) over [0, n) split across the host's threads (at most 16, at least
 // `grain` items each); the caller's thread runs whatever no new thread could take.
+inline unsigned host_threads() {
+  static const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));  // queried once
+  return hw;
+}
+
 template <typename F>
 void parallel_ranges(int64_t n, F body, int64_t grain = 16384) {
-  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const int64_t T = std::max<int64_t>(1, std::min<int64_t>(hw, n / grain));
+  if (n < 2 * grain) {  // small: no thread, no query
+    body(0, n);
+    return;
+  }
+  const int64_t T = std::max<int64_t>(1, std::min<int64_t>(host_threads(), n / grain));
   if (T == 1) {
     body(0, n);
     return;
