@@ -88,6 +88,13 @@ int gb_metric_set_number_of_histogram_bins(gb_metric *m, uint64_t bins);
  * (default 1.5; <= 0: no smoothing), Registration/Metricsv4/include/itkJointHistogramMutualInformationImageToImageMetricv4.h:141.
  * The joint-histogram metric takes affine transforms and 6 to 64 bins (default 20). */
 int gb_metric_set_joint_pdf_smoothing_variance(gb_metric *m, double variance);
+/* SetUseFloatingPointCorrection(on) / SetFloatingPointCorrectionResolution(resolution)
+ * (Registration/Metricsv4/include/itkImageToImageMetricv4.h:604-621; applied in
+ * ...GetValueAndDerivativeThreaderBase.hxx:284-294): each point's local derivative
+ * truncated to 1 / resolution before it is summed.  Runs MeanSquares with affine
+ * transforms (summed in FP64); no effect on Mattes, correlation and displacement
+ * fields, as in the reference; other combinations are GB_ERR_UNSUPPORTED at Initialize. */
+int gb_metric_set_floating_point_correction(gb_metric *m, int on, double resolution);
 
 /* SetFixedImage / SetMovingImage (itkImageToImageMetricv4.h SetFixedImage /
  * SetMovingImage): float voxels, x fastest, size[3] = (nx, ny, nz), start

@@ -88,6 +88,7 @@ SIGNATURES = {
     "gb_metric_destroy": [_P],
     "gb_metric_set_number_of_histogram_bins": [_P, _U64],
     "gb_metric_set_joint_pdf_smoothing_variance": [_P, _D],
+    "gb_metric_set_floating_point_correction": [_P, _I, _D],
     "gb_metric_set_image": [_P, _I, _P, _P, _P, _P, _P],
     "gb_metric_set_image_device": [_P, _I, _P, _P, _P, _P, _P],
     "gb_metric_set_gradient_source": [_P, _I],

@@ -394,8 +394,10 @@ extern "C" int gb_batch_add(gb_batch* b, gb_metric* m, const gb_regular_step_set
   if (!b || !m || !cfg || !slot) return fail(GB_ERR_BAD_ARG, "null argument");
   if (m->ctx->device != b->ctx->device) return fail(GB_ERR_BAD_ARG, "metric and batch on different devices");
   if (m->tkind != GB_TRANSFORM_AFFINE) return fail(GB_ERR_UNSUPPORTED, "the batched engine runs affine registrations");
-  if (m->kind == GB_METRIC_CORRELATION)
+  if (m->kind == GB_METRIC_CORRELATION || m->kind == GB_METRIC_JOINT_HISTOGRAM_MI)
     return fail(GB_ERR_UNSUPPORTED, "the batched engine runs MeanSquares and Mattes registrations");
+  if (m->kind == GB_METRIC_MEAN_SQUARES && m->fp_res > 0.0)
+    return fail(GB_ERR_UNSUPPORTED, "the batched engine runs without the floating point correction");
   for (const gb_batch::Reg& R : b->regs)
     if (R.m == m && !R.done) return fail(GB_ERR_BAD_ARG, "metric already running in this batch");
   gb_batch::Reg R;

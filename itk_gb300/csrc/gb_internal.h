@@ -190,6 +190,7 @@ struct gb_metric {
   gb::DevBuf<float4> d_nodes;    // B-spline coefficients as float4 nodes
   gb::DevBuf<uint32_t> d_voff;   // displacement field on a point set: each sample's nearest virtual voxel
   double jhmi_variance = 1.5;    // joint-histogram MI: variance of the joint-PDF smoothing
+  double fp_res = 0.0;           // UseFloatingPointCorrection resolution, 0 = off
   gb::DevBuf<unsigned char> d_jhmi;  // joint-histogram MI constants (JhmiConsts)
   int64_t nchunks = 0;
   int64_t node_entries_count = 0;  // (node, chunk) pairs: chooses the parameter gather's shape

@@ -184,6 +184,9 @@ struct EvalArgs {
   int vnx, vny, vnz;                  // the virtual grid, which is the field's
   const unsigned* __restrict__ voff;  // point sets: each sample's nearest virtual voxel (~0u: outside)
   int field_full;                     // dense, one sample per voxel: every derivative entry is written
+  // UseFloatingPointCorrection (MeanSquares, affine): each sample's local derivatives
+  // truncated to 1 / fp_res and summed in FP64; 0 = off
+  double fp_res;
 };
 
 // The optimizer's stop flag (read once per block, after the launch dependency).
@@ -356,11 +359,15 @@ __device__ __forceinline__ bool last_block(unsigned* ticket, VGrid vg = hw_grid(
 // ---------------------------------------------------------------------------
 // MeanSquares, affine: value = sum (f - m)^2 / N, d[p] = sum 2 (f - m) (J^T g)[p] / N
 
-template <int GRAD>
+template <int GRAD, bool FPC = false>
 __device__ __forceinline__ void msq_affine_body(const EvalArgs& a, VGrid vg) {
   __shared__ EvalConsts K;
   __shared__ float red[kBlock / 32][13];
+  __shared__ double redd[FPC ? kBlock / 32 : 1][12];
   __shared__ double blk[13], fin[13];
+  double dacc[FPC ? 12 : 1];
+#pragma unroll
+  for (int k = 0; k < (FPC ? 12 : 1); ++k) dacc[k] = 0.0;
   griddep_wait();
   if (halted(a)) return;
   griddep_launch_dependents();
@@ -388,14 +395,40 @@ __device__ __forceinline__ void msq_affine_body(const EvalArgs& a, VGrid vg) {
       const float3 v = jac_vec(K, s.x, s.y, s.z);
       const float vx = v.x, vy = v.y, vz = v.z;
       const float t0 = t * g.x, t1 = t * g.y, t2 = t * g.z;
-      acc[1].add(t0 * vx); acc[2].add(t0 * vy); acc[3].add(t0 * vz);
-      acc[4].add(t1 * vx); acc[5].add(t1 * vy); acc[6].add(t1 * vz);
-      acc[7].add(t2 * vx); acc[8].add(t2 * vy); acc[9].add(t2 * vz);
-      acc[10].add(t0); acc[11].add(t1); acc[12].add(t2);
+      if (FPC) {
+        // StorePointDerivativeResult with UseFloatingPointCorrection
+        // (ThreaderBase.hxx:284-294): static_cast<intmax_t>(d * r) / r per parameter
+        const float ld[12] = {t0 * vx, t0 * vy, t0 * vz, t1 * vx, t1 * vy, t1 * vz,
+                              t2 * vx, t2 * vy, t2 * vz, t0, t1, t2};
+#pragma unroll
+        for (int k = 0; k < (FPC ? 12 : 1); ++k)
+          dacc[k] += (double)(long long)((double)ld[k] * a.fp_res) / a.fp_res;
+      } else {
+        acc[1].add(t0 * vx); acc[2].add(t0 * vy); acc[3].add(t0 * vz);
+        acc[4].add(t1 * vx); acc[5].add(t1 * vy); acc[6].add(t1 * vz);
+        acc[7].add(t2 * vx); acc[8].add(t2 * vy); acc[9].add(t2 * vz);
+        acc[10].add(t0); acc[11].add(t1); acc[12].add(t2);
+      }
     }
   }
   block_count(nv, a.acc_n);
   block_sums<13>(acc, red, blk);
+  if (FPC) {
+    // the truncated derivatives: FP64 warp trees, warps in order
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < (FPC ? 12 : 1); ++k) {
+      const double w = warp_sum_d(dacc[k]);
+      if (lane == 0) redd[warp][k] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+      double s = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += redd[w][threadIdx.x];
+      blk[1 + threadIdx.x] = s;
+    }
+    __syncthreads();
+  }
   if (!grid_sums<13>(blk, a.part, a.grp, a.tickets + kTicketMain, fin, vg)) return;
   if (threadIdx.x == 0) {
     // AfterThreadedExecution + VerifyNumberOfValidPoints (ThreaderBase.hxx:116-172)
@@ -415,9 +448,9 @@ __device__ __forceinline__ void msq_affine_body(const EvalArgs& a, VGrid vg) {
   }
 }
 
-template <int GRAD>
+template <int GRAD, bool FPC = false>
 __global__ void __launch_bounds__(kBlock) k_msq_affine(EvalArgs a) {
-  msq_affine_body<GRAD>(a, hw_grid());
+  msq_affine_body<GRAD, FPC>(a, hw_grid());
 }
 
 // ---------------------------------------------------------------------------

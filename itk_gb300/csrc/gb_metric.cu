@@ -312,6 +312,14 @@ extern "C" int gb_metric_destroy(gb_metric* m) {
   return GB_OK;
 }
 
+extern "C" int gb_metric_set_floating_point_correction(gb_metric* m, int on, double resolution) {
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  if (on && !(resolution > 0.0)) return fail(GB_ERR_BAD_ARG, "floating point correction resolution must be > 0");
+  m->fp_res = on ? resolution : 0.0;
+  m->initialized = false;
+  return GB_OK;
+}
+
 extern "C" int gb_metric_set_joint_pdf_smoothing_variance(gb_metric* m, double variance) {
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (!(variance == variance)) return fail(GB_ERR_BAD_ARG, "variance is NaN");
@@ -538,6 +546,11 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric runs affine transforms");
   if (jhmi && (m->bins < 6 || m->bins > kJhmiMaxBins))
     return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric takes 6 to 64 bins");
+  // the floating point correction acts where points store a global derivative
+  // (MeanSquares, joint-histogram MI); Mattes, correlation and local-support
+  // transforms accumulate elsewhere, so it has no effect there, as in the reference
+  if (m->fp_res > 0.0 && (jhmi || (m->kind == GB_METRIC_MEAN_SQUARES && !field && m->tkind != GB_TRANSFORM_AFFINE)))
+    return fail(GB_ERR_UNSUPPORTED, "the floating point correction runs MeanSquares with affine transforms");
   double g_p2i[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   if (bspline) {
     // BSplineTransform fixed parameters: grid size, origin, spacing, direction (itkBSplineTransform.hxx:243-283)
@@ -968,6 +981,7 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.status = m->d_status.p;
   a.with_derivative = deriv ? 1 : 0;
   a.halt = m->eval_halt;
+  a.fp_res = m->fp_res;
   if (is_bspline(m)) {
     a.sup = m->d_sup.p;
     a.nodes = m->d_nodes.p;
@@ -1182,8 +1196,12 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
     return GB_OK;
   }
   if (m->kind == GB_METRIC_MEAN_SQUARES) {
-    GB_CUDA(cd ? launch_wave(m, k_msq_affine<kGradCentralDifference>, 0, a)
-               : launch_wave(m, k_msq_affine<kGradImage>, 0, a));
+    if (a.fp_res > 0.0)
+      GB_CUDA(cd ? launch_wave(m, k_msq_affine<kGradCentralDifference, true>, 0, a)
+                 : launch_wave(m, k_msq_affine<kGradImage, true>, 0, a));
+    else
+      GB_CUDA(cd ? launch_wave(m, k_msq_affine<kGradCentralDifference>, 0, a)
+                 : launch_wave(m, k_msq_affine<kGradImage>, 0, a));
     m->mark();
     return GB_OK;
   }

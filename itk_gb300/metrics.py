@@ -90,6 +90,21 @@ class ImageToImageMetricv4:
     def GetMovingTransform(self):
         return self._transform
 
+    def SetUseFloatingPointCorrection(self, on: bool):
+        """Truncate each point's local derivative to 1 / resolution before summing
+        (MeanSquares with affine transforms; no effect on Mattes, correlation and
+        displacement fields, as in the reference)."""
+        self._fp_correction = bool(on)
+
+    def GetUseFloatingPointCorrection(self):
+        return getattr(self, "_fp_correction", False)
+
+    def SetFloatingPointCorrectionResolution(self, resolution: float):
+        self._fp_resolution = float(resolution)
+
+    def GetFloatingPointCorrectionResolution(self):
+        return getattr(self, "_fp_resolution", 1e6)  # the reference's default
+
     def SetUseMovingImageGradientFilter(self, on: bool):
         """False selects CentralDifferenceImageFunction at each mapped point."""
         self._use_moving_gradient_filter = bool(on)
@@ -164,6 +179,8 @@ class ImageToImageMetricv4:
             check(self._L.gb_metric_set_sampled_points(self._h, ptr(self._points), self._points.shape[0],
                                                        int(self._points_virtual)))
         check(self._L.gb_metric_use_sampled_point_set(self._h, int(self._use_sampled)))
+        check(self._L.gb_metric_set_floating_point_correction(self._h, int(self.GetUseFloatingPointCorrection()),
+                                                               self.GetFloatingPointCorrectionResolution()))
         check(self._L.gb_metric_set_level_smoothing(self._h, self._level_sigma, int(self._level_sigma_physical)))
         check(self._L.gb_metric_set_level_shrink(self._h, ptr(i64(self._level_shrink))))
         self._pre_initialize()

@@ -749,7 +749,13 @@ static void *msq_worker(void *arg)
     for (int e = 0; e < row.count; ++e) {
       /* localDerivative[par] = sum_dim 2.0 * diff * J(dim,par) * g[dim]; with one
        * nonzero J entry per (par, dim) pair for affine rows and B-spline rows */
-      const double ld = 2.0 * diffC * row.val[e];
+      double ld = 2.0 * diffC * row.val[e];
+      if (j->in->fp_resolution > 0.0) {
+        /* UseFloatingPointCorrection: each local derivative truncated to the resolution
+         * before it is added (StorePointDerivativeResult, ThreaderBase.hxx:284-294) */
+        const double r = j->in->fp_resolution;
+        ld = (double)(int64_t)(ld * r) / r;
+      }
       kahan_add(&j->dsum[row.idx[e]], &j->dcomp[row.idx[e]], ld);
     }
   }
@@ -1368,6 +1374,23 @@ int orc_msq_flat(const float *fixed, const int64_t fsize[3], const double fgeo[1
   return orc_msq_flat_v(fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, tkind, tparams,
                         nparams, tfixed, nfixed, nthreads, compute_derivative, value, derivative, nvalid, NULL,
                         NULL);
+}
+
+int orc_msq_flat_fpc(const float *fixed, const int64_t fsize[3], const double fgeo[15], const float *moving,
+                     const int64_t msize[3], const double mgeo[15], const double *moving_grad, const float *points,
+                     int64_t npoints, int tkind, const double *tparams, int64_t nparams, const double *tfixed,
+                     int64_t nfixed, int nthreads, int compute_derivative, double *value, double *derivative,
+                     uint64_t *nvalid, double resolution)
+{
+  orc_inputs in;
+  orc_transform t;
+  int rc = inputs_from_flat(&in, fixed, fsize, fgeo, moving, msize, mgeo, moving_grad, points, npoints, nthreads,
+                            NULL, NULL);
+  if (rc) return rc;
+  in.fp_resolution = resolution;
+  rc = orc_transform_from_flat(&t, tkind, tparams, nparams, tfixed, nfixed);
+  if (rc) return rc;
+  return orc_msq_value_derivative(&in, &t, compute_derivative, value, derivative, nvalid);
 }
 
 int orc_msq_flat_v(const float *fixed, const int64_t fsize[3], const double fgeo[15], const float *moving,

@@ -122,6 +122,7 @@ typedef struct {
   int64_t npoints;
   int nthreads;
   int pixel_double;            /* 1: keep interpolated values in double, as for Image<double,N> */
+  double fp_resolution;        /* > 0: UseFloatingPointCorrection at this resolution (MeanSquares) */
 } orc_inputs;
 
 typedef struct {
@@ -202,6 +203,12 @@ int orc_mattes_flat_v(const float *fixed, const int64_t fsize[3], const double f
                       const double *tfixed, int64_t nfixed, int64_t bins, int nthreads, int compute_derivative,
                       double *value, double *derivative, uint64_t *nvalid, double *joint_pdf, double *state_out,
                       const int64_t *vsize, const double *vgeo);
+/* orc_msq_flat_v with UseFloatingPointCorrection at `resolution` (> 0) */
+int orc_msq_flat_fpc(const float *fixed, const int64_t fsize[3], const double fgeo[15],
+                     const float *moving, const int64_t msize[3], const double mgeo[15], const double *moving_grad,
+                     const float *points, int64_t npoints, int tkind, const double *tparams, int64_t nparams,
+                     const double *tfixed, int64_t nfixed, int nthreads, int compute_derivative,
+                     double *value, double *derivative, uint64_t *nvalid, double resolution);
 int orc_transform_point_flat(int tkind, const double *tparams, int64_t nparams, const double *tfixed,
                              int64_t nfixed, const double *x, int64_t n, double *y);
 int orc_interpolate_flat(const float *img, const int64_t size[3], const double geo[15], const double *points,

@@ -64,6 +64,7 @@ def lib():
                                       i64, ctypes.c_int, ctypes.c_int, P, P, P, P, P]
         L.orc_msq_flat_v.argtypes = L.orc_msq_flat.argtypes + [P, P]
         L.orc_corr_flat_v.argtypes = L.orc_msq_flat_v.argtypes
+        L.orc_msq_flat_fpc.argtypes = L.orc_msq_flat.argtypes + [ctypes.c_double]
         L.orc_mattes_flat_v.argtypes = L.orc_mattes_flat.argtypes + [P, P]
         L.orc_jhmi_flat_v.argtypes = [P, P, P, P, P, P, P, P, i64, ctypes.c_int, P, i64, P, i64, i64,
                                       ctypes.c_double, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]
@@ -161,6 +162,23 @@ def mean_squares(fixed, fgeom, moving, mgeom, transform, moving_grad=None, point
                           0 if pts is None else pts.shape[0], transform.kind, _p(tp), tp.size, _p(tf), tf.size,
                           _threads(nthreads, pixel_double), int(compute_derivative), _p(value), _p(deriv),
                           _p(nvalid), _p(vs), _p(vg))
+    return rc, float(value[0]), deriv, int(nvalid[0])
+
+
+def mean_squares_fpc(fixed, fgeom, moving, mgeom, transform, resolution, moving_grad=None, points=None, nthreads=None):
+    """MeanSquares with UseFloatingPointCorrection at `resolution`.  Returns (status, value, derivative, nvalid)."""
+    L = lib()
+    fixed, moving = _img(fixed), _img(moving)
+    mg, pts = _grad(moving_grad), _pts(points)
+    tp = np.ascontiguousarray(transform.params, dtype=np.float64)
+    tf = np.ascontiguousarray(transform.fixed, dtype=np.float64)
+    value = np.zeros(1, np.float64)
+    deriv = np.zeros(tp.size, np.float64)
+    nvalid = np.zeros(1, np.uint64)
+    fs, fg, ms, mgeo = fgeom.size_array(), fgeom.flat(), mgeom.size_array(), mgeom.flat()
+    rc = L.orc_msq_flat_fpc(_p(fixed), _p(fs), _p(fg), _p(moving), _p(ms), _p(mgeo), _p(mg), _p(pts),
+                            0 if pts is None else pts.shape[0], transform.kind, _p(tp), tp.size, _p(tf), tf.size,
+                            _threads(nthreads, False), 1, _p(value), _p(deriv), _p(nvalid), float(resolution))
     return rc, float(value[0]), deriv, int(nvalid[0])
 
 

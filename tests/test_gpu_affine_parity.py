@@ -215,3 +215,32 @@ def test_full_size_mattes_config(pair_mm):
     pts = data.random_points(fixed, 0.2, seed=1001)
     check_against_oracle("mattes", fixed, moving, perturbed(T, 11, scale=0.01, trans=2.0), grad, points=pts,
                          nvalid_slack=8)
+
+
+@pytest.mark.parametrize("resolution", [10.0, 1e6])
+def test_floating_point_correction(resolution):
+    """SetUseFloatingPointCorrection on the GPU (MeanSquares, affine) against the oracle's
+    truncated sums; the correction is seen at a coarse resolution."""
+    from cases import geom, oracle_transform
+    from oracle import oracle as O
+    fixed, moving, T = small_pair((40, 36, 32), config=0)
+    U = perturbed(T, 8)
+    grad = data.gradient_image(moving)
+    out = []
+    for on in (False, True):
+        m = MeanSquaresImageToImageMetricv4()
+        m.SetFixedImage(fixed)
+        m.SetMovingImage(moving)
+        m.SetMovingTransform(U)
+        m.SetMovingImageGradientImage(grad)
+        m.SetUseFloatingPointCorrection(on)
+        m.SetFloatingPointCorrectionResolution(resolution)
+        m.Initialize()
+        out.append(m.GetValueAndDerivative())
+    rc, rv, rd, nv = O.mean_squares_fpc(fixed.array, geom(fixed), moving.array, geom(moving), oracle_transform(U),
+                                        resolution, moving_grad=grad.array)
+    assert rc == 0
+    assert out[0][0] == out[1][0]
+    assert_deriv_close(out[1][1], rd)
+    if resolution == 10.0:
+        assert np.max(np.abs(out[1][1] - out[0][1])) > 1e-3 / nv
