@@ -4,7 +4,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -104,23 +103,13 @@ inline unsigned host_threads() {
   return hw;
 }
 
-// Helper threads running in parallel_ranges across the process: concurrent callers
-// (a server's set-up threads) share the host's cores instead of each taking all.
-inline std::atomic<int>& busy_helpers() {
-  static std::atomic<int> n{0};
-  return n;
-}
-
 template <typename F>
 void parallel_ranges(int64_t n, F body, int64_t grain = 16384) {
   if (n < 2 * grain) {  // small: no thread, no query
     body(0, n);
     return;
   }
-  const int want = (int)std::max<int64_t>(1, std::min<int64_t>(host_threads(), n / grain));
-  const int extra = std::max(0, std::min(want - 1, (int)host_threads() - 1 - busy_helpers().fetch_add(want - 1)));
-  busy_helpers().fetch_sub(want - 1 - extra);  // keep only the helpers this call can have
-  const int64_t T = 1 + extra;
+  const int64_t T = std::max<int64_t>(1, std::min<int64_t>(host_threads(), n / grain));
   if (T == 1) {
     body(0, n);
     return;
@@ -133,7 +122,6 @@ void parallel_ranges(int64_t n, F body, int64_t grain = 16384) {
   }
   for (std::thread& x : th) x.join();
   if (started < T) body(n * started / T, n);
-  busy_helpers().fetch_sub(extra);
 }
 
 // memcpy split across the host's threads for large buffers (a displacement
