@@ -119,3 +119,34 @@ def test_bspline_composite_mattes_random():
     rms = displacement_rms(fixed, C, C0)
     assert rms <= 0.05, f"displacement RMS {rms:.4f} voxel"
     assert np.max(np.abs(Bs.GetParameters())) > 0.1  # it moved
+
+
+@pytest.mark.parametrize("kind", ["jhmi", "correlation"])
+def test_other_metrics_through_the_registration_method(pair_mono, pair_mm, kind):
+    """JointHistogram MI (multimodal pair) and correlation (single-modality pair) drive
+    ImageRegistrationMethodv4 and the device optimizer to the generating transform."""
+    from itk_gb300 import CorrelationImageToImageMetricv4, JointHistogramMutualInformationImageToImageMetricv4
+    fixed, moving, T = pair_mm if kind == "jhmi" else pair_mono
+    U = perturbed(T, 23, scale=0.01, trans=1.5)
+    start = displacement_rms(fixed, U, T)
+    m = JointHistogramMutualInformationImageToImageMetricv4() if kind == "jhmi" else CorrelationImageToImageMetricv4()
+    o = RegularStepGradientDescentOptimizerv4()
+    o.SetLearningRate(0.5)
+    o.SetNumberOfIterations(100)
+    o.SetMinimumStepLength(1e-3)
+    o.SetScales(AFFINE_SCALES)
+    reg = ImageRegistrationMethodv4()
+    reg.SetFixedImage(fixed)
+    reg.SetMovingImage(moving)
+    reg.SetMetric(m)
+    reg.SetOptimizer(o)
+    reg.SetInitialTransform(U)
+    reg.SetNumberOfLevels(2)
+    reg.SetShrinkFactorsPerLevel([2, 1])
+    reg.SetSmoothingSigmasPerLevel([1.0, 0.0])
+    reg.SetMetricSamplingStrategy(RANDOM)
+    reg.SetMetricSamplingPercentage(0.3)
+    reg.MetricSamplingReinitializeSeed(5)
+    reg.Update()
+    end = displacement_rms(fixed, U, T)
+    assert end < 0.5 * start and end < 0.6, f"displacement RMS to the truth {start:.3f} -> {end:.3f} voxel"
