@@ -121,18 +121,10 @@ def test_bspline_composite_mattes_random():
     assert np.max(np.abs(Bs.GetParameters())) > 0.1  # it moved
 
 
-@pytest.mark.parametrize("kind", ["jhmi", "correlation"])
-def test_other_metrics_through_the_registration_method(pair_mono, pair_mm, kind):
-    """JointHistogram MI (multimodal pair) and correlation (single-modality pair) drive
-    ImageRegistrationMethodv4 and the device optimizer to the generating transform."""
-    from itk_gb300 import CorrelationImageToImageMetricv4, JointHistogramMutualInformationImageToImageMetricv4
-    fixed, moving, T = pair_mm if kind == "jhmi" else pair_mono
-    U = perturbed(T, 23, scale=0.01, trans=1.5)
-    start = displacement_rms(fixed, U, T)
-    m = JointHistogramMutualInformationImageToImageMetricv4() if kind == "jhmi" else CorrelationImageToImageMetricv4()
+def other_metric_registration(m, fixed, moving, U, levels, pct, iterations, seed=5):
     o = RegularStepGradientDescentOptimizerv4()
     o.SetLearningRate(0.5)
-    o.SetNumberOfIterations(100)
+    o.SetNumberOfIterations(iterations)
     o.SetMinimumStepLength(1e-3)
     o.SetScales(AFFINE_SCALES)
     reg = ImageRegistrationMethodv4()
@@ -141,12 +133,56 @@ def test_other_metrics_through_the_registration_method(pair_mono, pair_mm, kind)
     reg.SetMetric(m)
     reg.SetOptimizer(o)
     reg.SetInitialTransform(U)
-    reg.SetNumberOfLevels(2)
-    reg.SetShrinkFactorsPerLevel([2, 1])
-    reg.SetSmoothingSigmasPerLevel([1.0, 0.0])
+    reg.SetNumberOfLevels(len(levels))
+    reg.SetShrinkFactorsPerLevel([lv[0] for lv in levels])
+    reg.SetSmoothingSigmasPerLevel([lv[1] for lv in levels])
     reg.SetMetricSamplingStrategy(RANDOM)
-    reg.SetMetricSamplingPercentage(0.3)
-    reg.MetricSamplingReinitializeSeed(5)
+    reg.SetMetricSamplingPercentage(pct)
+    reg.MetricSamplingReinitializeSeed(seed)
     reg.Update()
-    end = displacement_rms(fixed, U, T)
+    return reg, o
+
+
+def test_correlation_registration_recovers_the_transform(pair_mono):
+    """CorrelationImageToImageMetricv4 drives ImageRegistrationMethodv4 and the device
+    optimizer from the identity to the generating transform's inverse (moving(y) =
+    fixed(T(y)))."""
+    from itk_gb300 import AffineTransform, CorrelationImageToImageMetricv4
+    fixed, moving, T = pair_mono
+    truth = AffineTransform()
+    truth.SetCenter(T.GetCenter())
+    Minv = np.linalg.inv(T.GetMatrix())
+    truth.SetMatrix(Minv)
+    truth.SetTranslation(-Minv @ T.GetTranslation())
+    U = perturbed(T, 23, scale=0.01, trans=1.5)
+    start = displacement_rms(fixed, U, truth)
+    other_metric_registration(CorrelationImageToImageMetricv4(), fixed, moving, U, [(2, 1.0), (1, 0.0)], 0.3, 100)
+    end = displacement_rms(fixed, U, truth)
     assert end < 0.5 * start and end < 0.6, f"displacement RMS to the truth {start:.3f} -> {end:.3f} voxel"
+
+
+def test_jhmi_registration_matches_oracle_loop(pair_mono):
+    """JointHistogram MI through ImageRegistrationMethodv4 and the device optimizer against
+    the oracle's RegularStep restatement on the oracle metric with the same points."""
+    from itk_gb300 import JointHistogramMutualInformationImageToImageMetricv4
+    from cases import oracle_transform
+    from oracle import oracle as O
+    fixed, moving, T = pair_mono
+    U = perturbed(T, 24, scale=0.01, trans=1.0)
+    U0 = perturbed(T, 24, scale=0.01, trans=1.0)
+    reg, o = other_metric_registration(JointHistogramMutualInformationImageToImageMetricv4(), fixed, moving, U,
+                                       [(1, 0.0)], 0.3, 30)
+    pts = reg.GetMetricSamplePoints(0)
+    g = O.gradient_recursive_gaussian(moving.array, moving.spacing, moving.direction, float(max(moving.spacing)))
+
+    def evaluate(p):
+        U0.SetParameters(p)
+        rc, v, d, _, _ = O.joint_histogram_mi(fixed.array, geom(fixed), moving.array, geom(moving),
+                                              oracle_transform(U0), moving_grad=g, points=pts)
+        return rc, v, d
+
+    h = R.regular_step(evaluate, U0.GetParameters().copy(), learning_rate=0.5, minimum_step_length=1e-3,
+                       number_of_iterations=30, scales=AFFINE_SCALES)
+    U0.SetParameters(h["params"])
+    rms = displacement_rms(fixed, U, U0)
+    assert rms <= 0.05, f"displacement RMS {rms:.4f} voxel"
