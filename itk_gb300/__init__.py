@@ -17,6 +17,7 @@ from .metrics import (CorrelationImageToImageMetricv4, ImageToImageMetricv4,
                       MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4, context)
 from .optimizers import RegularStepGradientDescentOptimizerv4
 from .registration import ImageRegistrationMethodv4, sample_count, sample_points
+from .scales import RegistrationParameterScalesFromPhysicalShift
 from .serving import RegistrationRequest, RegistrationResult, RegistrationServer
 from .transformio import ReadTransform, WriteTransform
 from .transforms import AffineTransform, BSplineTransform, CompositeTransform, DisplacementFieldTransform
@@ -27,7 +28,8 @@ __all__ = [
     "GradientRecursiveGaussianImageFilter", "Image", "ImageRegistrationMethodv4", "ImageToImageMetricv4",
     "JointHistogramMutualInformationImageToImageMetricv4",
     "MattesMutualInformationImageToImageMetricv4", "MeanSquaresImageToImageMetricv4",
-    "RegistrationBatch", "RegistrationRequest", "RegistrationResult", "RegistrationServer",
+    "RegistrationBatch", "RegistrationParameterScalesFromPhysicalShift", "RegistrationRequest", "RegistrationResult",
+    "RegistrationServer",
     "RegularStepGradientDescentOptimizerv4", "ShrinkImageFilter", "SmoothingRecursiveGaussianImageFilter", "context",
     "ReadTransform", "WriteTransform", "lib", "library_path", "sample_count", "sample_points", "shrink_geometry",
 ]

@@ -103,6 +103,21 @@ class RegularStepGradientDescentOptimizerv4:
     def GetScales(self):
         return self._scales
 
+    def SetScalesEstimator(self, estimator):
+        """A RegistrationParameterScalesFromPhysicalShift: with DoEstimateScales on (the
+        default), StartOptimization sets the scales from it (GradientDescentOptimizerBasev4::
+        StartOptimization, Numerics/Optimizersv4/include/itkGradientDescentOptimizerBasev4.hxx:132-143)."""
+        self._scales_estimator = estimator
+
+    def GetScalesEstimator(self):
+        return getattr(self, "_scales_estimator", None)
+
+    def SetDoEstimateScales(self, on: bool):
+        self._do_estimate_scales = bool(on)
+
+    def GetDoEstimateScales(self):
+        return getattr(self, "_do_estimate_scales", True)
+
     def SetUseCudaGraphs(self, on: bool):
         """Capture each iteration in a CUDA graph (default on); off launches the kernels directly."""
         self._use_graphs = bool(on)
@@ -113,6 +128,9 @@ class RegularStepGradientDescentOptimizerv4:
         if m is None:
             raise ExceptionObject(_capi.GB_ERR_BAD_ARG, "m_Metric must be set.")
         m._sync_params()
+        est = self.GetScalesEstimator()
+        if est is not None and self.GetDoEstimateScales():
+            self._scales = f64(est.EstimateScales())
         if doOnlyInitialization:
             return
         s = RegularStepSettings(self._learning_rate, self._relaxation_factor, self._minimum_step_length,
