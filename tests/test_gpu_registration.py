@@ -186,3 +186,34 @@ def test_jhmi_registration_matches_oracle_loop(pair_mono):
     U0.SetParameters(h["params"])
     rms = displacement_rms(fixed, U, U0)
     assert rms <= 0.05, f"displacement RMS {rms:.4f} voxel"
+
+
+def test_scales_estimator_in_the_registration_method(pair_mono):
+    """A RegistrationParameterScalesFromPhysicalShift on the optimizer sets its scales at
+    every level (the level's shrunk virtual grid); the run equals one with those scales
+    given by hand."""
+    from itk_gb300 import RegistrationParameterScalesFromPhysicalShift
+    fixed, moving, T = pair_mono
+    U1 = perturbed(T, 25, scale=0.01, trans=1.0)
+    U2 = perturbed(T, 25, scale=0.01, trans=1.0)
+    m1 = MeanSquaresImageToImageMetricv4()
+    est = RegistrationParameterScalesFromPhysicalShift()
+    est.SetMetric(m1)
+    opt = dict(learning_rate=0.5, number_of_iterations=20, minimum_step_length=1e-3, scales=None)
+    o1 = RegularStepGradientDescentOptimizerv4()
+    o1.SetScalesEstimator(est)
+    reg1 = ImageRegistrationMethodv4()
+    reg1.SetFixedImage(fixed)
+    reg1.SetMovingImage(moving)
+    reg1.SetMetric(m1)
+    reg1.SetOptimizer(o1)
+    reg1.SetInitialTransform(U1)
+    o1.SetLearningRate(0.5)
+    o1.SetNumberOfIterations(20)
+    o1.SetMinimumStepLength(1e-3)
+    reg1.Update()
+    scales = o1.GetScales()
+    assert scales is not None and scales[9] == pytest.approx(1.0) and scales[0] > 1.0
+    opt["scales"] = scales
+    reg2, o2 = run_gpu("msq", fixed, moving, U2, [(1, 0.0)], NONE, 1.0, opt)
+    assert np.array_equal(U1.GetParameters(), U2.GetParameters())
