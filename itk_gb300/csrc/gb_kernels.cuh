@@ -56,6 +56,8 @@ struct EvalConsts {
   // displacement-field paths (map = the identity transform's map):
   AffineDF umap;  // physical displacement -> moving index offset (the moving image's P2I; b unused)
   AffineDF fmap;  // point set: physical point -> field continuous index
+  float fdiag;    // nonzero: map and umap are diagonal (axis-aligned grids), the field
+                  // position takes one product per axis (bitwise the same result)
 };
 
 __device__ __forceinline__ float3 jac_vec(const EvalConsts& K, float x, float y, float z) {
@@ -626,9 +628,53 @@ __device__ __forceinline__ float3 field_interp(const double* __restrict__ f, con
   return make_float3(u[0], u[1], u[2]);
 }
 
+// map(x) + umap u with diagonal matrices: the general double-float sums with their
+// zero terms left out (adding an exact zero changes neither the sum nor its error term).
+__device__ __forceinline__ DFPos field_pos_diag(const EvalConsts& K, float x, float y, float z, const float uhi[3],
+                                                const float ulo[3]) {
+  const float xs[3] = {x, y, z};
+  DFPos r;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float s = K.map.bhi[k], err = K.map.blo[k];
+    const float a = K.map.Ahi[4 * k];
+    const float p = __fmul_rn(a, xs[k]);
+    const float pe = __fmaf_rn(a, xs[k], -p);
+    float t, e;
+    two_sum(s, p, t, e);
+    s = t;
+    err = __fadd_rn(err, __fadd_rn(e, __fmaf_rn(K.map.Alo[4 * k], xs[k], pe)));
+    r.hi[k] = __fadd_rn(s, err);
+    r.lo[k] = __fsub_rn(err, __fsub_rn(r.hi[k], s));
+  }
+  DFPos q;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float s = r.hi[k], err = r.lo[k];
+    const float a = K.umap.Ahi[4 * k];
+    const float p = __fmul_rn(a, uhi[k]);
+    const float pe = __fmaf_rn(a, uhi[k], -p);
+    float t, e;
+    two_sum(s, p, t, e);
+    s = t;
+    err = __fadd_rn(err, __fadd_rn(e, __fadd_rn(pe, __fmaf_rn(K.umap.Alo[4 * k], uhi[k], __fmul_rn(a, ulo[k])))));
+    q.hi[k] = __fadd_rn(s, err);
+    q.lo[k] = __fsub_rn(err, __fsub_rn(q.hi[k], s));
+  }
+  return q;
+}
+
 template <int TK>
 __device__ __forceinline__ DFPos sample_pos(const EvalArgs& a, const EvalConsts& K, const float4& s, int64_t i,
                                             unsigned& voxel) {
+  if (TK == kMapFieldDense && K.fdiag != 0.f) {
+    voxel = (unsigned)s.x + (unsigned)a.vnx * ((unsigned)s.y + (unsigned)a.vny * (unsigned)s.z);
+    const double* q = a.field + 3ull * voxel;
+    float uhi[3], ulo[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) split_double_bits(__ldg(q + k), uhi[k], ulo[k]);
+    return field_pos_diag(K, s.x, s.y, s.z, uhi, ulo);
+  }
   const DFPos p = map_pos(K.map, s.x, s.y, s.z);
   if (TK == kMapAffine) return p;
   float uhi[3], ulo[3];

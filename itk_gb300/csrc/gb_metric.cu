@@ -925,6 +925,13 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
       }
       split_df(b, K.fmap.bhi[r], K.fmap.blo[r]);
     }
+    bool diag = true;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c)
+        if (r != c)
+          diag = diag && K.map.Ahi[3 * r + c] == 0.f && K.map.Alo[3 * r + c] == 0.f && K.umap.Ahi[3 * r + c] == 0.f &&
+                 K.umap.Alo[3 * r + c] == 0.f;
+    K.fdiag = diag ? 1.f : 0.f;
     GB_CUDA(cudaMemcpyAsync(m->d_consts.p, m->h_consts, sizeof(EvalConsts), cudaMemcpyHostToDevice, st));
   }
   GB_CUDA(cudaStreamSynchronize(st));

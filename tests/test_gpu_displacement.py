@@ -170,3 +170,22 @@ def test_device_optimizer_matches_host_loop():
     o.StartOptimization()
     assert o.GetStopCondition() == h["stop"] and o.GetCurrentIteration() == h["iterations"]
     assert np.max(np.abs(T.GetParameters() - h["params"])) <= 1e-9 * max(np.max(np.abs(h["params"])), 1.0)
+
+
+@pytest.mark.parametrize("kind", ["msq", "mattes"])
+def test_oblique_grids_match_oracle(pair, kind):
+    """A rotated image direction: the positions take the general double-float map
+    (the axis-aligned grids above take the diagonal one)."""
+    fixed0, moving0 = pair
+    t = np.deg2rad(20.0)
+    rot = np.array([[np.cos(t), -np.sin(t), 0.0], [np.sin(t), np.cos(t), 0.0], [0.0, 0.0, 1.0]])
+    fixed = Image(fixed0.array, spacing=(1.0, 1.2, 0.9), origin=(3.0, -2.0, 1.0), direction=rot)
+    moving = Image(moving0.array, spacing=(1.0, 1.2, 0.9), origin=(3.0, -2.0, 1.0), direction=rot)
+    T = field_transform(fixed, data.smooth_displacement_field(fixed, seed=11, max_disp=2.0).array)
+    grad = data.gradient_image(moving)
+    m = make(kind, fixed, moving, T, grad)
+    v, d = m.GetValueAndDerivative()
+    rc, rv, rd, nv = oracle(kind, fixed, moving, T, grad)
+    assert rc == 0 and m.GetNumberOfValidPoints() == nv
+    assert_value_close(v, rv)
+    assert_deriv_close(d, rd)
