@@ -25,6 +25,7 @@
 // reference's bin.
 #pragma once
 
+#include "gb_bspline.cuh"
 #include "gb_kernels.cuh"
 
 namespace gb {
@@ -233,6 +234,39 @@ __device__ __forceinline__ float jhmi_interp1(const float* t, int B, float c) {
   return lerp(t[x0], t[x1], d);
 }
 
+// One derivative point: false for an invalid or out-of-range sample; else sf, the
+// clamped log-slope difference of the joint PDF and the moving marginal along the
+// moving axis over (log 2 * moving range).
+__device__ __forceinline__ bool jhmi_scaling(const JhmiConsts& C, const float* pdf, const float* mm, int B, float f,
+                                             float m, float mlo, float mhi, float max_slope, float inv_scale,
+                                             float& sf) {
+  if (!(m == m)) return false;            // invalid sample
+  if (m < mlo || m > mhi) return false;   // outside the moving range
+  const float sp = C.spacing_f;
+  const float pa = (f - C.fmin_f) * C.finv_f, pb = (m - C.mmin_f) * C.minv_f;
+  const float ca = (pa - C.origin_f) * C.inv_spacing_f, cb = (pb - C.origin_f) * C.inv_spacing_f;
+  if (!(ca >= -0.5f && ca < (float)B - 0.5f && cb >= -0.5f && cb < (float)B - 0.5f)) return false;
+  const float jv = jhmi_interp2(pdf, B, ca, cb);
+  float l = pb - 0.5f * sp, r = pb + 0.5f * sp;
+  l = fminf(fmaxf(l, sp), 1.f);
+  r = fminf(fmaxf(r, sp), 1.f);
+  float dj = 0.f, dm = 0.f;
+  const float delta = r - l;
+  if (delta > 0.f) {
+    const float cl = (l - C.origin_f) * C.inv_spacing_f, cr = (r - C.origin_f) * C.inv_spacing_f;
+    dj = (jhmi_interp2(pdf, B, ca, cr) - jhmi_interp2(pdf, B, ca, cl)) / delta;
+    dm = (jhmi_interp1(mm, B, cr) - jhmi_interp1(mm, B, cl)) / delta;
+  }
+  const float mv = jhmi_interp1(mm, B, cb);
+  sf = 0.f;
+  if (jv > 1e-16f && mv > 1e-16f) {
+    const float t1 = fminf(fmaxf(dj / jv, -max_slope), max_slope);
+    const float t2 = fminf(fmaxf(dm / mv, -max_slope), max_slope);
+    sf = (t1 - t2) * inv_scale;
+  }
+  return true;
+}
+
 // k_jhmi_pass2: the derivative.  Dynamic shared memory: the B^2 + B FP32 tables.
 template <int GRAD>
 __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiConsts* __restrict__ gC, VGrid vg) {
@@ -255,7 +289,6 @@ __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiCon
   __syncthreads();
   const float* pdf = tab;
   const float* mm = tab + B * B;
-  const float sp = C.spacing_f;
   const float max_slope = (float)(36.841361487904734 / C.spacing);  // -log(1e-16) / spacing
   const float inv_scale = (float)(1.0 / (0.69314718055994530942 * (C.mmax - C.mmin)));
   const float mlo = (float)C.mmin, mhi = (float)C.mmax;  // exact: the true min / max are float values
@@ -266,31 +299,9 @@ __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiCon
   const int64_t stride = (int64_t)vg.n * blockDim.x;
   for (int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x; i < a.n; i += stride) {
     const float4 cc = __ldcs(a.cache + i);
-    const float m = cc.x;
-    if (!(m == m)) continue;                                  // invalid sample
-    if (m < mlo || m > mhi) continue;                         // outside the moving range
     const float4 s = __ldcs(a.samples + i);
-    const float pa = (s.w - C.fmin_f) * C.finv_f, pb = (m - C.mmin_f) * C.minv_f;
-    const float ca = (pa - C.origin_f) * C.inv_spacing_f, cb = (pb - C.origin_f) * C.inv_spacing_f;
-    if (!(ca >= -0.5f && ca < (float)B - 0.5f && cb >= -0.5f && cb < (float)B - 0.5f)) continue;
-    const float jv = jhmi_interp2(pdf, B, ca, cb);
-    float l = pb - 0.5f * sp, r = pb + 0.5f * sp;
-    l = fminf(fmaxf(l, sp), 1.f);
-    r = fminf(fmaxf(r, sp), 1.f);
-    float dj = 0.f, dm = 0.f;
-    const float delta = r - l;
-    if (delta > 0.f) {
-      const float cl = (l - C.origin_f) * C.inv_spacing_f, cr = (r - C.origin_f) * C.inv_spacing_f;
-      dj = (jhmi_interp2(pdf, B, ca, cr) - jhmi_interp2(pdf, B, ca, cl)) / delta;
-      dm = (jhmi_interp1(mm, B, cr) - jhmi_interp1(mm, B, cl)) / delta;
-    }
-    const float mv = jhmi_interp1(mm, B, cb);
-    float sf = 0.f;
-    if (jv > 1e-16f && mv > 1e-16f) {
-      const float t1 = fminf(fmaxf(dj / jv, -max_slope), max_slope);
-      const float t2 = fminf(fmaxf(dm / mv, -max_slope), max_slope);
-      sf = (t1 - t2) * inv_scale;
-    }
+    float sf;
+    if (!jhmi_scaling(C, pdf, mm, B, s.w, cc.x, mlo, mhi, max_slope, inv_scale, sf)) continue;
     ++nv;
     const float3 v = jac_vec(K, s.x, s.y, s.z);
     const float t0 = sf * cc.y, t1 = sf * cc.z, t2 = sf * cc.w;
@@ -328,6 +339,111 @@ __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiCon
 template <int GRAD>
 __global__ void __launch_bounds__(kBlock) k_jhmi_pass2(EvalArgs a, const JhmiConsts* C) {
   jhmi_pass2_body<GRAD>(a, C, hw_grid());
+}
+
+// ---------------------------------------------------------------------------
+// B-spline and [affine, B-spline] composite transforms: pass 1 with the B-spline
+// position (nodes staged in shared memory when they fit), caching (m, M^T g);
+// the same finalize; pass 2 turns each cached sample into its derivative factor
+// a_s = sf M^T g (zero for an invalid sample or one outside the B-spline's valid
+// region) in place, counts the derivative points, and leaves the sparse Jacobian
+// sums to the B-spline chunk and parameter kernels (MeanSquares form: sum / count).
+
+__device__ __forceinline__ void load_jhmi(const JhmiConsts* __restrict__ gC, JhmiConsts& C) {
+  const unsigned* src = reinterpret_cast<const unsigned*>(gC);
+  unsigned* dst = reinterpret_cast<unsigned*>(&C);
+  for (int k = threadIdx.x; k < (int)(sizeof(JhmiConsts) / 4); k += blockDim.x) dst[k] = __ldg(src + k);
+}
+
+// Dynamic shared memory: the B^2 histogram, then (16-byte aligned) the nodes.
+__host__ __device__ inline size_t jhmi_bspline_node_offset(int B) { return ((size_t)4 * B * B + 15) / 16 * 16; }
+
+template <int GRAD, bool SMEM>
+__global__ void __launch_bounds__(kBlock) k_jhmi_pass1_bspline(EvalArgs a, const JhmiConsts* gC) {
+  extern __shared__ __align__(16) unsigned char smem_jb[];
+  unsigned* hist_s = reinterpret_cast<unsigned*>(smem_jb);
+  __shared__ EvalConsts K;
+  __shared__ JhmiConsts C;
+  const int B = a.bins;
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) hist_s[k] = 0u;
+  griddep_wait();
+  if (halted(a)) return;
+  griddep_launch_dependents();
+  load_consts(a.consts, K);
+  load_jhmi(gC, C);
+  const float4* nodes = stage_nodes<SMEM>(a, reinterpret_cast<float4*>(smem_jb + jhmi_bspline_node_offset(B)));
+  __syncthreads();
+  unsigned nv = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 s = __ldcs(a.samples + i);
+    const float4 su = __ldcs(a.sup + i);
+    bool has_jac;
+    const DFPos p = bspline_position(K, nodes, a, s, su, has_jac);
+    float m = 0.f;
+    float3 g = make_float3(0.f, 0.f, 0.f);
+    const bool ok = eval_moving<GRAD>(a, p, a.with_derivative != 0 && has_jac, m, g);
+    if (a.with_derivative) {
+      const float3 gm = has_jac ? grad_map(K, g) : make_float3(0.f, 0.f, 0.f);
+      __stcs(a.cache + i, ok ? make_float4(m, gm.x, gm.y, gm.z) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f));
+    }
+    if (!ok) continue;
+    const int fb = jhmi_bin(s.w, C.fmin_f, C.finv_f, C.fmin, C.fmax, C, B);
+    const int mb = jhmi_bin(m, C.mmin_f, C.minv_f, C.mmin, C.mmax, C, B);
+    if (fb < 0 || mb < 0) continue;
+    atomicAdd(&hist_s[fb + B * mb], 1u);
+    ++nv;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < B * B; k += blockDim.x) {
+    const unsigned h = hist_s[k];
+    if (h) atomicAdd(&a.hist[k], (unsigned long long)h);
+  }
+  block_count(nv, a.acc_n);
+}
+
+// Pass 2 for the B-spline: a_s into the cache, the count into fmarg[0] (a spare
+// accumulator here); the last block makes the count the one the parameter kernel
+// divides by, and sets the status (no derivative point: a warning, value max).
+__global__ void __launch_bounds__(kBlock) k_jhmi_pass2_bspline(EvalArgs a, const JhmiConsts* gC) {
+  extern __shared__ float tab[];
+  __shared__ JhmiConsts C;
+  const int B = a.bins;
+  griddep_wait();
+  if (halted(a)) return;
+  griddep_launch_dependents();
+  for (int k = threadIdx.x; k < B * B + B; k += blockDim.x) tab[k] = __ldcg(&a.pratio[k]);
+  load_jhmi(gC, C);
+  __syncthreads();
+  const float max_slope = (float)(36.841361487904734 / C.spacing);  // -log(1e-16) / spacing
+  const float inv_scale = (float)(1.0 / (0.69314718055994530942 * (C.mmax - C.mmin)));
+  const float mlo = (float)C.mmin, mhi = (float)C.mmax;
+  unsigned nv = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 cc = __ldcg(a.cache + i);
+    const float f = __ldcs(&a.samples[i].w);
+    float sf;
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (jhmi_scaling(C, tab, tab + B * B, B, f, cc.x, mlo, mhi, max_slope, inv_scale, sf)) {
+      ++nv;
+      out = make_float4(sf * cc.y, sf * cc.z, sf * cc.w, 1.f);
+    }
+    __stcg(a.cache + i, out);
+  }
+  block_count(nv, a.fmarg);
+  if (!last_block(a.tickets + kTicketPass2)) return;
+  if (threadIdx.x == 0) {
+    const unsigned long long N = __ldcg(a.fmarg);
+    *a.acc_n = N;
+    a.out[1] = (double)N;
+    if (N == 0) {
+      a.out[0] = DBL_MAX;
+      *a.status = GB_ERR_NO_VALID_POINTS;
+    } else {
+      *a.status = GB_OK;
+    }
+  }
 }
 
 }  // namespace gb

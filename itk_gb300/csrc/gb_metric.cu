@@ -208,7 +208,9 @@ static void bspline_init_affine(const gb_metric* m, double p[12], double c[3]) {
 // they leave room for at least two resident blocks per SM, else read from HBM/L2.
 static size_t bspline_node_bytes(const gb_metric* m) { return (size_t)m->nper * sizeof(float4); }
 static bool nodes_in_smem(const gb_metric* m) {
-  const size_t base = m->kind == GB_METRIC_MATTES ? mattes_bspline_node_offset((int)m->bins) : 0;
+  const size_t base = m->kind == GB_METRIC_MATTES                ? mattes_bspline_node_offset((int)m->bins)
+                      : m->kind == GB_METRIC_JOINT_HISTOGRAM_MI ? jhmi_bspline_node_offset((int)m->bins)
+                                                                : 0;
   return base + bspline_node_bytes(m) <= 96 * 1024;
 }
 
@@ -542,8 +544,8 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
   if ((bspline || field) && m->kind == GB_METRIC_CORRELATION)
     return fail(GB_ERR_UNSUPPORTED, "the correlation metric runs affine transforms");
   const bool jhmi = m->kind == GB_METRIC_JOINT_HISTOGRAM_MI;
-  if (jhmi && m->tkind != GB_TRANSFORM_AFFINE)
-    return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric runs affine transforms");
+  if (jhmi && field)
+    return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric runs affine, B-spline and composite transforms");
   if (jhmi && (m->bins < 6 || m->bins > kJhmiMaxBins))
     return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric takes 6 to 64 bins");
   // the floating point correction acts where points store a global derivative
@@ -1144,21 +1146,55 @@ static int enqueue_eval_field(gb_metric* m, const EvalArgs& a, bool cd, bool der
 
 // Joint-histogram MI: the histogram pass, the one-block PDF / value kernel, the
 // derivative pass.
-static int enqueue_eval_jhmi(gb_metric* m, const EvalArgs& a, bool cd, bool deriv) {
+static int enqueue_eval_jhmi(gb_metric* m, const EvalArgs& a, bool cd, bool deriv, bool device_params) {
   const int B = (int)m->bins;
   const JhmiConsts* C = reinterpret_cast<const JhmiConsts*>(m->d_jhmi.p);
-  const size_t sh1 = sizeof(unsigned) * B * B;
-  GB_CUDA(cd ? launch_wave(m, k_jhmi_pass1<kGradCentralDifference>, sh1, a, C)
-             : launch_wave(m, k_jhmi_pass1<kGradImage>, sh1, a, C));
+  const bool bs = is_bspline(m);
+  if (bs) {
+    const bool sm = a.nodes_smem != 0;
+    if (device_params) {  // the host call uploads converted nodes
+      GB_CUDA(launch_chain(m, k_prepare_bspline, (unsigned)((m->nper + kBlock - 1) / kBlock), kBlock, 0, a));
+      m->mark();
+    }
+    const size_t sh1 = jhmi_bspline_node_offset(B) + (sm ? bspline_node_bytes(m) : 0);
+    cudaError_t e;
+    if (cd) e = sm ? launch_wave(m, k_jhmi_pass1_bspline<kGradCentralDifference, true>, sh1, a, C)
+                   : launch_wave(m, k_jhmi_pass1_bspline<kGradCentralDifference, false>, sh1, a, C);
+    else e = sm ? launch_wave(m, k_jhmi_pass1_bspline<kGradImage, true>, sh1, a, C)
+                : launch_wave(m, k_jhmi_pass1_bspline<kGradImage, false>, sh1, a, C);
+    GB_CUDA(e);
+  } else {
+    const size_t sh1 = sizeof(unsigned) * B * B;
+    GB_CUDA(cd ? launch_wave(m, k_jhmi_pass1<kGradCentralDifference>, sh1, a, C)
+               : launch_wave(m, k_jhmi_pass1<kGradImage>, sh1, a, C));
+  }
   m->mark();
   const size_t shf = sizeof(double) * (2 * B * B + 2 * B);
   GB_CUDA(cudaFuncSetAttribute(k_jhmi_finalize, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shf));
   GB_CUDA(launch_chain(m, k_jhmi_finalize, (unsigned)kJhmiFinalizeBlocks, kBlock, shf, a, C));
   m->mark();
-  if (deriv) {
+  if (deriv && !bs) {
     const size_t sh2 = sizeof(float) * (B * B + B);
     GB_CUDA(cd ? launch_wave(m, k_jhmi_pass2<kGradCentralDifference>, sh2, a, C)
                : launch_wave(m, k_jhmi_pass2<kGradImage>, sh2, a, C));
+    m->mark();
+  } else if (deriv) {
+    // per-sample factors, then the B-spline's sparse Jacobian sums (MeanSquares form)
+    const size_t sh2 = sizeof(float) * (B * B + B);
+    GB_CUDA(launch_wave(m, k_jhmi_pass2_bspline, sh2, a, C));
+    m->mark();
+    if (m->nchunks > 0) {
+      GB_CUDA(launch_chain(m, k_bspline_chunks<false>, (unsigned)m->nchunks, kChunkLen, 0, a));
+      m->mark();
+    }
+    const int nper = (int)m->nper;
+    if (m->node_entries_count >= (int64_t)kParamsBlock * nper) {
+      GB_CUDA(launch_chain(m, k_bspline_params<false, true>, (unsigned)nper, kParamsBlock, 0, a));
+    } else {
+      const int64_t threads = (int64_t)nper * 32;
+      GB_CUDA(launch_chain(m, k_bspline_params<false, false>, (unsigned)((threads + kParamsBlock - 1) / kParamsBlock),
+                           kParamsBlock, 0, a));
+    }
     m->mark();
   }
   return GB_OK;
@@ -1187,9 +1223,9 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
   const bool cd = m->grad_source == GB_GRADIENT_CENTRAL_DIFFERENCE;
   m->nevents = 0;
   m->mark();
+  if (m->kind == GB_METRIC_JOINT_HISTOGRAM_MI) return enqueue_eval_jhmi(m, a, cd, deriv, device_params);
   if (is_bspline(m)) return enqueue_eval_bspline(m, a, cd, deriv, device_params);
   if (is_field(m)) return enqueue_eval_field(m, a, cd, deriv);
-  if (m->kind == GB_METRIC_JOINT_HISTOGRAM_MI) return enqueue_eval_jhmi(m, a, cd, deriv);
   if (m->kind == GB_METRIC_CORRELATION) {
     // averages, then the value and derivative (at most kCorrMaxBlocks blocks: 27 partials each)
     GB_CUDA(cd ? launch_wave(m, k_corr_mean_affine<kGradCentralDifference>, 0, a)

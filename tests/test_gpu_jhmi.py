@@ -158,6 +158,33 @@ def test_bins_and_transform_limits(pair):
     fixed, moving, T = pair
     with pytest.raises(ExceptionObject, match="6 to 64 bins"):
         make(fixed, moving, perturbed(T, 1), bins=65)
-    B = data.random_bspline_coefficients(data.bspline_over_image(fixed, (3, 3, 3)), seed=1)
-    with pytest.raises(ExceptionObject, match="affine"):
-        make(fixed, moving, B)
+    from itk_gb300 import DisplacementFieldImage, DisplacementFieldTransform
+    F = DisplacementFieldTransform()
+    F.SetDisplacementField(DisplacementFieldImage.like(fixed))
+    with pytest.raises(ExceptionObject, match="affine, B-spline and composite"):
+        make(fixed, moving, F)
+
+
+@pytest.mark.parametrize("composite", [False, True])
+@pytest.mark.parametrize("sampled", [False, True])
+@pytest.mark.parametrize("gradient", ["image", "cd"])
+def test_bspline_matches_oracle(pair, composite, sampled, gradient):
+    """B-spline and [affine, B-spline] composite transforms: the B-spline pass 1, the
+    per-sample derivative factors and the sparse Jacobian sums against the oracle."""
+    from itk_gb300 import CompositeTransform
+    fixed, moving, T = pair
+    B = data.random_bspline_coefficients(data.bspline_over_image(fixed, (3, 3, 3)), seed=4, max_disp=2.0)
+    if composite:
+        U = CompositeTransform()
+        U.AddTransform(perturbed(T, 5))
+        U.AddTransform(B)
+    else:
+        U = B
+    pts = data.random_points(fixed, 0.3, seed=9) if sampled else None
+    m = make(fixed, moving, U, gradient, pts)
+    v, d = m.GetValueAndDerivative()
+    rc, rv, rd, nv, pdf = oracle(fixed, moving, U, gradient, pts)
+    assert rc == 0 and m.GetNumberOfValidPoints() == nv
+    assert_value_close(v, rv)
+    assert_deriv_close(d, rd)
+    assert m.GetValue() == v
