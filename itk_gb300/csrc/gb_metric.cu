@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "gb_bspline.cuh"
+#include "gb_corr_bspline.cuh"
 #include "gb_field.cuh"
 #include "gb_jhmi.cuh"
 #include "gb_init.cuh"
@@ -541,8 +542,8 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     return fail(GB_ERR_BAD_ARG, "gradient source is a gradient image but none was set");
   const bool bspline = is_bspline(m);
   const bool field = is_field(m);
-  if ((bspline || field) && m->kind == GB_METRIC_CORRELATION)
-    return fail(GB_ERR_UNSUPPORTED, "the correlation metric runs affine transforms");
+  if (field && m->kind == GB_METRIC_CORRELATION)
+    return fail(GB_ERR_UNSUPPORTED, "the correlation metric runs affine, B-spline and composite transforms");
   const bool jhmi = m->kind == GB_METRIC_JOINT_HISTOGRAM_MI;
   if (jhmi && field)
     return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric runs affine, B-spline and composite transforms");
@@ -1144,6 +1145,54 @@ static int enqueue_eval_field(gb_metric* m, const EvalArgs& a, bool cd, bool der
   return GB_OK;
 }
 
+// The B-spline chunk sums and the per-parameter gather of per-sample factors in the
+// cache (the MeanSquares form: sums / count).
+static int enqueue_bspline_sums(gb_metric* m, const EvalArgs& a) {
+  if (m->nchunks > 0) {
+    GB_CUDA(launch_chain(m, k_bspline_chunks<false>, (unsigned)m->nchunks, kChunkLen, 0, a));
+    m->mark();
+  }
+  const int nper = (int)m->nper;
+  if (m->node_entries_count >= (int64_t)kParamsBlock * nper) {
+    GB_CUDA(launch_chain(m, k_bspline_params<false, true>, (unsigned)nper, kParamsBlock, 0, a));
+  } else {
+    const int64_t threads = (int64_t)nper * 32;
+    GB_CUDA(launch_chain(m, k_bspline_params<false, false>, (unsigned)((threads + kParamsBlock - 1) / kParamsBlock),
+                         kParamsBlock, 0, a));
+  }
+  m->mark();
+  return GB_OK;
+}
+
+// Correlation, B-spline / composite: averages, the sums and value, the per-sample
+// factors, the sparse Jacobian sums.
+static int enqueue_eval_corr_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool deriv, bool device_params) {
+  const bool sm = a.nodes_smem != 0;
+  const size_t nb = sm ? bspline_node_bytes(m) : 0;
+  if (device_params) {
+    GB_CUDA(launch_chain(m, k_prepare_bspline, (unsigned)((m->nper + kBlock - 1) / kBlock), kBlock, 0, a));
+    m->mark();
+  }
+  cudaError_t e;
+  if (cd) e = sm ? launch_wave(m, k_corr_mean_bspline<kGradCentralDifference, true>, nb, a)
+                 : launch_wave(m, k_corr_mean_bspline<kGradCentralDifference, false>, nb, a);
+  else e = sm ? launch_wave(m, k_corr_mean_bspline<kGradImage, true>, nb, a)
+              : launch_wave(m, k_corr_mean_bspline<kGradImage, false>, nb, a);
+  GB_CUDA(e);
+  m->mark();
+  if (deriv) e = launch_wave(m, k_corr_sums_bspline<kGradImage, false, false>, 0, a);
+  else if (cd) e = sm ? launch_wave(m, k_corr_sums_bspline<kGradCentralDifference, true, true>, nb, a)
+                      : launch_wave(m, k_corr_sums_bspline<kGradCentralDifference, false, true>, nb, a);
+  else e = sm ? launch_wave(m, k_corr_sums_bspline<kGradImage, true, true>, nb, a)
+              : launch_wave(m, k_corr_sums_bspline<kGradImage, false, true>, nb, a);
+  GB_CUDA(e);
+  m->mark();
+  if (!deriv) return GB_OK;
+  GB_CUDA(launch_wave(m, k_corr_factor_bspline, 0, a));
+  m->mark();
+  return enqueue_bspline_sums(m, a);
+}
+
 // Joint-histogram MI: the histogram pass, the one-block PDF / value kernel, the
 // derivative pass.
 static int enqueue_eval_jhmi(gb_metric* m, const EvalArgs& a, bool cd, bool deriv, bool device_params) {
@@ -1183,19 +1232,7 @@ static int enqueue_eval_jhmi(gb_metric* m, const EvalArgs& a, bool cd, bool deri
     const size_t sh2 = sizeof(float) * (B * B + B);
     GB_CUDA(launch_wave(m, k_jhmi_pass2_bspline, sh2, a, C));
     m->mark();
-    if (m->nchunks > 0) {
-      GB_CUDA(launch_chain(m, k_bspline_chunks<false>, (unsigned)m->nchunks, kChunkLen, 0, a));
-      m->mark();
-    }
-    const int nper = (int)m->nper;
-    if (m->node_entries_count >= (int64_t)kParamsBlock * nper) {
-      GB_CUDA(launch_chain(m, k_bspline_params<false, true>, (unsigned)nper, kParamsBlock, 0, a));
-    } else {
-      const int64_t threads = (int64_t)nper * 32;
-      GB_CUDA(launch_chain(m, k_bspline_params<false, false>, (unsigned)((threads + kParamsBlock - 1) / kParamsBlock),
-                           kParamsBlock, 0, a));
-    }
-    m->mark();
+    return enqueue_bspline_sums(m, a);
   }
   return GB_OK;
 }
@@ -1224,6 +1261,7 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
   m->nevents = 0;
   m->mark();
   if (m->kind == GB_METRIC_JOINT_HISTOGRAM_MI) return enqueue_eval_jhmi(m, a, cd, deriv, device_params);
+  if (m->kind == GB_METRIC_CORRELATION && is_bspline(m)) return enqueue_eval_corr_bspline(m, a, cd, deriv, device_params);
   if (is_bspline(m)) return enqueue_eval_bspline(m, a, cd, deriv, device_params);
   if (is_field(m)) return enqueue_eval_field(m, a, cd, deriv);
   if (m->kind == GB_METRIC_CORRELATION) {

@@ -132,3 +132,29 @@ def test_device_optimizer_matches_host_loop(pair):
     assert o.GetStopCondition() == h["stop"] and o.GetCurrentIteration() == h["iterations"]
     assert np.max(np.abs(U.GetParameters() - h["params"])) <= 1e-9 * max(np.max(np.abs(h["params"])), 1.0)
     assert o.GetValue() < -0.5  # correlated
+
+
+@pytest.mark.parametrize("composite", [False, True])
+@pytest.mark.parametrize("sampled", [False, True])
+@pytest.mark.parametrize("gradient_image", [True, False])
+def test_bspline_matches_oracle(pair, composite, sampled, gradient_image):
+    """B-spline and [affine, B-spline] composites: the derivative from per-sample factors
+    2 fm / (f2 m2) (f1 - fm / m2 m1) M^T g through the B-spline chunk and parameter sums."""
+    from itk_gb300 import CompositeTransform
+    fixed, moving, T = pair
+    B = data.random_bspline_coefficients(data.bspline_over_image(fixed, (3, 3, 3)), seed=6, max_disp=2.0)
+    if composite:
+        U = CompositeTransform()
+        U.AddTransform(perturbed(T, 7))
+        U.AddTransform(B)
+    else:
+        U = B
+    grad = data.gradient_image(moving) if gradient_image else None
+    pts = data.random_points(fixed, 0.3, seed=3) if sampled else None
+    m = make(fixed, moving, U, grad, pts)
+    v, d = m.GetValueAndDerivative()
+    rc, rv, rd, nv = oracle(fixed, moving, U, grad, pts)
+    assert rc == 0 and m.GetNumberOfValidPoints() == nv
+    assert_value_close(v, rv)
+    assert_deriv_close(d, rd)
+    assert m.GetValue() == pytest.approx(v, rel=1e-12)
