@@ -294,8 +294,8 @@ class MeanSquaresImageToImageMetricv4(ImageToImageMetricv4):
 
 class CorrelationImageToImageMetricv4(ImageToImageMetricv4):
     """Normalized cross correlation: value -(sum f1 m1)^2 / (sum f1^2 sum m1^2) with
-    f1, m1 the intensities less their averages over the valid points (affine
-    transforms)."""
+    f1, m1 the intensities less their averages over the valid points (affine,
+    B-spline and [affine, B-spline] transforms)."""
 
     _kind = _capi.GB_METRIC_CORRELATION
 
@@ -304,7 +304,7 @@ class JointHistogramMutualInformationImageToImageMetricv4(ImageToImageMetricv4):
     """Joint-histogram mutual information (value -MI in bits): counts of (fixed, moving)
     intensity bins over the valid points, normalized and smoothed by a discrete
     Gaussian; the derivative from the smoothed PDF's slope along the moving axis
-    (affine transforms; default 20 bins, variance 1.5)."""
+    (affine, B-spline and [affine, B-spline] transforms; default 20 bins, variance 1.5)."""
 
     _kind = _capi.GB_METRIC_JOINT_HISTOGRAM_MI
 
