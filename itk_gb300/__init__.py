@@ -4,7 +4,7 @@ GetValueAndDerivative of MeanSquaresImageToImageMetricv4 and
 MattesMutualInformationImageToImageMetricv4 on Image<float,3> under affine,
 B-spline, [affine, B-spline] composite and displacement-field transforms (and
 CorrelationImageToImageMetricv4 and JointHistogramMutualInformationImageToImageMetricv4
-under affine transforms), computed by hand-written
+under affine and B-spline transforms), computed by hand-written
 sm_103a CUDA kernels behind the C ABI in include/itk_gb300.h.
 """
 from ._capi import ExceptionObject, lib, library_path
