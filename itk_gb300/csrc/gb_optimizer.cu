@@ -53,9 +53,18 @@ __global__ void __launch_bounds__(kStepBlock) k_step_reduce(StepArgs s) {
   griddep_launch_dependents();
   const int status = __ldcg(s.status);
   const bool err = metric_error(s, status);
-  const long long j = (long long)blockIdx.x * kStepBlock + threadIdx.x;
   DD q = {0.0, 0.0}, r = {0.0, 0.0};
-  if (j < s.P && !err) step_terms(s, j, q.hi, r.hi);
+  if (!err) {
+    // one parameter per thread up to the grid's size, a grid-stride run of them beyond
+    // (a displacement field's millions); each thread's terms added by two-sum
+    const long long stride = (long long)gridDim.x * kStepBlock;
+    for (long long j = (long long)blockIdx.x * kStepBlock + threadIdx.x; j < s.P; j += stride) {
+      double qq, rr;
+      step_terms(s, j, qq, rr);
+      q = dd_add(q, DD{qq, 0.0});
+      r = dd_add(r, DD{rr, 0.0});
+    }
+  }
   block_dd2(q, r);
   __shared__ bool last;
   if (threadIdx.x == 0) {
@@ -93,8 +102,8 @@ __global__ void __launch_bounds__(kStepBlock) k_step_apply(StepArgs s) {
   griddep_launch_dependents();
   const OptState* S = s.st;
   const int act = __ldcg(&S->action);
-  const long long j = (long long)blockIdx.x * kStepBlock + threadIdx.x;
-  if (j < s.P) step_apply(s, S, act, j);
+  const long long stride = (long long)gridDim.x * kStepBlock;
+  for (long long j = (long long)blockIdx.x * kStepBlock + threadIdx.x; j < s.P; j += stride) step_apply(s, S, act, j);
 }
 
 // The whole step of a registration with at most 32 parameters in one warp
@@ -194,8 +203,7 @@ int opt_setup(gb_metric* m, const gb_regular_step_settings* cfg, const double* s
   if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
   const int64_t P = (int64_t)m->tparams.size();
   if (P <= 0) return fail(GB_ERR_BAD_ARG, "the moving transform has no parameters");
-  if (P > (int64_t)kStepBlock * kStepMaxBlocks)
-    return fail(GB_ERR_UNSUPPORTED, "more than 16384 parameters in the device optimizer");
+  if (P > (int64_t)0x7fffffff) return fail(GB_ERR_UNSUPPORTED, "more than 2^31-1 parameters in the device optimizer");
   if (cfg->number_of_iterations < 0) return fail(GB_ERR_BAD_ARG, "number of iterations must be >= 0");
   if (cfg->gradient_magnitude_tolerance < 0.0)
     return fail(GB_ERR_BAD_ARG, "Gradient magnitude tolerance must be greater or equal 0.0. Current value is " +
@@ -326,7 +334,7 @@ extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_st
   if (rc) return rc;
   cudaStream_t st = m->stream;
   OptState* S = a.st;
-  const unsigned blocks = (unsigned)((a.P + kStepBlock - 1) / kStepBlock);
+  const unsigned blocks = (unsigned)std::min<int64_t>(kStepMaxBlocks, (a.P + kStepBlock - 1) / kStepBlock);
 
   LoopGuard guard{m, m->profiling};
   m->profiling = false;

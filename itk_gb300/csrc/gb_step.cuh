@@ -21,7 +21,7 @@
 namespace gb {
 
 constexpr int kStepBlock = 256;
-constexpr int kStepMaxBlocks = 64;  // up to 16384 parameters in the multi-block step
+constexpr int kStepMaxBlocks = 256;  // blocks of the multi-block step (grid-stride beyond 65536 parameters)
 
 enum { kActNone = 0, kActStep = 1, kActRestoreBest = 2 };
 enum { kRunning = -1 };

@@ -189,3 +189,29 @@ def test_oblique_grids_match_oracle(pair, kind):
     assert rc == 0 and m.GetNumberOfValidPoints() == nv
     assert_value_close(v, rv)
     assert_deriv_close(d, rd)
+
+
+def test_device_optimizer_many_parameters(pair):
+    """The device RegularStep loop on a field of 138,240 parameters (grid-stride step
+    kernels) against the oracle's RegularStep restatement driven by the same metric."""
+    fixed, moving = pair
+    T = field_transform(fixed, np.zeros(fixed.array.shape + (3,)))
+    p0 = T.GetParameters().copy()
+    assert p0.size > 65536
+    m = make("mattes", fixed, moving, T, data.gradient_image(moving))
+
+    def evaluate(p):
+        T.SetParameters(p)
+        v, d = m.GetValueAndDerivative()
+        return 0, v, d
+
+    h = R.regular_step(evaluate, p0, learning_rate=1.0, minimum_step_length=1e-3, number_of_iterations=8)
+    T.SetParameters(p0)
+    o = RegularStepGradientDescentOptimizerv4()
+    o.SetMetric(m)
+    o.SetLearningRate(1.0)
+    o.SetMinimumStepLength(1e-3)
+    o.SetNumberOfIterations(8)
+    o.StartOptimization()
+    assert o.GetStopCondition() == h["stop"] and o.GetCurrentIteration() == h["iterations"]
+    assert np.max(np.abs(T.GetParameters() - h["params"])) <= 1e-9 * max(np.max(np.abs(h["params"])), 1.0)
