@@ -195,7 +195,8 @@ class ImageToImageMetricv4:
         p = view() if view is not None else f64(self._transform.GetParameters())
         if p.size != self._nparams:
             raise ExceptionObject(_capi.GB_ERR_BAD_ARG, "transform parameter count changed; call Initialize()")
-        check(self._L.gb_metric_set_parameters(self._h, ptr(p), p.size))
+        # .ctypes.data: the array is held by the local name for the call (data_as costs ~2 us)
+        check(self._L.gb_metric_set_parameters(self._h, p.ctypes.data, p.size))
 
     def _handle_status(self, rc):
         if rc == _capi.GB_OK:
@@ -210,7 +211,7 @@ class ImageToImageMetricv4:
         self._sync_params()
         value = np.zeros(1)
         deriv = np.empty(self._nparams)  # every entry is written by the call
-        rc = self._L.gb_metric_get_value_and_derivative(self._h, ptr(value), ptr(deriv), self._nparams)
+        rc = self._L.gb_metric_get_value_and_derivative(self._h, value.ctypes.data, deriv.ctypes.data, self._nparams)
         self._handle_status(rc)
         self._value = float(value[0])
         return self._value, deriv
