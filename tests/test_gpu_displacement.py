@@ -215,3 +215,38 @@ def test_device_optimizer_many_parameters(pair):
     o.StartOptimization()
     assert o.GetStopCondition() == h["stop"] and o.GetCurrentIteration() == h["iterations"]
     assert np.max(np.abs(T.GetParameters() - h["params"])) <= 1e-9 * max(np.max(np.abs(h["params"])), 1.0)
+
+
+@pytest.mark.parametrize("kind", ["msq", "mattes"])
+def test_virtual_domain_with_dropped_voxels(pair, kind):
+    """A virtual domain shifted by half a voxel: its last plane falls outside the fixed
+    image, those voxels hold no sample, and the derivative field is cleared before the
+    blocks are stored (the other voxels' blocks as the oracle's)."""
+    fixed, moving = pair
+    virt = Image(np.zeros(fixed.array.shape, np.float32), spacing=fixed.spacing, origin=fixed.origin + 0.5,
+                 direction=fixed.direction)
+    T = field_transform(virt, data.smooth_displacement_field(virt, seed=13, max_disp=1.5).array)
+    grad = data.gradient_image(moving)
+    m = MeanSquaresImageToImageMetricv4() if kind == "msq" else MattesMutualInformationImageToImageMetricv4()
+    if kind != "msq":
+        m.SetNumberOfHistogramBins(BINS)
+    m.SetFixedImage(fixed)
+    m.SetMovingImage(moving)
+    m.SetVirtualDomainFromImage(virt)
+    m.SetMovingTransform(T)
+    m.SetMovingImageGradientImage(grad)
+    m.Initialize()
+    v, d = m.GetValueAndDerivative()
+    assert m.GetNumberOfDomainPoints() == virt.array.size
+    g = grad.array
+    if kind == "msq":
+        rc, rv, rd, nv = O.mean_squares(fixed.array, geom(fixed), moving.array, geom(moving), oracle_transform(T),
+                                        moving_grad=g, virtual_geom=geom(virt))
+    else:
+        rc, rv, rd, nv, _, _ = O.mattes(fixed.array, geom(fixed), moving.array, geom(moving), oracle_transform(T),
+                                        bins=BINS, moving_grad=g, virtual_geom=geom(virt))
+    assert rc == 0 and m.GetNumberOfValidPoints() == nv < virt.array.size
+    assert_value_close(v, rv)
+    assert_deriv_close(d, rd)
+    blocks = np.asarray(d).reshape(virt.array.shape + (3,))
+    assert not np.any(blocks[:, :, -1])  # the last x plane maps outside the fixed image
