@@ -167,6 +167,9 @@ int gb_metric_use_sampled_point_set(gb_metric *m, int on);
  *             the derivative is a field too, each point's block added at its
  *             virtual voxel and not divided by the number of valid points
  *             (Registration/Metricsv4/include/itkImageToImageMetricv4GetValueAndDerivativeThreaderBase.hxx:128-172,276-327).
+ *             fixed = 33 appends an initial affine (12 parameters, centre 3): the
+ *             CompositeTransform [affine, displacement field], the field applied
+ *             first and optimized, the local derivative M^T-mapped.
  *             MeanSquares and Mattes only. */
 int gb_metric_set_moving_transform(gb_metric *m, int kind, const double *params, int64_t nparams,
                                    const double *fixed, int64_t nfixed);

@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(kBlock) k_msq_field(EvalArgs a) {
       acc[0].add(diff * diff);
       ++nv;
     }
-    if (deriv) field_store<TK>(a, voxel, ok, 2.f * diff, g);
+    if (deriv) field_store<TK>(a, voxel, ok, 2.f * diff, field_grad(K, g));
   }
   block_count(nv, a.acc_n);
   block_sums<1>(acc, red, blk);

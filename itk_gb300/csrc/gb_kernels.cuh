@@ -664,6 +664,14 @@ __device__ __forceinline__ DFPos field_pos_diag(const EvalConsts& K, float x, fl
   return q;
 }
 
+// A displacement field's local Jacobian product: M^T g behind an initial affine
+// (identity M: g exactly), K.Mg = M^T.
+__device__ __forceinline__ float3 field_grad(const EvalConsts& K, float3 g) {
+  return make_float3(fmaf(K.Mg[0], g.x, fmaf(K.Mg[1], g.y, K.Mg[2] * g.z)),
+                     fmaf(K.Mg[3], g.x, fmaf(K.Mg[4], g.y, K.Mg[5] * g.z)),
+                     fmaf(K.Mg[6], g.x, fmaf(K.Mg[7], g.y, K.Mg[8] * g.z)));
+}
+
 template <int TK>
 __device__ __forceinline__ DFPos sample_pos(const EvalArgs& a, const EvalConsts& K, const float4& s, int64_t i,
                                             unsigned& voxel) {
@@ -919,6 +927,7 @@ __device__ __forceinline__ void mattes_pass1_affine_body(const EvalArgs& a, VGri
       unsigned voxel;
       const DFPos p = sample_pos<TK>(a, K, s, i, voxel);
       ok = eval_moving<GRAD>(a, p, a.with_derivative != 0, m, g);
+      if (TK != kMapAffine) g = field_grad(K, g);
       // reject moving values outside [MovingImageTrueMin, MovingImageTrueMax], Mattes...Threader.hxx:238-245
       ok = ok && !(m < a.mmin) && !(m > a.mmax);
     }

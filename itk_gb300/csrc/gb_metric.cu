@@ -464,7 +464,9 @@ extern "C" int gb_metric_set_moving_transform(gb_metric* m, int kind, const doub
   } else if (kind == GB_TRANSFORM_DISPLACEMENT_FIELD) {
     // DisplacementFieldTransform fixed parameters: size, origin, spacing, direction
     // (itkDisplacementFieldTransform.hxx:520-570); the parameters are the field
-    if (nfixed != 18) return fail(GB_ERR_BAD_ARG, "displacement field fixed parameters: size, origin, spacing, direction (18)");
+    if (nfixed != 18 && nfixed != 33)
+      return fail(GB_ERR_BAD_ARG, "displacement field fixed parameters: size, origin, spacing, direction (18), "
+                                  "+ 15 for the initial affine of a composite");
     int64_t nv = 1;
     for (int i = 0; i < 3; ++i) {
       const double g = fixed[i];
@@ -915,10 +917,21 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     // the displacement-field constants are geometry only: the identity transform's
     // map, the moving image's physical-to-index matrix for the displacement and,
     // for a point set, the physical point -> field continuous index map
-    const double p[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0}, c[3] = {0, 0, 0};
+    // a [affine, field] composite: the map is the initial affine's, the displacement
+    // goes through P2I M and the gradient through M^T (K.Mg)
+    double p[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0}, c[3] = {0, 0, 0};
+    if (m->tfixed.size() == 33) {
+      for (int i = 0; i < 12; ++i) p[i] = m->tfixed[18 + i];
+      for (int i = 0; i < 3; ++i) c[i] = m->tfixed[30 + i];
+    }
     EvalConsts& K = *m->h_consts;
     affine_consts(p, c, m->moving.p2i, m->moving.origin, sampled ? nullptr : m->virt.i2p, m->virt.origin, K);
-    for (int i = 0; i < 9; ++i) split_df(m->moving.p2i[i], K.umap.Ahi[i], K.umap.Alo[i]);
+    for (int r = 0; r < 3; ++r)
+      for (int cc = 0; cc < 3; ++cc) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s = gb::dadd(s, gb::dmul(m->moving.p2i[3 * r + k], p[3 * k + cc]));
+        split_df(s, K.umap.Ahi[3 * r + cc], K.umap.Alo[3 * r + cc]);
+      }
     for (int r = 0; r < 3; ++r) {
       K.umap.bhi[r] = K.umap.blo[r] = 0.f;
       double b = 0.0;

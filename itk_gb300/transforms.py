@@ -15,7 +15,8 @@
   (Filtering/DisplacementField/include/itkDisplacementFieldTransform.hxx:67-100,520-570).
 * ``CompositeTransform`` -- queue applied in reverse
   (Core/Transform/include/itkCompositeTransform.hxx:60-70), the most recently
-  added transform optimized; supported queues: [T] and [affine, B-spline].
+  added transform optimized; supported queues: [T], [affine, B-spline] and
+  [affine, displacement field].
 """
 from __future__ import annotations
 
@@ -305,7 +306,11 @@ class CompositeTransform:
         if len(self.queue) == 2 and isinstance(self.queue[0], AffineTransform) and \
                 isinstance(self.queue[1], BSplineTransform):
             return TRANSFORM_COMPOSITE
-        raise ValueError("supported composite queues: [T] or [AffineTransform, BSplineTransform]")
+        if len(self.queue) == 2 and isinstance(self.queue[0], AffineTransform) and \
+                isinstance(self.queue[1], DisplacementFieldTransform):
+            return TRANSFORM_DISPLACEMENT_FIELD  # the field's flat form with the initial affine appended
+        raise ValueError("supported composite queues: [T], [AffineTransform, BSplineTransform] or "
+                         "[AffineTransform, DisplacementFieldTransform]")
 
     def GetNumberOfParameters(self):
         return self.active.GetNumberOfParameters()
@@ -330,7 +335,7 @@ class CompositeTransform:
         return y
 
     def GetFixedParameters(self):
-        if self.kind == TRANSFORM_COMPOSITE:
+        if self.kind == TRANSFORM_COMPOSITE or len(self.queue) == 2:
             a, b = self.queue
             return np.concatenate([b.GetFixedParameters(), a.GetParameters(), a.GetFixedParameters()])
         return self.active.GetFixedParameters()

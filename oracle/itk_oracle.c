@@ -517,7 +517,13 @@ void orc_transform_point(const orc_transform *t, const double x[3], double y[3])
   if (t->kind == ORC_TRANSFORM_AFFINE) {
     affine_apply(t, x, y);
   } else if (t->kind == ORC_TRANSFORM_DISPLACEMENT) {
-    displacement_apply(t, x, y);
+    if (t->field_affine) {
+      double u[3];
+      displacement_apply(t, x, u);
+      affine_apply(t, u, y);
+    } else {
+      displacement_apply(t, x, y);
+    }
   } else if (t->kind == ORC_TRANSFORM_BSPLINE) {
     bspline_apply(t, x, y, w, st);
   } else {
@@ -573,7 +579,13 @@ static inline int evaluate_point(const orc_inputs *in, const orc_transform *t, c
   if (t->kind == ORC_TRANSFORM_AFFINE) {
     affine_apply(t, vp, mp);
   } else if (t->kind == ORC_TRANSFORM_DISPLACEMENT) {
-    displacement_apply(t, vp, mp);
+    if (t->field_affine) {
+      double u[3];
+      displacement_apply(t, vp, u);
+      affine_apply(t, u, mp); /* CompositeTransform: the field first, then the affine */
+    } else {
+      displacement_apply(t, vp, mp);
+    }
   } else if (t->kind == ORC_TRANSFORM_BSPLINE) {
     inside_bs = bspline_apply(t, vp, mp, pe->w, pe->start);
   } else {
@@ -667,6 +679,21 @@ static inline void domain_point(const orc_inputs *in, int64_t i, double vp[3])
   }
 }
 
+/* J^T g of a displacement field's local parameters: g, or M^T g behind an initial
+ * affine (the composite's chain rule, itkCompositeTransform.hxx:525-580) */
+static inline void field_grad(const orc_transform *t, const double g[3], double out[3])
+{
+  for (int d = 0; d < 3; ++d) {
+    if (!t->field_affine) {
+      out[d] = g[d];
+      continue;
+    }
+    double s = 0.0;
+    for (int dim = 0; dim < 3; ++dim) s += t->M[dim * 3 + d] * g[dim];
+    out[d] = s;
+  }
+}
+
 /* ComputeParameterOffsetFromVirtualIndex (Numerics/Optimizersv4/include/itkObjectToObjectMetric.hxx:332-343):
  * the point's virtual index (its own index for the dense domain,
  * TransformPhysicalPointToIndex for a point set) times 3.  -1 for a point set
@@ -742,7 +769,9 @@ static void *msq_worker(void *arg)
       /* local support: the point's own derivative block, stored at its offset
        * afterwards (StorePointDerivativeResult, ThreaderBase.hxx:301-320) */
       j->loff[i - j->begin] = local_offset(j->in, i, vp);
-      for (int d = 0; d < 3; ++d) j->lval[3 * (i - j->begin) + d] = 2.0 * diffC * pe.grad[d];
+      double gd[3];
+      field_grad(j->t, pe.grad, gd);
+      for (int d = 0; d < 3; ++d) j->lval[3 * (i - j->begin) + d] = 2.0 * diffC * gd[d];
       continue;
     }
     jacobian_product(j->t, &pe, &row);
@@ -1133,7 +1162,9 @@ static void *mattes_worker(void *arg)
         /* ComputePDFDerivativesLocalSupportTransform (.hxx:394-412) with the
          * identity Jacobian: innerProduct = g[mu] */
         const double dval = orc_bspline3_derivative(arg);
-        for (int d = 0; d < 3; ++d) j->lval[12 * q + 3 * bin + d] = pe.grad[d] * dval;
+        double gd[3];
+        field_grad(j->t, pe.grad, gd);
+        for (int d = 0; d < 3; ++d) j->lval[12 * q + 3 * bin + d] = gd[d] * dval;
       } else if (j->compute_derivative) {
         const double dval = orc_bspline3_derivative(arg);
         double *dst = j->pdfd + (fidx * bins + pdfm) * P;
@@ -1325,9 +1356,13 @@ int orc_transform_from_flat(orc_transform *t, int tkind, const double *tparams, 
     return nparams == 3 * t->nper ? ORC_OK : ORC_ERR_BAD_ARG;
   }
   if (tkind == ORC_TRANSFORM_DISPLACEMENT) {
-    if (nfixed != 18) return ORC_ERR_BAD_ARG;
+    if (nfixed != 18 && nfixed != 33) return ORC_ERR_BAD_ARG;
     int rc = orc_displacement_init(t, tfixed, tparams);
     if (rc) return rc;
+    if (nfixed == 33) {
+      affine_setup(t, tfixed + 18, tfixed + 30);
+      t->field_affine = 1;
+    }
     return nparams == 3 * t->nvox ? ORC_OK : ORC_ERR_BAD_ARG;
   }
   if (tkind == ORC_TRANSFORM_COMPOSITE) {

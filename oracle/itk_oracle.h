@@ -111,6 +111,7 @@ typedef struct {
   orc_geom fgeom;
   int64_t nvox;
   const double *field; /* 3*nvox, voxel-major (x, y, z per voxel), x-fastest voxels */
+  int field_affine;    /* 1: [affine, displacement field] composite, y = affine(x + field(x)) */
 } orc_transform;
 
 typedef struct {
@@ -172,7 +173,9 @@ int orc_mattes_value_derivative(const orc_inputs *in, const orc_mattes_state *st
  *              parameters, 3 initial-affine centre (33 values)
  *   DISPLACEMENT: tparams = 3*voxels field values, tfixed = 18 (field size,
  *              origin, spacing, direction); the field must share the virtual
- *              domain's grid (VerifyDisplacementFieldSizeAndPhysicalSpace)
+ *              domain's grid (VerifyDisplacementFieldSizeAndPhysicalSpace);
+ *              tfixed = 33 adds an initial affine (12 parameters, centre 3):
+ *              the [affine, displacement field] composite, field applied first
  * Geometry flat encoding (15 doubles): spacing(3), origin(3), direction(9).
  * nthreads: low 16 bits = thread count; bit 16 set = double pixel type
  * (interpolated values are not rounded to float, as for Image<double,N>). */

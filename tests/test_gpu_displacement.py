@@ -250,3 +250,31 @@ def test_virtual_domain_with_dropped_voxels(pair, kind):
     assert_deriv_close(d, rd)
     blocks = np.asarray(d).reshape(virt.array.shape + (3,))
     assert not np.any(blocks[:, :, -1])  # the last x plane maps outside the fixed image
+
+
+@pytest.mark.parametrize("kind", ["msq", "mattes"])
+@pytest.mark.parametrize("sampled", [False, True])
+def test_affine_then_field_composite(pair, kind, sampled):
+    """CompositeTransform [affine, displacement field] (the field applied first and
+    optimized, as behind a registration's moving initial transform): positions
+    A(x + u(x)), local blocks from M^T g, against the oracle."""
+    from itk_gb300 import CompositeTransform
+    fixed, moving = pair
+    A = AffineTransform()
+    A.SetCenter(fixed.physical_center())
+    t = np.deg2rad(6.0)
+    A.SetMatrix([[np.cos(t), -np.sin(t), 0.0], [np.sin(t), np.cos(t), 0.0], [0.0, 0.0, 1.0]])
+    A.SetTranslation([0.8, -0.5, 0.3])
+    F = field_transform(fixed, data.smooth_displacement_field(fixed, seed=17, max_disp=1.5).array)
+    C = CompositeTransform()
+    C.AddTransform(A)
+    C.AddTransform(F)
+    grad = data.gradient_image(moving)
+    pts = data.unique_voxel_points(fixed, 0.25, seed=5) if sampled else None
+    m = make(kind, fixed, moving, C, grad, pts)
+    assert m.HasLocalSupport() and m.GetNumberOfParameters() == 3 * fixed.array.size
+    v, d = m.GetValueAndDerivative()
+    rc, rv, rd, nv = oracle(kind, fixed, moving, C, grad, pts)
+    assert rc == 0 and m.GetNumberOfValidPoints() == nv
+    assert_value_close(v, rv)
+    assert_deriv_close(d, rd)
