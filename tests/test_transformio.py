@@ -83,3 +83,22 @@ def test_reader_rejects_unknown_types_and_bad_tags():
         transforms_from_text("#Insight Transform File V1.0\nTransform: AffineTransform_double_10_10\n")
     with pytest.raises(ValueError):
         transforms_from_text("Transform AffineTransform_double_3_3\n")
+
+
+def test_round_trip_displacement_field_and_composite(tmp_path):
+    from itk_gb300 import DisplacementFieldImage, DisplacementFieldTransform
+    img = Image(np.zeros((5, 6, 7), np.float32), spacing=(1.0, 1.5, 0.8), origin=(1.0, 2.0, 3.0))
+    F = DisplacementFieldTransform()
+    F.SetDisplacementField(DisplacementFieldImage.like(img, np.random.default_rng(2).normal(size=(5, 6, 7, 3))))
+    C = CompositeTransform()
+    C.AddTransform(affine())
+    C.AddTransform(F)
+    for t in (F, C):
+        p = tmp_path / "f.tfm"
+        WriteTransform(t, str(p))
+        r = ReadTransform(str(p))
+        assert type(r) is type(t)
+        assert np.array_equal(r.GetParameters(), t.GetParameters())
+        assert np.array_equal(r.GetFixedParameters(), t.GetFixedParameters())
+        x = np.array([[3.0, 4.0, 5.0], [6.0, 9.0, 4.0]])
+        assert np.array_equal(r.TransformPoint(x), t.TransformPoint(x))
