@@ -26,6 +26,7 @@
 #pragma once
 
 #include "gb_bspline.cuh"
+#include "gb_field.cuh"
 #include "gb_kernels.cuh"
 
 namespace gb {
@@ -62,7 +63,7 @@ __device__ __forceinline__ int jhmi_bin(float v, float vmin_f, float vinv_f, dou
 }
 
 // k_jhmi_pass1: histogram counts in shared memory (u32), the cache (m, g) for pass 2.
-template <int GRAD>
+template <int GRAD, int TK = kMapAffine>
 __device__ __forceinline__ void jhmi_pass1_body(const EvalArgs& a, const JhmiConsts* __restrict__ gC, VGrid vg) {
   extern __shared__ unsigned hist_s[];
   __shared__ EvalConsts K;
@@ -85,7 +86,9 @@ __device__ __forceinline__ void jhmi_pass1_body(const EvalArgs& a, const JhmiCon
     const float4 s = __ldcs(a.samples + i);
     float m = 0.f;
     float3 g = make_float3(0.f, 0.f, 0.f);
-    const bool ok = eval_moving<GRAD>(a, map_pos(K.map, s.x, s.y, s.z), a.with_derivative != 0, m, g);
+    unsigned voxel;
+    const bool ok = eval_moving<GRAD>(a, sample_pos<TK>(a, K, s, i, voxel), a.with_derivative != 0, m, g);
+    if (TK != kMapAffine) g = field_grad(K, g);
     if (a.with_derivative)
       __stcs(a.cache + i, ok ? make_float4(m, g.x, g.y, g.z) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f));
     if (!ok) continue;
@@ -438,6 +441,58 @@ __global__ void __launch_bounds__(kBlock) k_jhmi_pass2_bspline(EvalArgs a, const
     *a.acc_n = N;
     a.out[1] = (double)N;
     if (N == 0) {
+      a.out[0] = DBL_MAX;
+      *a.status = GB_ERR_NO_VALID_POINTS;
+    } else {
+      *a.status = GB_OK;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Displacement fields (local support): pass 1 with the field's positions, caching
+// (m, M^T g); the same finalize; pass 2 stores each derivative point's block
+// sf M^T g at its voxel, not averaged (the base threader's local branch), and the
+// last block sets the count and status.
+
+template <int GRAD, int TK>
+__global__ void __launch_bounds__(kBlock) k_jhmi_pass1_field(EvalArgs a, const JhmiConsts* C) {
+  jhmi_pass1_body<GRAD, TK>(a, C, hw_grid());
+}
+
+template <int TK>
+__global__ void __launch_bounds__(kBlock) k_jhmi_pass2_field(EvalArgs a, const JhmiConsts* gC) {
+  extern __shared__ float tab[];
+  __shared__ JhmiConsts C;
+  const int B = a.bins;
+  griddep_wait();
+  if (halted(a)) return;
+  griddep_launch_dependents();
+  for (int k = threadIdx.x; k < B * B + B; k += blockDim.x) tab[k] = __ldcg(&a.pratio[k]);
+  load_jhmi(gC, C);
+  __syncthreads();
+  const float max_slope = (float)(36.841361487904734 / C.spacing);  // -log(1e-16) / spacing
+  const float inv_scale = (float)(1.0 / (0.69314718055994530942 * (C.mmax - C.mmin)));
+  const float mlo = (float)C.mmin, mhi = (float)C.mmax;
+  unsigned nv = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const float4 cc = __ldcs(a.cache + i);
+    const float4 s = __ldcs(a.samples + i);
+    const unsigned voxel = TK == kMapFieldDense
+                               ? (unsigned)s.x + (unsigned)a.vnx * ((unsigned)s.y + (unsigned)a.vny * (unsigned)s.z)
+                               : __ldg(a.voff + i);
+    float sf = 0.f;
+    const bool ok = jhmi_scaling(C, tab, tab + B * B, B, s.w, cc.x, mlo, mhi, max_slope, inv_scale, sf);
+    nv += ok ? 1u : 0u;
+    field_store<TK>(a, voxel, ok, sf, make_float3(cc.y, cc.z, cc.w));
+  }
+  block_count(nv, a.fmarg);
+  if (!last_block(a.tickets + kTicketPass2)) return;
+  if (threadIdx.x == 0) {
+    const unsigned long long N = __ldcg(a.fmarg);
+    a.out[1] = (double)N;
+    if (N == 0) {  // a warning, value max; no block was stored
       a.out[0] = DBL_MAX;
       *a.status = GB_ERR_NO_VALID_POINTS;
     } else {

@@ -544,11 +544,9 @@ extern "C" int gb_metric_initialize(gb_metric* m) {
     return fail(GB_ERR_BAD_ARG, "gradient source is a gradient image but none was set");
   const bool bspline = is_bspline(m);
   const bool field = is_field(m);
-  if (field && m->kind == GB_METRIC_CORRELATION)
-    return fail(GB_ERR_UNSUPPORTED, "the correlation metric runs affine, B-spline and composite transforms");
+  if (field && m->kind == GB_METRIC_CORRELATION)  // as the reference's constructor refuses it
+    return fail(GB_ERR_UNSUPPORTED, "the correlation metric does not support displacement field transforms");
   const bool jhmi = m->kind == GB_METRIC_JOINT_HISTOGRAM_MI;
-  if (jhmi && field)
-    return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric runs affine, B-spline and composite transforms");
   if (jhmi && (m->bins < 6 || m->bins > kJhmiMaxBins))
     return fail(GB_ERR_UNSUPPORTED, "the joint-histogram metric takes 6 to 64 bins");
   // the floating point correction acts where points store a global derivative
@@ -1212,6 +1210,29 @@ static int enqueue_eval_jhmi(gb_metric* m, const EvalArgs& a, bool cd, bool deri
   const int B = (int)m->bins;
   const JhmiConsts* C = reinterpret_cast<const JhmiConsts*>(m->d_jhmi.p);
   const bool bs = is_bspline(m);
+  if (is_field(m)) {
+    const bool pts = m->use_sampled;
+    if (deriv && !a.field_full) GB_CUDA(cudaMemsetAsync(a.out + 2, 0, sizeof(double) * m->tparams.size(), m->stream));
+    const size_t sh1 = sizeof(unsigned) * B * B;
+    cudaError_t e;
+    if (pts) e = cd ? launch_wave(m, k_jhmi_pass1_field<kGradCentralDifference, kMapFieldPoints>, sh1, a, C)
+                    : launch_wave(m, k_jhmi_pass1_field<kGradImage, kMapFieldPoints>, sh1, a, C);
+    else e = cd ? launch_wave(m, k_jhmi_pass1_field<kGradCentralDifference, kMapFieldDense>, sh1, a, C)
+                : launch_wave(m, k_jhmi_pass1_field<kGradImage, kMapFieldDense>, sh1, a, C);
+    GB_CUDA(e);
+    m->mark();
+    const size_t shf = sizeof(double) * (2 * B * B + 2 * B);
+    GB_CUDA(cudaFuncSetAttribute(k_jhmi_finalize, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shf));
+    GB_CUDA(launch_chain(m, k_jhmi_finalize, (unsigned)kJhmiFinalizeBlocks, kBlock, shf, a, C));
+    m->mark();
+    if (deriv) {
+      const size_t sh2 = sizeof(float) * (B * B + B);
+      GB_CUDA(pts ? launch_wave(m, k_jhmi_pass2_field<kMapFieldPoints>, sh2, a, C)
+                  : launch_wave(m, k_jhmi_pass2_field<kMapFieldDense>, sh2, a, C));
+      m->mark();
+    }
+    return GB_OK;
+  }
   if (bs) {
     const bool sm = a.nodes_smem != 0;
     if (device_params) {  // the host call uploads converted nodes

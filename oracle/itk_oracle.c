@@ -1727,6 +1727,8 @@ typedef struct {
   double *dsum, *dcomp;
   uint64_t nvalid;
   int64_t nparams;
+  int64_t *loff; /* local support: per point, the derivative offset (-1: none) */
+  double *lval;  /* local support: per point, 3 local derivatives */
 } jhmi_job;
 
 /* JointHistogramMutualInformationComputeJointPDFThreaderBase::ProcessPoint
@@ -1808,6 +1810,14 @@ static void *jhmi_deriv_worker(void *arg)
       sf = (t1 - t2) / (log2 * mrange);
     }
     j->nvalid++;
+    if (j->loff) {
+      /* local support: sf J^T g stored at the point's voxel afterwards, not averaged */
+      double gd[3];
+      field_grad(j->t, pe.grad, gd);
+      j->loff[i - j->begin] = local_offset(j->in, i, vp);
+      for (int d = 0; d < 3; ++d) j->lval[3 * (i - j->begin) + d] = sf * gd[d];
+      continue;
+    }
     jacobian_product(j->t, &pe, &row);
     for (int e = 0; e < row.count; ++e) kahan_add(&j->dsum[row.idx[e]], &j->dcomp[row.idx[e]], sf * row.val[e]);
   }
@@ -1822,7 +1832,8 @@ int orc_jhmi_value_derivative(const orc_inputs *in, const orc_jhmi_state *st, co
   const int64_t P = orc_transform_nparams(t);
   const int64_t B = st->bins;
   if (n < 1) return ORC_ERR_BAD_ARG;
-  if (t->kind == ORC_TRANSFORM_DISPLACEMENT) return ORC_ERR_BAD_ARG; /* global-support transforms only here */
+  if (verify_field_domain(in, t)) return ORC_ERR_BAD_ARG;
+  const int local = t->kind == ORC_TRANSFORM_DISPLACEMENT;
   const int T = resolve_threads(in->nthreads, n);
   jhmi_job *jobs = (jhmi_job *)calloc((size_t)T, sizeof(jhmi_job));
   pthread_t *th = (pthread_t *)calloc((size_t)T, sizeof(pthread_t));
@@ -1910,9 +1921,17 @@ int orc_jhmi_value_derivative(const orc_inputs *in, const orc_jhmi_state *st, co
     for (int k = 0; k < T && rc == ORC_OK; ++k) {
       jobs[k].pdf = pdf;
       jobs[k].mmarg = mmarg;
-      jobs[k].dsum = (double *)calloc((size_t)P, sizeof(double));
-      jobs[k].dcomp = (double *)calloc((size_t)P, sizeof(double));
-      if (!jobs[k].dsum || !jobs[k].dcomp) rc = ORC_ERR_OOM;
+      if (local) {
+        const int64_t len = jobs[k].end - jobs[k].begin > 0 ? jobs[k].end - jobs[k].begin : 1;
+        jobs[k].loff = (int64_t *)malloc(sizeof(int64_t) * (size_t)len);
+        jobs[k].lval = (double *)malloc(sizeof(double) * 3 * (size_t)len);
+        if (!jobs[k].loff || !jobs[k].lval) rc = ORC_ERR_OOM;
+        for (int64_t q = 0; jobs[k].loff && q < len; ++q) jobs[k].loff[q] = -1;
+      } else {
+        jobs[k].dsum = (double *)calloc((size_t)P, sizeof(double));
+        jobs[k].dcomp = (double *)calloc((size_t)P, sizeof(double));
+        if (!jobs[k].dsum || !jobs[k].dcomp) rc = ORC_ERR_OOM;
+      }
     }
     if (rc == ORC_OK) {
       for (int k = 0; k < T; ++k) pthread_create(&th[k], NULL, jhmi_deriv_worker, &jobs[k]);
@@ -1920,10 +1939,21 @@ int orc_jhmi_value_derivative(const orc_inputs *in, const orc_jhmi_state *st, co
       uint64_t nv = 0;
       for (int k = 0; k < T; ++k) nv += jobs[k].nvalid;
       *nvalid = nv;
-      for (int64_t p = 0; p < P; ++p) {
-        double s = 0.0, cc = 0.0;
-        for (int k = 0; k < T; ++k) kahan_add(&s, &cc, jobs[k].dsum[p]);
-        derivative[p] = nv > 0 ? s / (double)nv : 0.0;
+      if (local) {
+        /* Derivatives[offset + i] += LocalDerivatives[i] in point order, no averaging */
+        for (int64_t p = 0; p < P; ++p) derivative[p] = 0.0;
+        for (int k = 0; nv > 0 && k < T; ++k)
+          for (int64_t q = 0; q < jobs[k].end - jobs[k].begin; ++q) {
+            const int64_t o = jobs[k].loff[q];
+            if (o < 0) continue;
+            for (int d = 0; d < 3; ++d) derivative[o + d] += jobs[k].lval[3 * q + d];
+          }
+      } else {
+        for (int64_t p = 0; p < P; ++p) {
+          double s = 0.0, cc = 0.0;
+          for (int k = 0; k < T; ++k) kahan_add(&s, &cc, jobs[k].dsum[p]);
+          derivative[p] = nv > 0 ? s / (double)nv : 0.0;
+        }
       }
       if (nv == 0) {
         *value = DBL_MAX; /* VerifyNumberOfValidPoints: a warning, value max, zero derivative */
@@ -1934,7 +1964,9 @@ int orc_jhmi_value_derivative(const orc_inputs *in, const orc_jhmi_state *st, co
     }
   }
   if (joint_pdf && pdf) memcpy(joint_pdf, pdf, sizeof(double) * (size_t)(B * B));
-  for (int k = 0; jobs && k < T; ++k) { free(jobs[k].hist); free(jobs[k].dsum); free(jobs[k].dcomp); }
+  for (int k = 0; jobs && k < T; ++k) {
+    free(jobs[k].hist); free(jobs[k].dsum); free(jobs[k].dcomp); free(jobs[k].loff); free(jobs[k].lval);
+  }
   free(jobs);
   free(th);
   free(pdf);

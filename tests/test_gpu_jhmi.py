@@ -158,11 +158,15 @@ def test_bins_and_transform_limits(pair):
     fixed, moving, T = pair
     with pytest.raises(ExceptionObject, match="6 to 64 bins"):
         make(fixed, moving, perturbed(T, 1), bins=65)
-    from itk_gb300 import DisplacementFieldImage, DisplacementFieldTransform
+    from itk_gb300 import CorrelationImageToImageMetricv4, DisplacementFieldImage, DisplacementFieldTransform
     F = DisplacementFieldTransform()
     F.SetDisplacementField(DisplacementFieldImage.like(fixed))
-    with pytest.raises(ExceptionObject, match="affine, B-spline and composite"):
-        make(fixed, moving, F)
+    c = CorrelationImageToImageMetricv4()
+    c.SetFixedImage(fixed)
+    c.SetMovingImage(moving)
+    c.SetMovingTransform(F)
+    with pytest.raises(ExceptionObject, match="does not support displacement field"):
+        c.Initialize()
 
 
 @pytest.mark.parametrize("composite", [False, True])
@@ -184,6 +188,26 @@ def test_bspline_matches_oracle(pair, composite, sampled, gradient):
     m = make(fixed, moving, U, gradient, pts)
     v, d = m.GetValueAndDerivative()
     rc, rv, rd, nv, pdf = oracle(fixed, moving, U, gradient, pts)
+    assert rc == 0 and m.GetNumberOfValidPoints() == nv
+    assert_value_close(v, rv)
+    assert_deriv_close(d, rd)
+    assert m.GetValue() == v
+
+
+@pytest.mark.parametrize("sampled", [False, True])
+@pytest.mark.parametrize("gradient", ["image", "cd"])
+def test_displacement_field_matches_oracle(pair, sampled, gradient):
+    """A displacement field (local support): the derivative field's blocks sf g at each
+    point's voxel, not averaged, against the oracle."""
+    from itk_gb300 import DisplacementFieldImage, DisplacementFieldTransform
+    fixed, moving, _ = pair
+    F = DisplacementFieldTransform()
+    F.SetDisplacementField(DisplacementFieldImage.like(fixed, data.smooth_displacement_field(fixed, 21, 2.0).array))
+    pts = data.unique_voxel_points(fixed, 0.25, seed=7) if sampled else None
+    m = make(fixed, moving, F, gradient, pts)
+    assert m.HasLocalSupport()
+    v, d = m.GetValueAndDerivative()
+    rc, rv, rd, nv, pdf = oracle(fixed, moving, F, gradient, pts)
     assert rc == 0 and m.GetNumberOfValidPoints() == nv
     assert_value_close(v, rv)
     assert_deriv_close(d, rd)
