@@ -86,8 +86,8 @@ int gb_metric_destroy(gb_metric *m);
 int gb_metric_set_number_of_histogram_bins(gb_metric *m, uint64_t bins);
 /* JointHistogramMutualInformationImageToImageMetricv4::SetVarianceForJointPDFSmoothing
  * (default 1.5; <= 0: no smoothing), Registration/Metricsv4/include/itkJointHistogramMutualInformationImageToImageMetricv4.h:141.
- * The joint-histogram metric takes affine, B-spline and [affine, B-spline] transforms
- * and 6 to 64 bins (default 20). */
+ * The joint-histogram metric takes affine, B-spline, [affine, B-spline] and
+ * displacement-field transforms and 6 to 64 bins (default 20). */
 int gb_metric_set_joint_pdf_smoothing_variance(gb_metric *m, double variance);
 /* SetUseFloatingPointCorrection(on) / SetFloatingPointCorrectionResolution(resolution)
  * (Registration/Metricsv4/include/itkImageToImageMetricv4.h:604-621; applied in

@@ -305,7 +305,8 @@ class JointHistogramMutualInformationImageToImageMetricv4(ImageToImageMetricv4):
     """Joint-histogram mutual information (value -MI in bits): counts of (fixed, moving)
     intensity bins over the valid points, normalized and smoothed by a discrete
     Gaussian; the derivative from the smoothed PDF's slope along the moving axis
-    (affine, B-spline and [affine, B-spline] transforms; default 20 bins, variance 1.5)."""
+    (affine, B-spline, [affine, B-spline] and displacement-field transforms; default
+    20 bins, variance 1.5)."""
 
     _kind = _capi.GB_METRIC_JOINT_HISTOGRAM_MI
 

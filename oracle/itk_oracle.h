@@ -260,7 +260,7 @@ int orc_corr_flat_v(const float *fixed, const int64_t fsize[3], const double fge
  * (fixed, moving) bins, normalized, smoothed by a discrete Gaussian, MI in bits;
  * derivative from the smoothed PDF's moving-axis slope (flat inputs as
  * orc_msq_flat_v; joint_pdf = the smoothed bins x bins PDF, fixed index fastest,
- * or NULL).  Global-support transforms. */
+ * or NULL).  A displacement field stores sf J^T g at each point's voxel, not averaged. */
 typedef struct {
   int64_t bins;
   double variance;
