@@ -7,10 +7,17 @@
 // allocation after start-up, and libraries embedded in hosts that account for
 // every device allocation.  This entry point takes all inputs and the output
 // in caller-owned device memory and keeps its own scratch -- block partial
-// sums, counters, the status word -- in one file-scope __device__ array of
+// sums and counters -- in one file-scope __device__ array of
 // kNoAllocScratchBytes (about 112 KiB), which every GPU that loads this
 // library holds until the process exits.
+//
+// The array's device address belongs to a CUDA context, not to a device: a
+// cudaDeviceReset re-creates the primary context (and reloads this module), and
+// a caller may make the call under a context of its own.  The address is
+// therefore looked up once per context, keyed by the context's unique ID
+// (cuCtxGetId, never reused within a process), with that context current.
 #define GB_KERNELS_HELPERS_ONLY
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -26,21 +33,26 @@ namespace {
 constexpr int kNoAllocMaxBlocks = 1024;  // grid cap: the partial-sum capacity of the scratch array
 constexpr int kNoAllocGroups = kNoAllocMaxBlocks / kGroup;
 constexpr int kNoAllocValues = 13;  // value + 12 affine derivative terms
-// byte layout: header (counter, tickets, status; cleared by every call) | block partials | group partials
+// byte layout: header (counter, tickets; cleared by every call) | block partials | group partials
 constexpr size_t kNoAllocHeaderBytes = 1024;
 constexpr size_t kNoAllocPartOffset = kNoAllocHeaderBytes;
 constexpr size_t kNoAllocGroupOffset = kNoAllocPartOffset + sizeof(double) * kNoAllocMaxBlocks * kNoAllocValues;
 constexpr size_t kNoAllocScratchBytes = kNoAllocGroupOffset + sizeof(double) * kNoAllocGroups * kNoAllocValues;
-static_assert(8 + 4 * (kNoAllocGroups + 1) + 4 <= kNoAllocHeaderBytes, "scratch header too small");
+static_assert(8 + 4 * (kNoAllocGroups + 1) <= kNoAllocHeaderBytes, "scratch header too small");
 static_assert(kNoAllocScratchBytes == GB_NOALLOC_SCRATCH_BYTES, "header constant out of date");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch per device, looked up once with that device current.
-constexpr int kMaxDevices = 64;
+// Device address of g_noalloc_scratch and the grid size, per CUDA context.
+constexpr int kMaxContexts = 64;
+struct ScratchEntry {
+  unsigned long long ctx_id;  // 0: unused
+  void* ptr;
+  int blocks;
+};
 std::mutex g_setup_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
-int g_wave_blocks[kMaxDevices] = {};
+ScratchEntry g_entries[kMaxContexts] = {};
+int g_next_entry = 0;  // round-robin replacement once every entry is used
 
 struct NoAllocArgs {
   EvalConsts K;  // by value: nothing to copy into device memory first
@@ -62,7 +74,6 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine_noalloc(NoAllocArgs na) {
   __syncthreads();
   unsigned long long* acc_n = reinterpret_cast<unsigned long long*>(na.scratch);
   unsigned* tickets = reinterpret_cast<unsigned*>(na.scratch + 8);
-  int* status = reinterpret_cast<int*>(na.scratch + 8 + 4 * (kNoAllocGroups + 1));
   double* part = reinterpret_cast<double*>(na.scratch + kNoAllocPartOffset);
   double* grp = reinterpret_cast<double*>(na.scratch + kNoAllocGroupOffset);
   KahanF acc[kNoAllocValues];
@@ -95,35 +106,78 @@ __global__ void __launch_bounds__(kBlock) k_msq_affine_noalloc(NoAllocArgs na) {
       na.out[0] = DBL_MAX;  // VerifyNumberOfValidPoints, itkObjectToObjectMetric.hxx:512-527
       na.out[1] = 0.0;
       for (int p = 0; p < 12; ++p) na.out[2 + p] = 0.0;
-      *status = GB_ERR_NO_VALID_POINTS;
     } else {
       na.out[0] = fin[0] / (double)N;
       na.out[1] = (double)N;
       for (int p = 0; p < 12; ++p) na.out[2 + p] = fin[1 + p] / (double)N;
-      *status = GB_OK;
     }
   }
 }
 
-// Once per device, with that device current: the device address of the
+// The unique ID of the calling thread's current context (0 when none is
+// current), through the runtime's driver entry points (no libcuda link).
+int current_context_id(unsigned long long* id) {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  static cudaError_t load_err = cudaSuccess;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSuccess, q2 = cudaDriverEntryPointSuccess;
+    load_err = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", reinterpret_cast<void**>(&get_current), 4000,
+                                                cudaEnableDefault, &q1);
+    if (load_err == cudaSuccess)
+      load_err = cudaGetDriverEntryPointByVersion("cuCtxGetId", reinterpret_cast<void**>(&get_id), 12000,
+                                                  cudaEnableDefault, &q2);
+    if (load_err == cudaSuccess && (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess))
+      load_err = cudaErrorSymbolNotFound;
+  });
+  if (load_err != cudaSuccess || !get_current || !get_id)
+    return fail(GB_ERR_CUDA, std::string("driver entry points cuCtxGetCurrent / cuCtxGetId: ") +
+                                 cudaGetErrorString(load_err));
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS) return fail(GB_ERR_CUDA, "cuCtxGetCurrent failed");
+  *id = 0;
+  if (ctx && get_id(ctx, id) != CUDA_SUCCESS) return fail(GB_ERR_CUDA, "cuCtxGetId failed");
+  return GB_OK;
+}
+
+// Once per context, with that context current: the device address of the
 // scratch array (the host-side symbol is only a stand-in) and the grid size.
-int setup_device(int dev, void** scratch, int* blocks) {
+int setup_context(int dev, void** scratch, int* blocks) {
+  unsigned long long id = 0;
+  int rc = current_context_id(&id);
+  if (rc) return rc;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (dev < 0 || dev >= kMaxDevices) return fail(GB_ERR_UNSUPPORTED, "device index above 63");
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(GB_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
-    int sms = 0, per_sm = 0;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_msq_affine_noalloc, kBlock, 0);
-    if (e != cudaSuccess) return fail(GB_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
-    g_wave_blocks[dev] = std::max(1, std::min(kNoAllocMaxBlocks, sms * std::max(per_sm, 1)));
-    g_scratch_ptr[dev] = p;
+  if (id)
+    for (const ScratchEntry& en : g_entries)
+      if (en.ctx_id == id) {
+        *scratch = en.ptr;
+        *blocks = en.blocks;
+        return GB_OK;
+      }
+  // the lookup makes the device's primary context current when no context was
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(GB_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+  if (!id) {
+    rc = current_context_id(&id);
+    if (rc) return rc;
+    if (!id) return fail(GB_ERR_CUDA, "no CUDA context is current after the symbol lookup");
   }
-  *scratch = g_scratch_ptr[dev];
-  *blocks = g_wave_blocks[dev];
+  int sms = 0, per_sm = 0;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_msq_affine_noalloc, kBlock, 0);
+  if (e != cudaSuccess) return fail(GB_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
+  ScratchEntry& en = g_entries[g_next_entry];
+  g_next_entry = (g_next_entry + 1) % kMaxContexts;
+  en.ctx_id = id;
+  en.ptr = p;
+  en.blocks = std::max(1, std::min(kNoAllocMaxBlocks, sms * std::max(per_sm, 1)));
+  *scratch = en.ptr;
+  *blocks = en.blocks;
   return GB_OK;
 }
 
@@ -157,7 +211,7 @@ extern "C" int gb_msq_affine_noalloc(const void* device_samples, int64_t n, cons
   if (e != cudaSuccess) return fail(GB_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   void* scratch = nullptr;
   int blocks = 0;
-  rc = setup_device(dev, &scratch, &blocks);
+  rc = setup_context(dev, &scratch, &blocks);
   if (rc) return rc;
 
   NoAllocArgs na;
@@ -171,7 +225,7 @@ extern "C" int gb_msq_affine_noalloc(const void* device_samples, int64_t n, cons
   na.scratch = static_cast<unsigned char*>(scratch);
   na.out = device_out;
   const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  // the array keeps the previous call's contents: clear the counter, tickets and status
+  // the array keeps the previous call's contents: clear the counter and tickets
   e = cudaMemsetAsync(scratch, 0, kNoAllocHeaderBytes, st);
   if (e != cudaSuccess) return fail(GB_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
   const int64_t want = (n + kBlock - 1) / kBlock;
