@@ -211,3 +211,46 @@ def test_rejects_non_affine(pairs):
     b = RegistrationBatch()
     with pytest.raises(ExceptionObject):
         b.Add(o)
+
+
+def test_first_iteration_matches_oracle(pairs):
+    """One iteration of every registration in a mixed batch (MeanSquares and Mattes MI,
+    dense and sampled, four volume sizes) against the FP64 oracle at the start
+    parameters: the value the batch reports, and the derivative recovered from its
+    step p1 = p0 + lr (d / s) / ||d / s|| (with ||d / s|| the reported gradient
+    magnitude), within 1e-5 and 1e-4."""
+    from cases import geom, oracle_transform
+    from conftest import MATTES_VALUE_ATOL, assert_deriv_close, assert_value_close
+    from oracle import oracle as O
+
+    lr = 0.5
+    b = RegistrationBatch()
+    b.SetSamplesPerBlock(4096, 4096, 4096)
+    regs = []
+    for i in range(len(SPECS)):
+        U, o = make(pairs, i, *SPECS[i], iters=1, lr=lr)
+        regs.append((i, U, o, U.GetParameters().copy()))
+        b.Add(o)
+    assert b.Run() == 0
+    for i, U, o, p0 in regs:
+        kind, sampled = SPECS[i]
+        m = o.GetMetric()
+        fixed, moving = m.GetFixedImage(), m.GetMovingImage()
+        pts = data.random_points(fixed, 0.3, seed=7 + i) if sampled else None
+        grad = O.gradient_recursive_gaussian(moving.array, moving.spacing, moving.direction,
+                                             float(max(moving.spacing)))
+        T0 = AffineTransform()
+        T0.SetCenter(U.GetCenter())
+        T0.SetParameters(p0)
+        Tk = oracle_transform(T0)
+        if kind == "msq":
+            rc, v, d, nv = O.mean_squares(fixed.array, geom(fixed), moving.array, geom(moving), Tk,
+                                          moving_grad=grad, points=pts)
+        else:
+            rc, v, d, nv, _, _ = O.mattes(fixed.array, geom(fixed), moving.array, geom(moving), Tk, bins=32,
+                                          moving_grad=grad, points=pts)
+        assert rc == 0
+        assert o.GetCurrentIteration() == 1
+        assert_value_close(o.GetValue(), v, atol=MATTES_VALUE_ATOL if kind == "mattes" else 0.0)
+        d_batch = (U.GetParameters() - p0) * SCALES * (o.GetGradientMagnitude() / lr)
+        assert_deriv_close(d_batch, d)

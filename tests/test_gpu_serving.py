@@ -102,3 +102,55 @@ def test_failed_request_does_not_disturb_others(requests):
     for rid, req in zip(ids, requests[:3]):
         same(s.results[rid], run_alone(req))
     assert s.used_bytes == 0
+
+
+def test_served_results_match_oracle_registrations(requests):
+    """Every request served in a mix against the oracle's restatement of its levels and
+    optimizer with the same sample points: per level the same stop and iteration count
+    and the final value within 1e-4 (a level's images are smoothed on the device in
+    FP32, the oracle smooths in FP64); final displacement within 0.05 voxel RMS."""
+    from cases import geom
+    from conftest import assert_value_close
+    from itk_gb300.filters import shrink_geometry
+    from itk_gb300.registration import sample_points
+    from oracle import registration as R
+
+    s = RegistrationServer(samples_per_block=(4096, 4096, 4096), iterations_per_tick=3)
+    ids = [s.submit(r) for r in requests]
+    s.drain()
+    for rid, req in zip(ids, requests):
+        res = s.results[rid]
+        assert res.status == _capi.GB_OK
+        levels, seed = [], req.seed
+        for lv in range(req.levels):
+            f = req.shrink_factors[lv]
+            pts = None
+            if req.sampling != NONE:
+                size, sp, org = shrink_geometry(req.fixed, (f, f, f))
+                pts, seed = sample_points(req.sampling, size, sp, org, req.fixed.direction, req.sampling_percentage,
+                                          seed)
+            levels.append(dict(shrink=(f,) * 3, sigma=req.smoothing_sigmas[lv], sigma_physical=True, points=pts))
+        kindcode, p0, tfixed = req.transform.flat()
+        out = []
+        for lv, iters in zip(levels, req.iterations):
+            opt = dict(learning_rate=req.learning_rate, number_of_iterations=iters,
+                       minimum_step_length=req.minimum_step_length, scales=req.scales)
+            p0, r = R.register(req.metric, req.fixed.array, geom(req.fixed), req.moving.array, geom(req.moving),
+                               kindcode, p0, tfixed, [lv], opt, bins=req.bins)
+            out.append(r[0])
+        assert res.stop_conditions == [r["stop"] for r in out]
+        assert res.iterations == [r["iterations"] for r in out]
+        for got, r in zip(res.values, out):
+            assert_value_close(got, r["value"], rtol=1e-4)
+        T1 = AffineTransform()
+        T1.SetCenter(req.transform.GetCenter())
+        T1.SetParameters(res.parameters)
+        T2 = AffineTransform()
+        T2.SetCenter(req.transform.GetCenter())
+        T2.SetParameters(p0)
+        nx, ny, nz = req.fixed.GetSize()
+        g = np.stack(np.meshgrid(*(np.arange(0, n, 3) for n in (nx, ny, nz)), indexing="ij"), -1).reshape(-1, 3)
+        x = g.astype(np.float64) @ req.fixed.index_to_physical().T + req.fixed.origin
+        dd = (T1.TransformPoint(x) - T2.TransformPoint(x)) / req.fixed.spacing
+        rms = float(np.sqrt(np.mean(np.sum(dd * dd, axis=1))))
+        assert rms <= 0.05, f"request {rid}: displacement RMS {rms:.4f} voxel"
