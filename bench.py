@@ -69,9 +69,10 @@ def parse():
                     help="paths measured beside the batched engine: plain (host loop, one call per iteration), "
                          "loop (device optimizer loop per registration)")
     ap.add_argument("--only-forms", action="store_true", help="skip the single-evaluation measurement")
-    ap.add_argument("--forms", default="registration,batched,served",
-                    help="also measure the batched (64 registrations) and served (Poisson requests) forms; "
-                         "'' to skip")
+    ap.add_argument("--forms", default="bspline,registration,batched,served",
+                    help="sections beside the headline: bspline (the B-spline workload's own line), "
+                         "registration (64^3 MeanSquares registration), batched (64 registrations), served "
+                         "(Poisson requests); 'none' to skip")
     args = ap.parse_args()
     bs = args.transform == "bspline"
     if args.bins is None:
@@ -288,6 +289,9 @@ def dist_setup():
     return world, rank, local, dist
 
 
+REFERENCE_MAX_S = 120.0
+
+
 def run_reference(args):
     world, rank, local, dist = dist_setup()
     if rank != 0:
@@ -299,19 +303,27 @@ def run_reference(args):
     from cases import run_oracle
     kind = args.metric
     threads = os.cpu_count() or 1
-    for _ in range(min(args.warmup, 3)):
+    # the driver's step counts, unless a step is so slow that they would not end within a few
+    # minutes (then as many steps as fit in REFERENCE_MAX_S, and the line says how many ran)
+    t0 = time.perf_counter()
+    run_oracle(kind, fixed, moving, U, gradient=grad, points=pts, bins=args.bins, nthreads=threads)
+    one = time.perf_counter() - t0
+    fit = max(1, int(REFERENCE_MAX_S // max(one, 1e-3)))
+    warmup = max(0, min(args.warmup - 1, fit))
+    steps = max(1, min(args.steps, fit))
+    for _ in range(warmup):
         run_oracle(kind, fixed, moving, U, gradient=grad, points=pts, bins=args.bins, nthreads=threads)
-    steps = max(1, min(args.steps, 10))
+    warmup += 1
     t0 = time.perf_counter()
     for _ in range(steps):
         run_oracle(kind, fixed, moving, U, gradient=grad, points=pts, bins=args.bins, nthreads=threads)
     dt = time.perf_counter() - t0
     value = n_domain(fixed, pts) * steps / dt / 1e6
     per["value"] = value
-    per["sample"] = f"{steps} full evaluations ({n_domain(fixed, pts)} samples each) after {min(args.warmup, 3)} warm-up, " \
+    per["sample"] = f"{steps} full evaluations ({n_domain(fixed, pts)} samples each) after {warmup} warm-up, " \
                     f"FP64 oracle port of the reference algorithm, {threads} threads"
     line = {"metric": metric_name(args), "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
-            "warmup": min(args.warmup, 3), "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
+            "warmup": warmup, "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_dict(args, n_domain(fixed, pts)), "impl": "reference", "cpu_baseline": per,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -410,6 +422,32 @@ def run_gb300(args):
     world, rank, local, dist = dist_setup()
     if args.only_forms:
         return run_forms_only(args) if rank == 0 else None
+    line = measure_evaluation(args, world, rank, local, dist)
+    if rank != 0:
+        return
+    # the B-spline workload beside the headline: [affine, B-spline order 3, mesh 4^3 (1029
+    # parameters)], 192x192x160, 10 % samples, with its own roofline, e2e and CPU baseline
+    if world == 1 and args.transform == "affine" and args.metric == "mattes" and "bspline" in args.forms:
+        bargs = argparse.Namespace(**vars(args))
+        bargs.transform, bargs.mesh, bargs.size, bargs.fraction = "bspline", 4, "192,192,160", 0.1
+        bargs.cpu_seconds = min(args.cpu_seconds, 10.0)
+        line["bspline"] = measure_evaluation(bargs, world, rank, local, dist)
+    if world == 1 and "registration" in args.forms:
+        line["registration_64cubed"] = run_plain_registration(args)
+    if world == 1 and ("batched" in args.forms or "served" in args.forms):
+        t_gen = time.perf_counter()
+        inst = forms_instances(3, FORMS_N, 3000)
+        t_gen = time.perf_counter() - t_gen
+        if "batched" in args.forms:
+            line["batched"] = run_batched_form(args, inst, t_gen)
+        if "served" in args.forms:
+            line["served"] = run_served_form(args, inst)
+    print(json.dumps(line), flush=True)
+
+
+def measure_evaluation(args, world, rank, local, dist):
+    """One workload's line: device-timed value, e2e through the public call, the dominant
+    kernel's roofline, the CPU baseline (rank 0 of one process)."""
     import torch
 
     from itk_gb300 import (JointHistogramMutualInformationImageToImageMetricv4,
@@ -471,18 +509,20 @@ def run_gb300(args):
         torch.cuda.synchronize()
         dev_ms = sum(s.elapsed_time(e) for s, e in events)
         status = m.synchronize()
-        # end-to-end through the public call: params host->device, value+derivative device->host
-        for _ in range(args.warmup):
-            m.GetValueAndDerivative()
-        e2e_t = 0.0
-        for _ in range(args.steps):
-            with torch.cuda.stream(ext):
-                flush.zero_()
-            torch.cuda.synchronize()
-            t1 = time.perf_counter()
-            m.GetValueAndDerivative()
-            e2e_t += time.perf_counter() - t1
     clocks = clk.summary()
+    # end-to-end through the public call: params host->device, value+derivative device->host.
+    # Host wall time, so outside the clock sampler (an nvidia-smi query holds the driver for
+    # milliseconds and would stall the calls it overlaps).
+    for _ in range(args.warmup):
+        m.GetValueAndDerivative()
+    e2e_t = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        m.GetValueAndDerivative()
+        e2e_t += time.perf_counter() - t1
     if status != 0:
         raise RuntimeError(f"evaluation status {status}")
     if dist:
@@ -490,7 +530,7 @@ def run_gb300(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dev_ms, e2e_t = float(t[0]), float(t[1])
     if rank != 0:
-        return
+        return None
     value = world * n * args.steps / (dev_ms / 1e3) / 1e6
     e2e_value = world * n * args.steps / e2e_t / 1e6
 
@@ -540,28 +580,32 @@ def run_gb300(args):
             kname = "k_msq_affine"
     ktime = float(ktimes[kidx])
     peak, peak_src = measured_peak()
-    achieved = kbytes / (ktime / 1e3) / 1e9
+    b_alg = roofline.evaluation_bytes(n, v_touched, sparse=pts is not None, nparams=P)
+    eval_ms = dev_ms / args.steps
     traffic = None  # measured DRAM bytes of this kernel on this workload (profiles/traffic.txt), if captured
     tf = os.path.join(ROOT, "profiles", "traffic.txt")
     wkey = config_dict(args, n)["workload"]
     if os.path.exists(tf):
-        for line in open(tf):
-            parts = line.split()
+        for tline in open(tf):
+            parts = tline.split()
             if len(parts) == 3 and parts[0] == wkey and parts[1] == kname:
                 traffic = int(parts[2])
-    b_alg = roofline.evaluation_bytes(n, v_touched, sparse=pts is not None, nparams=P)
-    eval_ms = dev_ms / args.steps
+    achieved = b_alg / (ktime / 1e3) / 1e9
     line = {
         "metric": metric_name(args), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": eval_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args, n),
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-                     "algorithmic_bytes_per_launch": int(kbytes), "kernel_ms": ktime,
+                     "algorithmic_bytes_per_launch": int(b_alg),
+                     "algorithmic_bytes": "N_s*12 (point xyz; 0 for a dense grid) + V_touched*20 (fixed 4 B, moving "
+                                          "4 B, gradient 12 B per distinct touched voxel) + P*16 (parameters in, "
+                                          "derivative out): every distinct input byte once per evaluation",
+                     "v_touched": v_touched, "kernel_ms": ktime,
+                     "frac_evaluation": b_alg / (eval_ms / 1e3) / 1e9 / peak,
                      "kernel_ms_all": [float(x) for x in ktimes],
-                     "evaluation": {"b_alg_bytes": int(b_alg), "v_touched": v_touched,
-                                    "achieved_gbs": b_alg / (eval_ms / 1e3) / 1e9,
-                                    "frac": b_alg / (eval_ms / 1e3) / 1e9 / peak}},
+                     "kernel_min_dram_bytes": int(kbytes),
+                     "kernel_min_dram_frac": kbytes / (ktime / 1e3) / 1e9 / peak},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * P,
                 "d2h_bytes_per_step": 8 * (2 + P) + 4,
                 "note": "public GetValueAndDerivative call: parameters in, value/derivative/status out; "
@@ -573,17 +617,9 @@ def run_gb300(args):
     }
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(args, fixed, moving, grad, pts, U, args.cpu_seconds)
-    if world == 1 and "registration" in args.forms:
-        line["registration_64cubed"] = run_plain_registration(args)
-    if world == 1 and ("batched" in args.forms or "served" in args.forms):
-        t_gen = time.perf_counter()
-        inst = forms_instances(3, FORMS_N, 3000)
-        t_gen = time.perf_counter() - t_gen
-        if "batched" in args.forms:
-            line["batched"] = run_batched_form(args, inst, t_gen)
-        if "served" in args.forms:
-            line["served"] = run_served_form(args, inst)
-    print(json.dumps(line), flush=True)
+    del m, flush
+    torch.cuda.synchronize()
+    return line
 
 
 # ---------------------------------------------------------------------------

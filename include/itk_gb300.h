@@ -8,8 +8,8 @@
  * be used from different host threads; one call at a time per handle.
  *
  * Each entry point names the reference interface it replaces (paths relative
- * to the ITK source tree, Modules/).  The ITK-side shim that binds these
- * entry points behind itk::ObjectFactoryBase overrides is in INTEGRATION.md.
+ * to the ITK source tree, Modules/).  On the ITK side these entry points sit
+ * behind itk::ObjectFactoryBase overrides of the metric classes.
  */
 #ifndef ITK_GB300_H
 #define ITK_GB300_H
@@ -63,6 +63,11 @@ typedef struct gb_metric gb_metric;
 /* Text of the last error raised on the calling host thread (never NULL).
  * Mattes/MeanSquares errors reuse the reference's exception text. */
 const char *gb_last_error(void);
+/* Text of the last error raised by a call on metric handle m (never NULL; ""
+ * before any error), so that errors are not mis-attributed when one thread
+ * drives several handles.  This is the per-handle error text of the drop-in's
+ * exceptions (itkExceptionMacro in the metric, Core/Common/include/itkMacro.h:608). */
+const char *gb_metric_last_error(gb_metric *m);
 /* Library version string. */
 const char *gb_version(void);
 
@@ -230,14 +235,18 @@ int gb_metric_synchronize(gb_metric *m);
  *   out      14 doubles: value, number of valid points, derivative[12].
  * Geometry, the 12 affine parameters and the centre are host arrays.  The
  * call is asynchronous on `stream` (a cudaStream_t, 0 for the default
- * stream); when no sample maps inside the moving image, out = [DBL_MAX, 0,
- * 0...] as VerifyNumberOfValidPoints leaves it.
+ * stream), so the return code covers only the arguments and the launch.
+ * When no sample maps inside the moving image the call still succeeds and
+ * leaves out = [DBL_MAX, 0, 0...], as VerifyNumberOfValidPoints leaves the
+ * reference metric: out[1] == 0 is the only "no valid points" signal.
  * Scratch: one static device array of GB_NOALLOC_SCRATCH_BYTES bytes that
  * every GPU loading this library holds until the process exits.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress)
- * with that device current, so make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU (other
- * streams, other host threads) race; serialize them.
+ * call under each CUDA context (the device's primary context, again after a
+ * cudaDeviceReset, or a context the caller made current) looks up the array's
+ * device address (cudaGetSymbolAddress) with that context current, so make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (other streams, other host threads) race;
+ * serialize them.
  * Limits: n <= GB_NOALLOC_MAX_SAMPLES, moving voxels <= GB_NOALLOC_MAX_VOXELS;
  * larger sizes are rejected with GB_ERR_BAD_ARG. */
 #define GB_NOALLOC_SCRATCH_BYTES 114176
@@ -393,6 +402,19 @@ int gb_metric_set_profiling(gb_metric *m, int on);
  * value-only finalize; B-spline: [node conversion], the sample pass, [Mattes
  * finalize], chunk sums, parameter gather).  Synchronizes. */
 int gb_metric_get_kernel_times(gb_metric *m, double *ms, int max_kernels, int *count);
+
+/* ---- failure detection ------------------------------------------------- */
+/* No counterpart in the reference (whose failures are exceptions thrown by
+ * the metric): a test hook for the device-side failure path.  Every wait of
+ * the kernels on an asynchronous copy is bounded; when one runs out the
+ * kernel records GB_ERR_TIMEOUT, waits (bounded) for its other copies in
+ * flight and returns, so the context stays usable and the call reports the
+ * status.  GB_FAULT_STALLED_COPY makes the affine Mattes derivative pass
+ * issue none of its streamed record copies (with a short wait limit), so its
+ * waits run out: GetValueAndDerivative then returns GB_ERR_TIMEOUT.
+ * GB_FAULT_NONE restores normal evaluations. */
+enum { GB_FAULT_NONE = 0, GB_FAULT_STALLED_COPY = 1 };
+int gb_metric_set_fault_injection(gb_metric *m, int fault);
 
 #ifdef __cplusplus
 }

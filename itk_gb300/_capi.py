@@ -43,6 +43,10 @@ GB_GRADIENT_IMAGE = 0
 GB_GRADIENT_CENTRAL_DIFFERENCE = 1
 GB_GRADIENT_RECURSIVE_GAUSSIAN = 2
 
+# gb_metric_set_fault_injection
+GB_FAULT_NONE = 0
+GB_FAULT_STALLED_COPY = 1
+
 # MetricSamplingStrategyEnum
 GB_SAMPLING_NONE = 0
 GB_SAMPLING_REGULAR = 1
@@ -80,6 +84,7 @@ _D = ctypes.c_double
 # name -> argtypes (restype int unless listed in _RESTYPES)
 SIGNATURES = {
     "gb_last_error": [],
+    "gb_metric_last_error": [_P],
     "gb_version": [],
     "gb_ctx_create": [_I, _P],
     "gb_ctx_destroy": [_P],
@@ -121,6 +126,7 @@ SIGNATURES = {
     "gb_metric_synchronize": [_P],
     "gb_msq_affine_noalloc": [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _U64],
     "gb_metric_set_profiling": [_P, _I],
+    "gb_metric_set_fault_injection": [_P, _I],
     "gb_metric_get_kernel_times": [_P, _P, _I, _P],
     "gb_metric_optimize_regular_step": [_P, _P, _P, _I64, _P],
     "gb_metric_set_optimizer_graphs": [_P, _I],
@@ -137,7 +143,8 @@ SIGNATURES = {
     "gb_sample_count": [_I, _P, _D, _P],
     "gb_sample_points": [_I, _P, _P, _P, _P, _D, ctypes.c_int32, _P, _I64, _P, _P],
 }
-_RESTYPES = {"gb_last_error": ctypes.c_char_p, "gb_version": ctypes.c_char_p}
+_RESTYPES = {"gb_last_error": ctypes.c_char_p, "gb_version": ctypes.c_char_p,
+             "gb_metric_last_error": ctypes.c_char_p}
 
 _lib = None
 _lock = threading.Lock()
@@ -176,6 +183,11 @@ def lib():
 
 def last_error() -> str:
     msg = lib().gb_last_error()
+    return msg.decode() if msg else ""
+
+
+def metric_last_error(handle) -> str:
+    msg = lib().gb_metric_last_error(handle)
     return msg.decode() if msg else ""
 
 

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_batch_pass2(const EvalArgs* __res
   __shared__ EvalArgs sa;
   const int4 w = work[blockIdx.x];
   load_reg(regs, w.x, sa);
-  mattes_pass2_affine_body(sa, VGrid{w.y, w.z});
+  mattes_pass2_affine_body<false>(sa, VGrid{w.y, w.z});
 }
 
 // AdvanceOneStep of one registration per block (step_block), one warp for the
@@ -285,7 +285,7 @@ int rebuild_tables(gb_batch* b) {
     all.insert(all.end(), work[g].begin(), work[g].end());
   }
   b->smem1 = sizeof(unsigned long long) * (size_t)(maxbins * maxbins + maxbins) + sizeof(unsigned) * (size_t)maxbins;
-  b->smem2 = kStreamBytes + sizeof(float) * (size_t)maxbins * maxbins;
+  b->smem2 = mattes_pass2_smem(maxbins);
   if (maxbins > 0) {
     if (b->smem1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
     GB_B_CUDA(cudaFuncSetAttribute(k_batch_pass1<kGradImage>, cudaFuncAttributeMaxDynamicSharedMemorySize,

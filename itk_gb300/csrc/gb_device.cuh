@@ -201,9 +201,21 @@ struct DFPos {
 
 // Affine map virtual point -> moving continuous index, as FP32 hi/lo pairs:
 // cidx_k = sum_j (Ahi + Alo)[k][j] x_j + (bhi + blo)[k].
-struct AffineDF {
+struct __align__(16) AffineDF {
   float Ahi[9], Alo[9], bhi[3], blo[3];
 };
+
+// A copy of a shared-memory map in six 16-byte loads (the per-sample loops read
+// the map once per sample; narrower loads cost more shared-memory wavefronts).
+__device__ __forceinline__ AffineDF load_map(const AffineDF& s) {
+  static_assert(sizeof(AffineDF) == 96, "six float4");
+  AffineDF r;
+  const float4* v = reinterpret_cast<const float4*>(&s);
+  float4* o = reinterpret_cast<float4*>(&r);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) o[k] = v[k];
+  return r;
+}
 
 // Continuous index of one float point to ~1e-12 voxel: products by FMA error
 // terms, sums by two-sum.

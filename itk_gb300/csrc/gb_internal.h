@@ -81,9 +81,20 @@ struct DevBuf {
 cudaError_t sort_pairs_u64(const uint64_t* keys_in, uint64_t* keys_out, const uint32_t* vals_in, uint32_t* vals_out,
                            int64_t n, int end_bit, cudaStream_t stream);
 
-// Per-thread last-error text (gb_last_error()).
+// Per-thread last-error text (gb_last_error()).  While an entry point that takes a
+// metric handle runs, an ErrorScope names that handle, and fail() records the text
+// on the handle as well (gb_metric_last_error).
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
+gb_metric* error_scope();
+void set_error_scope(gb_metric* m);
+struct ErrorScope {
+  gb_metric* prev;
+  explicit ErrorScope(gb_metric* m) : prev(error_scope()) { set_error_scope(m); }
+  ~ErrorScope() { set_error_scope(prev); }
+  ErrorScope(const ErrorScope&) = delete;
+  ErrorScope& operator=(const ErrorScope&) = delete;
+};
 
 // Device image filters (gb_filters.cu).
 int smooth_rg_device(cudaStream_t st, const float* in, float* out, float* t1, float* t2, const int64_t size[3],
@@ -230,6 +241,9 @@ struct gb_metric {
   size_t device_bytes() const;  // all device buffers of the handle (gb_metric.cu)
   void release_buffers();       // frees them in the handle's stream order (gb_metric.cu)
   size_t h_cap = 0;             // doubles held by h_params and h_out (pinned, reused across levels)
+
+  int inject_fault = GB_FAULT_NONE;  // gb_metric_set_fault_injection
+  std::string last_error;            // text of the last error raised by a call on this handle
 
   // per-kernel event timing (gb_metric_set_profiling)
   bool profiling = false;

@@ -189,6 +189,9 @@ struct EvalArgs {
   // UseFloatingPointCorrection (MeanSquares, affine): each sample's local derivatives
   // truncated to 1 / fp_res and summed in FP64; 0 = off
   double fp_res;
+  // fault injection (gb_metric_set_fault_injection): GB_FAULT_STALLED_COPY makes the
+  // affine Mattes derivative pass issue none of its record copies
+  int inject_stall;
 };
 
 // The optimizer's stop flag (read once per block, after the launch dependency).
@@ -337,6 +340,30 @@ __device__ __forceinline__ bool grid_sums(const double* blk, double* part, doubl
   return true;
 }
 
+// One-level form of grid_sums for grids of at most kFlatMaxBlocks blocks: every block
+// writes its partials and takes one ticket; the last sums all blocks' partials in
+// block order (lane-strided, fixed XOR trees).  One global round trip fewer than
+// the grouped form.
+constexpr int kFlatMaxBlocks = 1024;
+template <int NV>
+__device__ __forceinline__ bool grid_sums_flat(const double* blk, double* part, unsigned* tick, double* fin,
+                                               VGrid vg = hw_grid()) {
+  __shared__ unsigned t;
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) part[vg.b * NV + k] = blk[k];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) t = atomicAdd(tick, 1u);
+  __syncthreads();
+  if (t != (unsigned)(vg.n - 1)) return false;
+  __threadfence();
+  __shared__ double fin_s[NV];
+  strided_sums<NV>(part, vg.n, fin_s);
+  __syncthreads();
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) fin[k] = fin_s[k];
+  __syncthreads();
+  return true;
+}
+
 __device__ __forceinline__ void block_count(unsigned nv, unsigned long long* gn) {
   __shared__ unsigned sh;
   if (threadIdx.x == 0) sh = 0u;
@@ -387,7 +414,7 @@ __device__ __forceinline__ void msq_affine_body(const EvalArgs& a, VGrid vg) {
     s_next = i + stride < a.n ? __ldcs(a.samples + i + stride) : make_float4(0.f, 0.f, 0.f, 0.f);
     float m;
     float3 g;
-    const DFPos p = map_pos(K.map, s.x, s.y, s.z);
+    const DFPos p = map_pos(load_map(K.map), s.x, s.y, s.z);
     if (!eval_moving<GRAD>(a, p, a.with_derivative != 0, m, g)) continue;
     const float diff = s.w - m;  // FixedImagePixelType diff, MeanSquares...Threader.hxx:46
     acc[0].add(diff * diff);
@@ -683,7 +710,7 @@ __device__ __forceinline__ DFPos sample_pos(const EvalArgs& a, const EvalConsts&
     for (int k = 0; k < 3; ++k) split_double_bits(__ldg(q + k), uhi[k], ulo[k]);
     return field_pos_diag(K, s.x, s.y, s.z, uhi, ulo);
   }
-  const DFPos p = map_pos(K.map, s.x, s.y, s.z);
+  const DFPos p = map_pos(load_map(K.map), s.x, s.y, s.z);
   if (TK == kMapAffine) return p;
   float uhi[3], ulo[3];
   if (TK == kMapFieldDense) {
@@ -740,8 +767,13 @@ __device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, 
   }
 }
 
-static __device__ __noinline__ void mattes_pratio_table(const EvalArgs& a, double T, unsigned long long* cs,
-                                                        unsigned* fm);
+// Barrier among the kBlock streaming threads of a pass-2 block (barrier 0 is
+// __syncthreads, which would also wait for the block's group warp).
+__device__ __forceinline__ void stream_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(kBlock) : "memory"); }
+
+template <bool STREAMERS>
+static __device__ __noinline__ void mattes_pratio_build(const EvalArgs& a, double T, float* dst, float* colf,
+                                                        unsigned* fmask);
 
 // u64 count -> float from its two 32-bit halves, FP32 arithmetic only (two roundings,
 // relative error below 2^-23)
@@ -750,13 +782,21 @@ __device__ __forceinline__ float u64_to_float(unsigned long long v) {
 }
 
 // End of Mattes pass 1 (any transform): flush the block histogram, marginals and
-// count; the last block computes the marginal logs and the derivative's table.
+// count; the last block forms the fixed-point total T and, with `table`, the
+// derivative's log(p / pm) table in global memory (the affine derivative pass
+// builds the table itself, in shared memory).
 __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigned nv, unsigned long long* hist,
-                                                      unsigned long long* cs, unsigned* fm, VGrid vg = hw_grid()) {
+                                                      unsigned long long* cs, unsigned* fm, VGrid vg = hw_grid(),
+                                                      bool table = true) {
   const int B = a.bins;
+  const int BB = B * B;
   __syncthreads();
-  // flush the nonzero bins; the block's column sums ride along as shared atomics
-  for (int k = threadIdx.x; k < B * B; k += blockDim.x) {
+  // flush the nonzero bins; the block's column sums ride along as shared atomics.  Each
+  // block starts at its own bin, so the blocks finishing together do not queue on the
+  // same global addresses.
+  const int rot = (int)(((long long)vg.b * 97) % BB);
+  for (int k0 = threadIdx.x; k0 < BB; k0 += blockDim.x) {
+    const int k = k0 + rot < BB ? k0 + rot : k0 + rot - BB;
     const unsigned long long h = hist[k];
     if (h) {
       atomicAdd(&a.hist[k], h);
@@ -772,8 +812,8 @@ __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigne
   block_count(nv, a.acc_n);
   if (!last_block(a.tickets + kTicketPass1, vg)) return;
   // Last block: the fixed-point total T of the joint histogram (the value's
-  // normalization, JointPDFSum) and the derivative's table.  It is on the
-  // critical path, so it does no FP64 transcendental work.
+  // normalization, JointPDFSum).  It is on the critical path, so it does no FP64
+  // transcendental work.
   __shared__ unsigned long long tot_sh;
   if (threadIdx.x == 0) tot_sh = 0ull;
   __syncthreads();
@@ -786,47 +826,58 @@ __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigne
     a.marg[0] = T;                         // fixed-point total
     a.marg[1] = T > 0.0 ? 1.0 / T : 0.0;   // normalization factor (of the fixed-point histogram)
   }
-  mattes_pratio_table(a, T, cs, fm);
+  if (table) mattes_pratio_build<false>(a, T, a.pratio, reinterpret_cast<float*>(cs), fm);
 }
 
 // The derivative's FP32 table log(p / pm) = log(h / colsum) (pRatio,
 // Mattes...v4.hxx:446-457), 0 where p, pm or pf is not above DBL_EPSILON:
 // for integer counts p > eps <=> h > floor(eps T) and pf > eps <=> count >
-// floor(eps T / 2^26).  Run by pass 1's last block; kept out of line so the
-// sample loop's code is unaffected.
-static __device__ __noinline__ void mattes_pratio_table(const EvalArgs& a, double T, unsigned long long* cs,
-                                                        unsigned* fm) {
+// floor(eps T / 2^26).  Run by a whole block (STREAMERS: by the kBlock streaming
+// threads of a pass-2 block, synchronized on their own barrier), into global
+// (dst = a.pratio) or shared memory, from the final histogram and marginals;
+// colf / fmask are B entries of shared scratch.  Kept out of line so the sample
+// loops' code is unaffected; every caller forms the same bits.
+template <bool STREAMERS>
+static __device__ __noinline__ void mattes_pratio_build(const EvalArgs& a, double T, float* dst, float* colf,
+                                                        unsigned* fmask) {
   const int B = a.bins;
+  const int nt = STREAMERS ? kBlock : (int)blockDim.x;
+  auto sync = [] {
+    if (STREAMERS) stream_barrier();
+    else __syncthreads();
+  };
   const unsigned long long N = __ldcg(a.acc_n);
   const bool bad = N == 0 || !(T * kQInv >= DBL_EPSILON);
   const unsigned long long hthr = (unsigned long long)(DBL_EPSILON * T);
   const unsigned long long fthr = (unsigned long long)(DBL_EPSILON * T * kQInv);
-  // marginals into shared memory (the block's own sums are flushed): column sums as
-  // floats (0 where pm is not above eps), fixed-bin validity
-  float* colf = reinterpret_cast<float*>(cs);
-  for (int k = threadIdx.x; k < B; k += blockDim.x) {
+  sync();  // colf / fmask may alias scratch the caller has just used
+  // marginals into shared memory: column sums as floats (0 where pm is not above
+  // eps), fixed-bin validity
+  for (int k = threadIdx.x; k < B; k += nt) {
     const unsigned long long c = __ldcg(&a.colsum[k]);
     colf[k] = c > hthr ? u64_to_float(c) : 0.f;
-    fm[k] = __ldcg(&a.fmarg[k]) > fthr ? 1u : 0u;
+    fmask[k] = __ldcg(&a.fmarg[k]) > fthr ? 1u : 0u;
   }
-  __syncthreads();
+  sync();
   constexpr int kBatch = 8;  // independent histogram loads in flight per thread
-  for (int k0 = threadIdx.x; k0 < B * B; k0 += kBatch * blockDim.x) {
+  for (int k0 = threadIdx.x; k0 < B * B; k0 += kBatch * nt) {
     unsigned long long h[kBatch];
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
-      const int k = k0 + j * blockDim.x;
+      const int k = k0 + j * nt;
       h[j] = (!bad && k < B * B) ? __ldcg(&a.hist[k]) : 0ull;
     }
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
-      const int k = k0 + j * blockDim.x;
+      const int k = k0 + j * nt;
       if (k >= B * B) break;
       const int f = k / B, m = k - f * B;
       const float c = colf[m];
-      a.pratio[k] = (h[j] > hthr && c > 0.f && fm[f]) ? logf(__fdiv_rn(u64_to_float(h[j]), c)) : 0.f;
+      // fast intrinsics: the ratio is in (0, 1], __logf's error there is below 2^-21 absolute
+      dst[k] = (h[j] > hthr && c > 0.f && fmask[f]) ? __logf(__fdividef(u64_to_float(h[j]), c)) : 0.f;
     }
   }
+  sync();
 }
 
 // Mattes status after pass 1 (Mattes...v4.hxx:367-370 and the valid-point check).
@@ -861,9 +912,10 @@ __device__ __forceinline__ double mattes_group_partial(const EvalArgs& a, int g,
       const double pm = c * invT;
       const double pf = n * (invT * 67108864.0);
       if (pf > DBL_EPSILON && pm > DBL_EPSILON && p > DBL_EPSILON) {
-        const double lr = log(h) - log(c);                                 // log(p / pm)
-        const double lf = log(n) + 26.0 * 0.69314718055994530942 - log(T);  // log pf
-        part = p * (lr - lf);
+        // log(p / pm) - log pf = log(h T / (c n 2^26)): the counts and T are integers
+        // below 2^53, so each product rounds once; one FP64 log per bin (GB300's FP64
+        // rate makes every log call cost microseconds per warp)
+        part = p * log((h * T) / ((c * n) * 67108864.0));
       }
     }
     a.pdf_out[bin] = p;
@@ -912,6 +964,8 @@ __device__ __forceinline__ void mattes_pass1_affine_body(const EvalArgs& a, VGri
   unsigned nv = 0;
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)vg.n * blockDim.x;
+  // the affine derivative pass builds the log(p / pm) table itself
+  constexpr bool kOwnTable = TK == kMapAffine;
   int64_t base = (int64_t)vg.b * blockDim.x + (threadIdx.x & ~31);
   float4 s_next = base + lane < a.n ? __ldcs(a.samples + base + lane) : make_float4(0.f, 0.f, 0.f, 0.f);
   for (; base < a.n; base += stride) {
@@ -948,7 +1002,7 @@ __device__ __forceinline__ void mattes_pass1_affine_body(const EvalArgs& a, VGri
     hist_add_aggregated(ok, fidx * B + pdfm, fidx, q, hist, fm);
     nv += ok ? 1u : 0u;
   }
-  mattes_pass1_epilogue(a, nv, hist, cs, fm, vg);
+  mattes_pass1_epilogue(a, nv, hist, cs, fm, vg, !kOwnTable);
 }
 
 template <int GRAD>
@@ -983,10 +1037,18 @@ __global__ void __launch_bounds__(kFinalizeThreads) k_mattes_finalize(EvalArgs a
 // Streamed record tiles: each block owns a contiguous, tile-aligned range of
 // samples; thread 0 keeps kStreamStages tiles of (cache, sample) records in
 // flight with bulk asynchronous copies, completed on one mbarrier per stage.
-constexpr int kStreamStages = 2;
+constexpr int kStreamStages = 4;
 constexpr int kStreamPer = 2;                     // records per thread and tile
 constexpr int kStreamTile = kBlock * kStreamPer;  // records per stage and stream
 constexpr size_t kStreamBytes = (size_t)2 * kStreamStages * kStreamTile * sizeof(float4);
+// mbarrier polls of a wait under the stalled-copy fault injection (GB_FAULT_STALLED_COPY)
+constexpr unsigned kInjectWaitPolls = 256;
+
+// Dynamic shared memory of the Mattes derivative pass: the record stages, the
+// bins^2 log(p / pm) table, B column sums and B fixed-bin flags.
+__host__ __device__ inline size_t mattes_pass2_smem(int bins) {
+  return kStreamBytes + sizeof(float) * (size_t)bins * bins + 8 * (size_t)bins;
+}
 
 // Whole tiles spread evenly: block b gets tiles [b T / G, (b + 1) T / G).
 __device__ __forceinline__ void block_range(int64_t n, int64_t& b0, int64_t& b1, VGrid vg) {
@@ -995,30 +1057,51 @@ __device__ __forceinline__ void block_range(int64_t n, int64_t& b0, int64_t& b1,
   b1 = min(n, (int64_t)(vg.b + 1) * tiles / vg.n * kStreamTile);
 }
 
+// Threads of a plain pass-2 block: kBlock streaming threads and one group warp.
+constexpr int kPass2Threads = kBlock + 32;
+
 // Mattes pass 2, affine: derivative from the cached Parzen terms and gradients.
-// Dynamic shared memory: kStreamBytes of record stages, then the bins^2 log(p/pm) table.
+// Dynamic shared memory: mattes_pass2_smem(bins).
+//
+// GROUP_WARP (the plain launch, kPass2Threads threads): the block's last warp forms
+// the value's FP64 group partial (block b: group b) while the other kBlock threads
+// stream the records, so the FP64 chain -- GB300 issues FP64 at a small fraction of
+// its FP32 rate -- overlaps the streaming instead of delaying it; the streaming
+// threads synchronize per tile on a named barrier of their own.  Without it (the
+// batched engine, kBlock threads) the last warp forms the groups before the loop.
+template <bool GROUP_WARP>
 __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGrid vg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int kWarps = (GROUP_WARP ? kPass2Threads : kBlock) / 32;
+  const int B = a.bins;
   float4* cbuf = reinterpret_cast<float4*>(smem_raw);  // [stage][tile] cache records
   float4* sbuf = cbuf + kStreamStages * kStreamTile;    // [stage][tile] sample records
   float* pr = reinterpret_cast<float*>(smem_raw + kStreamBytes);
+  float* colf = pr + B * B;
+  unsigned* fmask = reinterpret_cast<unsigned*>(colf + B);
   __shared__ unsigned long long full[kStreamStages];
   __shared__ int failed;
   __shared__ EvalConsts K;
-  __shared__ float red[kBlock / 32][12];
+  __shared__ float red[kWarps][12];
   __shared__ double blk[12], fin[12];
-  const int B = a.bins;
   int64_t b0, b1;
   block_range(a.n, b0, b1, vg);
   const int ntiles = (int)((b1 - b0 + kStreamTile - 1) / kStreamTile);
+  // fault injection: no copy is ever issued, so every wait runs out (after a short limit)
+  const bool stall = a.inject_stall != 0;
+  const unsigned limit = stall ? kInjectWaitPolls : kWaitLimit;
+  const bool streamer = !GROUP_WARP || (int)threadIdx.x < kBlock;
+  int issued = 0;  // thread 0: tiles whose copies are issued
   // tile t -> stage t % kStreamStages; the stage's phase parity is (t / kStreamStages) & 1
   auto issue = [&](int t) {
     const int st = t % kStreamStages;
     const int64_t r0 = b0 + (int64_t)t * kStreamTile;
     const unsigned bytes = (unsigned)(min((int64_t)kStreamTile, b1 - r0) * sizeof(float4));
+    const uint64_t pol = l2_policy_evict_first();  // last use of both records in this evaluation
     mbar_arrive_expect_tx(&full[st], 2 * bytes);
-    bulk_g2s(cbuf + st * kStreamTile, a.cache + r0, bytes, &full[st]);
-    bulk_g2s(sbuf + st * kStreamTile, a.samples + r0, bytes, &full[st]);
+    bulk_g2s_hint(cbuf + st * kStreamTile, a.cache + r0, bytes, &full[st], pol);
+    bulk_g2s_hint(sbuf + st * kStreamTile, a.samples + r0, bytes, &full[st], pol);
+    issued = t + 1;
   };
   if (threadIdx.x == 0) {
     for (int st = 0; st < kStreamStages; ++st) mbar_init(&full[st], 1);
@@ -1028,56 +1111,74 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
   griddep_wait();
   if (halted(a)) return;
   griddep_launch_dependents();
-  if (threadIdx.x == 0)
+  // the first tiles travel while the table and the constants are formed
+  if (threadIdx.x == 0 && !stall)
     for (int t = 0; t < min(kStreamStages, ntiles); ++t) issue(t);
-  for (int k = threadIdx.x; k < B * B; k += blockDim.x) pr[k] = __ldcg(&a.pratio[k]);
   load_consts(a.consts, K);
-  mattes_value_groups(a, vg);  // the value's FP64 group partials, last warp (thread 0 feeds the copies)
-  __syncthreads();
-  // plain FP32 per thread (a thread adds a few dozen samples; the warp tree and the
-  // FP64 cross-block sums follow)
+  __syncthreads();  // the barriers' initialization and the constants
   float acc[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k] = 0.f;
-  int t = 0;
-  for (; t < ntiles; ++t) {
-    const int st = t % kStreamStages;
-    if (!mbar_wait(&full[st], (unsigned)(t / kStreamStages) & 1u)) failed = 1;
-    const int64_t r0 = b0 + (int64_t)t * kStreamTile;
-    const int cnt = (int)min((int64_t)kStreamTile, b1 - r0);
-#pragma unroll
-    for (int u = 0; u < kStreamPer; ++u) {
-      const int j = threadIdx.x + u * kBlock;
-      if (failed || j >= cnt) continue;
-      const float4 cc = cbuf[st * kStreamTile + j];
-      const float4 s = sbuf[st * kStreamTile + j];
-      if (cc.x != cc.x) continue;  // NaN term: rejected sample
-      int pdfm;
-      float tt, d[4];
-      parzen_window(cc.x, B, pdfm, tt);
-      parzen_deriv(tt, d);
-      const float* row = pr + __float_as_int(s.w) * B + pdfm;
-      const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
-      const float3 v = jac_vec(K, s.x, s.y, s.z);
-      const float t0 = w * cc.y, t1 = w * cc.z, t2 = w * cc.w;
-      acc[0] = fmaf(t0, v.x, acc[0]); acc[1] = fmaf(t0, v.y, acc[1]); acc[2] = fmaf(t0, v.z, acc[2]);
-      acc[3] = fmaf(t1, v.x, acc[3]); acc[4] = fmaf(t1, v.y, acc[4]); acc[5] = fmaf(t1, v.z, acc[5]);
-      acc[6] = fmaf(t2, v.x, acc[6]); acc[7] = fmaf(t2, v.y, acc[7]); acc[8] = fmaf(t2, v.z, acc[8]);
-      acc[9] += t0; acc[10] += t1; acc[11] += t2;
-    }
-    __syncthreads();  // stage st consumed by every thread
-    if (failed) break;
-    if (threadIdx.x == 0 && t + kStreamStages < ntiles) {
-      fence_proxy_async_smem();
-      issue(t + kStreamStages);
+  if (!GROUP_WARP) {
+    mattes_pratio_build<false>(a, __ldcg(&a.marg[0]), pr, colf, fmask);
+    mattes_value_groups(a, vg);  // the value's FP64 group partials, last warp
+    __syncthreads();
+  } else if (streamer) {
+    mattes_pratio_build<true>(a, __ldcg(&a.marg[0]), pr, colf, fmask);
+  } else {
+    // the group warp: its FP64 chain runs while the other warps stream
+    const int ng = mattes_groups(B);
+    for (int g = vg.b; g < ng; g += vg.n) {
+      const double sg = mattes_group_partial(a, g, threadIdx.x & 31);
+      if ((threadIdx.x & 31) == 0) a.part[g] = sg;
     }
   }
+  int t = 0;
+  if (streamer) {
+    // plain FP32 per thread (a thread adds a few dozen samples; the warp tree and the
+    // FP64 cross-block sums follow)
+    for (; t < ntiles; ++t) {
+      const int st = t % kStreamStages;
+      const bool landed = mbar_wait(&full[st], (unsigned)(t / kStreamStages) & 1u, limit);
+      if (!landed) failed = 1;
+      const int64_t r0 = b0 + (int64_t)t * kStreamTile;
+      const int cnt = (int)min((int64_t)kStreamTile, b1 - r0);
+#pragma unroll
+      for (int u = 0; u < kStreamPer; ++u) {
+        const int j = threadIdx.x + u * kBlock;
+        if (!landed || j >= cnt) continue;
+        const float4 cc = cbuf[st * kStreamTile + j];
+        const float4 s = sbuf[st * kStreamTile + j];
+        if (cc.x != cc.x) continue;  // NaN term: rejected sample
+        int pdfm;
+        float tt, d[4];
+        parzen_window(cc.x, B, pdfm, tt);
+        parzen_deriv(tt, d);
+        const float* row = pr + __float_as_int(s.w) * B + pdfm;
+        const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
+        const float3 v = jac_vec(K, s.x, s.y, s.z);
+        const float t0 = w * cc.y, t1 = w * cc.z, t2 = w * cc.w;
+        acc[0] = fmaf(t0, v.x, acc[0]); acc[1] = fmaf(t0, v.y, acc[1]); acc[2] = fmaf(t0, v.z, acc[2]);
+        acc[3] = fmaf(t1, v.x, acc[3]); acc[4] = fmaf(t1, v.y, acc[4]); acc[5] = fmaf(t1, v.z, acc[5]);
+        acc[6] = fmaf(t2, v.x, acc[6]); acc[7] = fmaf(t2, v.y, acc[7]); acc[8] = fmaf(t2, v.z, acc[8]);
+        acc[9] += t0; acc[10] += t1; acc[11] += t2;
+      }
+      // stage st consumed by every streaming thread; `failed` seen by all of them
+      if (GROUP_WARP) stream_barrier();
+      else __syncthreads();
+      if (failed) break;
+      if (threadIdx.x == 0 && t + kStreamStages < ntiles) {
+        fence_proxy_async_smem();
+        issue(t + kStreamStages);
+      }
+    }
+  }
+  if (GROUP_WARP) __syncthreads();  // the group warp joins
   if (failed) {
-    // a copy never completed: report, drain what is still in flight (bounded), leave
+    // a copy never completed: report, wait (bounded) for the copies still in flight, leave
     if (threadIdx.x == 0) {
       atomicExch(a.status, GB_ERR_TIMEOUT);
-      for (int u = t + 1; u < min(ntiles, t + kStreamStages); ++u)
-        mbar_wait(&full[u % kStreamStages], (unsigned)(u / kStreamStages) & 1u);
+      for (int u = t + 1; u < issued; ++u) mbar_wait(&full[u % kStreamStages], (unsigned)(u / kStreamStages) & 1u);
     }
     return;
   }
@@ -1088,7 +1189,10 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
     kacc[k].c = 0.f;
   }
   block_sums<12>(kacc, red, blk);
-  if (!grid_sums<12>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin, vg)) return;
+  const bool last = vg.n <= kFlatMaxBlocks
+                        ? grid_sums_flat<12>(blk, a.part + kPartPass2, a.tickets + kTicketPass2, fin, vg)
+                        : grid_sums<12>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin, vg);
+  if (!last) return;
   // last block: the value from the group partials (all blocks wrote theirs before their tickets)
   if (threadIdx.x < 32) {
     const double s = mattes_value_sum(a.part, mattes_groups(B), threadIdx.x);
@@ -1111,7 +1215,9 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
 }
 
 #ifndef GB_KERNELS_HELPERS_ONLY
-__global__ void __launch_bounds__(kBlock, 4) k_mattes_pass2_affine(EvalArgs a) { mattes_pass2_affine_body(a, hw_grid()); }
+__global__ void __launch_bounds__(kPass2Threads, 3) k_mattes_pass2_affine(EvalArgs a) {
+  mattes_pass2_affine_body<true>(a, hw_grid());
+}
 #endif  // GB_KERNELS_HELPERS_ONLY
 
 }  // namespace gb

@@ -22,8 +22,15 @@
 namespace gb {
 
 static thread_local std::string g_last_error;
+static thread_local gb_metric* g_error_scope = nullptr;
 
-void set_error(const std::string& msg) { g_last_error = msg; }
+gb_metric* error_scope() { return g_error_scope; }
+void set_error_scope(gb_metric* m) { g_error_scope = m; }
+
+void set_error(const std::string& msg) {
+  g_last_error = msg;
+  if (g_error_scope) g_error_scope->last_error = msg;
+}
 
 int fail(int code, const std::string& msg) {
   set_error(msg);
@@ -224,6 +231,8 @@ using namespace gb;
 
 extern "C" const char* gb_last_error(void) { return g_last_error.c_str(); }
 
+extern "C" const char* gb_metric_last_error(gb_metric* m) { return m ? m->last_error.c_str() : ""; }
+
 extern "C" const char* gb_version(void) { return "itk_gb300 0.1 (sm_103a)"; }
 
 extern "C" int gb_ctx_create(int device, gb_ctx** out) {
@@ -316,6 +325,7 @@ extern "C" int gb_metric_destroy(gb_metric* m) {
 }
 
 extern "C" int gb_metric_set_floating_point_correction(gb_metric* m, int on, double resolution) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (on && !(resolution > 0.0)) return fail(GB_ERR_BAD_ARG, "floating point correction resolution must be > 0");
   m->fp_res = on ? resolution : 0.0;
@@ -324,6 +334,7 @@ extern "C" int gb_metric_set_floating_point_correction(gb_metric* m, int on, dou
 }
 
 extern "C" int gb_metric_set_joint_pdf_smoothing_variance(gb_metric* m, double variance) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (!(variance == variance)) return fail(GB_ERR_BAD_ARG, "variance is NaN");
   m->jhmi_variance = variance;
@@ -332,6 +343,7 @@ extern "C" int gb_metric_set_joint_pdf_smoothing_variance(gb_metric* m, double v
 }
 
 extern "C" int gb_metric_set_number_of_histogram_bins(gb_metric* m, uint64_t bins) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (bins < 5) bins = 5;  // itkSetClampMacro(NumberOfHistogramBins, SizeValueType, 5, max)
   if (bins > 4096) return fail(GB_ERR_BAD_ARG, "number of histogram bins above 4096");
@@ -364,16 +376,19 @@ static int set_image_common(gb_metric* m, int which, const float* src, bool devi
 
 extern "C" int gb_metric_set_image(gb_metric* m, int which, const float* voxels, const int64_t size[3],
                                    const double spacing[3], const double origin[3], const double direction[9]) {
+  gb::ErrorScope scope_(m);
   return set_image_common(m, which, voxels, false, size, spacing, origin, direction);
 }
 
 extern "C" int gb_metric_set_image_device(gb_metric* m, int which, const float* device_voxels, const int64_t size[3],
                                           const double spacing[3], const double origin[3],
                                           const double direction[9]) {
+  gb::ErrorScope scope_(m);
   return set_image_common(m, which, device_voxels, true, size, spacing, origin, direction);
 }
 
 extern "C" int gb_metric_set_gradient_source(gb_metric* m, int source) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (source != GB_GRADIENT_IMAGE && source != GB_GRADIENT_CENTRAL_DIFFERENCE &&
       source != GB_GRADIENT_RECURSIVE_GAUSSIAN)
@@ -384,6 +399,7 @@ extern "C" int gb_metric_set_gradient_source(gb_metric* m, int source) {
 }
 
 extern "C" int gb_metric_set_moving_gradient_image(gb_metric* m, const double* gradient_xyz) {
+  gb::ErrorScope scope_(m);
   if (!m || !gradient_xyz) return fail(GB_ERR_BAD_ARG, "null argument");
   if (!m->moving.set) return fail(GB_ERR_BAD_ARG, "set the moving image before its gradient image");
   GB_CUDA(cudaSetDevice(m->ctx->device));
@@ -399,6 +415,7 @@ extern "C" int gb_metric_set_moving_gradient_image(gb_metric* m, const double* g
 
 extern "C" int gb_metric_set_virtual_domain(gb_metric* m, const int64_t size[3], const double spacing[3],
                                             const double origin[3], const double direction[9]) {
+  gb::ErrorScope scope_(m);
   if (!m || !size || !spacing || !origin || !direction) return fail(GB_ERR_BAD_ARG, "null argument");
   Geom g;
   int rc = geom_init(g, size, spacing, origin, direction);
@@ -410,6 +427,7 @@ extern "C" int gb_metric_set_virtual_domain(gb_metric* m, const int64_t size[3],
 }
 
 extern "C" int gb_metric_set_level_smoothing(gb_metric* m, double sigma, int sigma_in_physical_units) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (!(sigma >= 0.0) || !std::isfinite(sigma)) return fail(GB_ERR_BAD_ARG, "smoothing sigma must be >= 0");
   m->level_sigma = sigma;
@@ -419,6 +437,7 @@ extern "C" int gb_metric_set_level_smoothing(gb_metric* m, double sigma, int sig
 }
 
 extern "C" int gb_metric_set_level_shrink(gb_metric* m, const int64_t factors[3]) {
+  gb::ErrorScope scope_(m);
   if (!m || !factors) return fail(GB_ERR_BAD_ARG, "null argument");
   for (int i = 0; i < 3; ++i) m->level_shrink[i] = factors[i] < 1 ? 1 : factors[i];  // ShrinkImageFilter clamps to 1
   m->initialized = false;
@@ -426,6 +445,7 @@ extern "C" int gb_metric_set_level_shrink(gb_metric* m, const int64_t factors[3]
 }
 
 extern "C" int gb_metric_set_sampled_points(gb_metric* m, const float* xyz, int64_t n, int virtual_space) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (n < 0 || (n > 0 && !xyz)) return fail(GB_ERR_BAD_ARG, "bad point array");
   if (n > (int64_t)0x7fffffff) return fail(GB_ERR_BAD_ARG, "more than 2^31-1 sample points");
@@ -436,6 +456,7 @@ extern "C" int gb_metric_set_sampled_points(gb_metric* m, const float* xyz, int6
 }
 
 extern "C" int gb_metric_use_sampled_point_set(gb_metric* m, int on) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   m->use_sampled = on != 0;
   m->initialized = false;
@@ -444,6 +465,7 @@ extern "C" int gb_metric_use_sampled_point_set(gb_metric* m, int on) {
 
 extern "C" int gb_metric_set_moving_transform(gb_metric* m, int kind, const double* params, int64_t nparams,
                                               const double* fixed, int64_t nfixed) {
+  gb::ErrorScope scope_(m);
   if (!m || !params || !fixed) return fail(GB_ERR_BAD_ARG, "null argument");
   if (kind == GB_TRANSFORM_AFFINE) {
     if (nparams != 12 || nfixed != 3) return fail(GB_ERR_BAD_ARG, "affine transform takes 12 parameters and a 3-D centre");
@@ -488,6 +510,7 @@ extern "C" int gb_metric_set_moving_transform(gb_metric* m, int kind, const doub
 }
 
 extern "C" int gb_metric_set_parameters(gb_metric* m, const double* params, int64_t nparams) {
+  gb::ErrorScope scope_(m);
   if (!m || !params) return fail(GB_ERR_BAD_ARG, "null argument");
   if (m->tkind < 0) return fail(GB_ERR_BAD_ARG, "no moving transform set");
   if ((size_t)nparams != m->tparams.size()) return fail(GB_ERR_BAD_ARG, "parameter count mismatch");
@@ -497,6 +520,7 @@ extern "C" int gb_metric_set_parameters(gb_metric* m, const double* params, int6
 
 extern "C" int gb_metric_update_transform_parameters(gb_metric* m, const double* update, int64_t nparams,
                                                      double factor) {
+  gb::ErrorScope scope_(m);
   if (!m || !update) return fail(GB_ERR_BAD_ARG, "null argument");
   if ((size_t)nparams != m->tparams.size())
     return fail(GB_ERR_BAD_ARG, "Parameter update size must be same as transform parameter size");
@@ -508,6 +532,7 @@ extern "C" int gb_metric_update_transform_parameters(gb_metric* m, const double*
 }
 
 extern "C" int gb_metric_get_parameters(gb_metric* m, double* params, int64_t nparams) {
+  gb::ErrorScope scope_(m);
   if (!m || !params) return fail(GB_ERR_BAD_ARG, "null argument");
   if ((size_t)nparams != m->tparams.size()) return fail(GB_ERR_BAD_ARG, "parameter count mismatch");
   copy_parallel(params, m->tparams.data(), sizeof(double) * m->tparams.size());
@@ -515,6 +540,7 @@ extern "C" int gb_metric_get_parameters(gb_metric* m, double* params, int64_t np
 }
 
 extern "C" int gb_metric_get_number_of_parameters(gb_metric* m, int64_t* nparams) {
+  gb::ErrorScope scope_(m);
   if (!m || !nparams) return fail(GB_ERR_BAD_ARG, "null argument");
   *nparams = (int64_t)m->tparams.size();
   return GB_OK;
@@ -535,6 +561,7 @@ static size_t acc_layout_bytes(const gb_metric* m) {
 }
 
 extern "C" int gb_metric_initialize(gb_metric* m) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   m->drop_host_graphs();  // they hold this level's buffers and arguments
   if (!m->fixed.set) return fail(GB_ERR_BAD_ARG, "FixedImage is not present");
@@ -1003,6 +1030,7 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   a.with_derivative = deriv ? 1 : 0;
   a.halt = m->eval_halt;
   a.fp_res = m->fp_res;
+  a.inject_stall = m->inject_fault == GB_FAULT_STALLED_COPY ? 1 : 0;
   if (is_bspline(m)) {
     a.sup = m->d_sup.p;
     a.nodes = m->d_nodes.p;
@@ -1056,6 +1084,21 @@ static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalAr
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   return launch_chain(m, kernel, (unsigned)full_wave(m, kernel, smem, m->nsamples), kBlock, smem, a, extra...);
+}
+
+// Mattes pass 2 (affine): kPass2Threads threads per block (the streaming threads and
+// the value's group warp), one full wave, at most kFlatMaxBlocks blocks (the one-level
+// cross-block sums).
+static cudaError_t launch_pass2(gb_metric* m, size_t smem, const EvalArgs& a) {
+  cudaError_t e = cudaFuncSetAttribute(k_mattes_pass2_affine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mattes_pass2_affine, kPass2Threads, smem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 2;
+  const int grid = std::min(grid_for(m, m->nsamples, per_sm), kFlatMaxBlocks);
+  return launch_chain(m, k_mattes_pass2_affine, (unsigned)grid, kPass2Threads, smem, a);
 }
 
 // B-spline / composite evaluation: node conversion (large grids), the per-sample
@@ -1323,7 +1366,7 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
   // Mattes: pass 1, finalize, pass 2
   const int B = (int)m->bins;
   const size_t sh1 = sizeof(unsigned long long) * (B * B + B) + sizeof(unsigned) * B;
-  const size_t sh2 = kStreamBytes + sizeof(float) * B * B;  // record stages + log(p/pm) table
+  const size_t sh2 = mattes_pass2_smem(B);  // record stages + log(p/pm) table
   if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
   GB_CUDA(cd ? launch_wave(m, k_mattes_pass1_affine<kGradCentralDifference>, sh1, a)
              : launch_wave(m, k_mattes_pass1_affine<kGradImage>, sh1, a));
@@ -1332,13 +1375,23 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
     GB_CUDA(launch_chain(m, k_mattes_finalize, (unsigned)mattes_groups(B), kFinalizeThreads, 0, a));
     m->mark();
   } else {
-    GB_CUDA(launch_wave(m, k_mattes_pass2_affine, sh2, a));
+    GB_CUDA(launch_pass2(m, sh2, a));
     m->mark();
   }
   return GB_OK;
 }
 
+extern "C" int gb_metric_set_fault_injection(gb_metric* m, int fault) {
+  gb::ErrorScope scope_(m);
+  if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
+  if (fault != GB_FAULT_NONE && fault != GB_FAULT_STALLED_COPY) return fail(GB_ERR_BAD_ARG, "unknown fault");
+  if (fault != m->inject_fault) m->drop_host_graphs();  // the graphs hold the kernels' arguments
+  m->inject_fault = fault;
+  return GB_OK;
+}
+
 extern "C" int gb_metric_set_profiling(gb_metric* m, int on) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   m->profiling = on != 0;
   m->nevents = 0;
@@ -1346,6 +1399,7 @@ extern "C" int gb_metric_set_profiling(gb_metric* m, int on) {
 }
 
 extern "C" int gb_metric_get_kernel_times(gb_metric* m, double* ms, int max_kernels, int* count) {
+  gb::ErrorScope scope_(m);
   if (!m || !count) return fail(GB_ERR_BAD_ARG, "null argument");
   GB_CUDA(cudaSetDevice(m->ctx->device));
   const int n = m->nevents > 1 ? m->nevents - 1 : 0;
@@ -1459,33 +1513,40 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
                 "overlap appropriately.");
   }
   if (status == GB_ERR_JOINT_PDF_SUM_ZERO) return fail(status, "Joint PDF summed to zero");
+  if (status == GB_ERR_TIMEOUT)
+    return fail(status, "metric evaluation timed out: a streamed copy did not complete within its wait limit");
   if (status != GB_OK) return fail(status, "metric evaluation failed");
   return GB_OK;
 }
 
 extern "C" int gb_metric_get_value_and_derivative(gb_metric* m, double* value, double* derivative, int64_t nparams) {
+  gb::ErrorScope scope_(m);
   if (!derivative || !value) return fail(GB_ERR_BAD_ARG, "null output");
   return eval_host(m, value, derivative, nparams, true);
 }
 
 extern "C" int gb_metric_get_value(gb_metric* m, double* value) {
+  gb::ErrorScope scope_(m);
   if (!value) return fail(GB_ERR_BAD_ARG, "null output");
   return eval_host(m, value, nullptr, 0, false);
 }
 
 extern "C" int gb_metric_get_number_of_valid_points(gb_metric* m, uint64_t* nvalid) {
+  gb::ErrorScope scope_(m);
   if (!m || !nvalid) return fail(GB_ERR_BAD_ARG, "null argument");
   *nvalid = m->last_nvalid;
   return GB_OK;
 }
 
 extern "C" int gb_metric_get_number_of_domain_points(gb_metric* m, uint64_t* n) {
+  gb::ErrorScope scope_(m);
   if (!m || !n) return fail(GB_ERR_BAD_ARG, "null argument");
   *n = (uint64_t)m->ndomain;
   return GB_OK;
 }
 
 extern "C" int gb_metric_get_joint_pdf(gb_metric* m, double* out, int64_t n) {
+  gb::ErrorScope scope_(m);
   if (!m || !out) return fail(GB_ERR_BAD_ARG, "null argument");
   if (m->kind != GB_METRIC_MATTES && m->kind != GB_METRIC_JOINT_HISTOGRAM_MI)
     return fail(GB_ERR_BAD_ARG, "joint PDF exists for the Mattes and joint-histogram metrics only");
@@ -1498,6 +1559,7 @@ extern "C" int gb_metric_get_joint_pdf(gb_metric* m, double* out, int64_t n) {
 }
 
 extern "C" int gb_metric_get_mattes_state(gb_metric* m, double out8[8]) {
+  gb::ErrorScope scope_(m);
   if (!m || !out8) return fail(GB_ERR_BAD_ARG, "null argument");
   if (m->kind != GB_METRIC_MATTES) return fail(GB_ERR_BAD_ARG, "Mattes metric only");
   for (int i = 0; i < 8; ++i) out8[i] = m->mstate[i];
@@ -1515,12 +1577,14 @@ size_t gb_metric::device_bytes() const {
 }
 
 extern "C" int gb_metric_get_device_bytes(gb_metric* m, uint64_t* bytes) {
+  gb::ErrorScope scope_(m);
   if (!m || !bytes) return fail(GB_ERR_BAD_ARG, "null argument");
   *bytes = (uint64_t)m->device_bytes();
   return GB_OK;
 }
 
 extern "C" int gb_metric_get_stream(gb_metric* m, uint64_t* stream) {
+  gb::ErrorScope scope_(m);
   if (!m || !stream) return fail(GB_ERR_BAD_ARG, "null argument");
   *stream = (uint64_t)(uintptr_t)m->stream;
   return GB_OK;
@@ -1528,6 +1592,7 @@ extern "C" int gb_metric_get_stream(gb_metric* m, uint64_t* stream) {
 
 extern "C" int gb_metric_evaluate_device(gb_metric* m, const double* device_params, double* device_out,
                                          int with_derivative) {
+  gb::ErrorScope scope_(m);
   if (!m || !device_params || !device_out) return fail(GB_ERR_BAD_ARG, "null argument");
   if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
   GB_CUDA(cudaSetDevice(m->ctx->device));
@@ -1535,6 +1600,7 @@ extern "C" int gb_metric_evaluate_device(gb_metric* m, const double* device_para
 }
 
 extern "C" int gb_metric_synchronize(gb_metric* m) {
+  gb::ErrorScope scope_(m);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   GB_CUDA(cudaSetDevice(m->ctx->device));
   GB_CUDA(cudaMemcpyAsync(m->h_status, m->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));

@@ -276,6 +276,12 @@ class ImageToImageMetricv4:
     def synchronize(self) -> int:
         return self._L.gb_metric_synchronize(self._h)
 
+    def set_fault_injection(self, fault: int):
+        """Failure-detection test hook (gb_metric_set_fault_injection): GB_FAULT_STALLED_COPY makes
+        the affine Mattes derivative pass's bounded copy waits run out (GB_ERR_TIMEOUT);
+        GB_FAULT_NONE restores normal evaluations."""
+        check(self._L.gb_metric_set_fault_injection(self._h, int(fault)))
+
     def set_profiling(self, on: bool = True):
         check(self._L.gb_metric_set_profiling(self._h, int(on)))
 
