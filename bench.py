@@ -632,7 +632,8 @@ def measure_evaluation(args, world, rank, local, dist):
 # 1 for the translation; learning rate 1 mm, minimum step 5e-3, 100 iterations).  Three
 # paths run the same registrations: the plain per-call GPU path (host optimizer
 # loop, one GetValueAndDerivative call per iteration), the device optimizer loop
-# one registration after another, and the batched engine.
+# one registration after another, and the batched engine (per-phase launches in a CUDA
+# graph; beside it the persistent form, several iterations per launch, for comparison).
 # Served: 64 requests on the same image pairs (other sampling seeds), 1-3 pyramid
 # levels (shrink 4/2/1, sigma 2/1/0), 50-200 iterations per level, Poisson
 # arrivals at 80 % of the server's measured capacity, 120 GB HBM budget; the
@@ -763,8 +764,9 @@ def run_batched_form(args, inst, t_gen):
             its.append(o.GetCurrentIteration())
         return time.perf_counter() - t0, its, [T.GetParameters().copy() for _, T, _, _, _, _ in sel]
 
-    def batched(sel, tune=True):
+    def batched(sel, tune=True, persistent=False):
         b = RegistrationBatch()
+        b.SetPersistent(persistent)
         opts = []
         for m, T, p0, _, sc, _ in sel:
             T.SetParameters(p0)
@@ -806,7 +808,9 @@ def run_batched_form(args, inst, t_gen):
         tp, ip, pp = plain(sel) if "plain" in paths else (None, None, None)
         tl, il, pl = loop(sel) if "loop" in paths else (None, None, None)
         tb, ib, pb, spb, t_tune, stats = batched(sel)
-        res["regs_per_s"] = {"batched": len(sel) / tb}
+        tq, iq, pq, _, _, _ = batched(sel, persistent=True)
+        res["regs_per_s"] = {"batched": len(sel) / tb, "batched_persistent_form": len(sel) / tq}
+        res["persistent_equals_per_phase"] = bool(all(np.array_equal(x, y) for x, y in zip(pb, pq)))
         res["msamples_per_s"] = {"batched": evals(sel, ib) / tb / 1e6}
         res["seconds"] = {"batched": tb, "autotune": t_tune}
         res["iterations_total"] = {"batched": int(sum(ib))}

@@ -345,8 +345,9 @@ int gb_metric_set_optimizer_graphs(gb_metric *m, int on);
  * RegularStepGradientDescentOptimizerv4 settings, advance together -- one
  * launch per phase of an iteration for all of them (accumulator clear,
  * transform constants, MeanSquares pass, Mattes pass 1, Mattes pass 2,
- * AdvanceOneStep), captured as a CUDA graph.  A registration's results do not
- * depend on which others share the batch.  While a metric is in a batch, make
+ * AdvanceOneStep), captured as a CUDA graph -- or, in the persistent form, one
+ * launch for several iterations.  A registration's results do not depend on which others share
+ * the batch.  While a metric is in a batch, make
  * no other call on it. */
 typedef struct gb_batch gb_batch;
 int gb_batch_create(gb_ctx *ctx, gb_batch **out);
@@ -367,8 +368,15 @@ int gb_batch_result(gb_batch *b, int64_t slot, int *finished, gb_optimizer_repor
 int gb_batch_set_samples_per_block(gb_batch *b, const int64_t spb[3]);
 int gb_batch_get_samples_per_block(gb_batch *b, int64_t spb[3]);
 int gb_batch_autotune(gb_batch *b, int iterations, int64_t spb[3]);
-/* Capture the iteration in a CUDA graph (default on). */
+/* Capture the iteration in a CUDA graph (default on; the per-phase form). */
 int gb_batch_set_graphs(gb_batch *b, int on);
+/* The persistent form (default off): every iteration of every running
+ * registration -- clears, constants, metric passes, steps -- in one kernel
+ * launch that runs several iterations, each work item waiting (bounded) only
+ * for its own registration's earlier items; off: one launch per phase and
+ * iteration, captured as a CUDA graph.  A registration's results are bitwise
+ * the same in both forms. */
+int gb_batch_set_persistent(gb_batch *b, int on);
 /* Iterations launched, table rebuilds (registrations joining or leaving) and
  * the host seconds they took, since the batch was created. */
 int gb_batch_get_stats(gb_batch *b, int64_t *iterations, int64_t *rebuilds, double *rebuild_seconds);

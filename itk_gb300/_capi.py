@@ -139,6 +139,7 @@ SIGNATURES = {
     "gb_batch_get_samples_per_block": [_P, _P],
     "gb_batch_autotune": [_P, _I, _P],
     "gb_batch_set_graphs": [_P, _I],
+    "gb_batch_set_persistent": [_P, _I],
     "gb_batch_get_stats": [_P, _P, _P, _P],
     "gb_sample_count": [_I, _P, _D, _P],
     "gb_sample_points": [_I, _P, _P, _P, _P, _D, ctypes.c_int32, _P, _I64, _P, _P],

@@ -2,7 +2,8 @@
 
 Each registration is an initialized metric with a
 RegularStepGradientDescentOptimizerv4 holding its settings; one optimizer
-iteration of every running registration is one graph launch.  A registration's
+iteration of every running registration is one graph launch of a kernel per phase
+(or, in the persistent form, one kernel launch carries several iterations).  A registration's
 result does not depend on the others in the batch.
 """
 from __future__ import annotations
@@ -99,3 +100,8 @@ class RegistrationBatch:
 
     def SetUseCudaGraphs(self, on: bool):
         check(self._L.gb_batch_set_graphs(self._h, int(bool(on))))
+
+    def SetPersistent(self, on: bool):
+        """Several iterations of every registration per kernel launch, or (default) one
+        launch per phase and iteration; the results are bitwise the same."""
+        check(self._L.gb_batch_set_persistent(self._h, int(bool(on))))

@@ -108,8 +108,196 @@ __global__ void __launch_bounds__(32) k_batch_step(const StepArgs* __restrict__ 
   step_block<32>(s);
 }
 
-// out[r] = halt word of registration r; out[n] = the number still running.
-__global__ void __launch_bounds__(kBlock) k_batch_halts(const StepArgs* __restrict__ steps, int n, int* out) {
+// ---------------------------------------------------------------------------
+// The persistent form: `iters` iterations of every running registration in ONE
+// launch.  The items of one iteration (a table of per_iter entries, the same for
+// every iteration) are, in order: the accumulator clears, the 22 constant entries
+// of every registration, the MeanSquares / Mattes pass-1 virtual blocks, the
+// pass-2 virtual blocks, the steps; the launch's queue is that table repeated
+// `iters` times.  Blocks take items in queue order (one atomic counter) and each
+// item waits only for its own registration's earlier items, through monotonic
+// completion counters:
+//   clear / constants of iteration i   after the step of iteration i - 1
+//   MeanSquares / pass 1 of i          after the 23 clear and constant items of i
+//   pass 2 of i                        after every pass-1 block of i
+//   step of i                          after every MeanSquares / pass-2 block of i
+// Every item an item waits for comes earlier in the queue and has therefore been
+// taken by a block that is running, so the launch always completes, whether or not
+// all its blocks are resident.  Waits are bounded (kDepWaitNs of the GPU's global
+// timer); one that runs out records GB_ERR_TIMEOUT and the item is skipped.  A
+// registration's virtual blocks and bodies are those of the per-phase launches,
+// so its results are bitwise the same in both forms.
+enum { kItClear = 0, kItPrepare = 1, kItMsqImage = 2, kItMsqCD = 3, kItP1Image = 4, kItP1CD = 5, kItP2 = 6,
+       kItStep = 7 };
+
+struct RegSync {  // per running registration; zeroed when the tables are built
+  unsigned prep, p1, eval, step;
+};
+
+struct LaunchSync {
+  unsigned next;      // next queue entry of this launch
+  unsigned finished;  // blocks done with this launch
+  unsigned base;      // iterations launched since the tables were built
+  int error;          // GB_ERR_TIMEOUT once a dependency wait ran out
+};
+
+constexpr unsigned long long kDepWaitNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Thread 0 waits until *c >= target (bounded); the whole block then proceeds.
+__device__ __forceinline__ bool block_wait_at_least(const unsigned* c, unsigned target, int* err) {
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    if (ld_acquire(c) < target) {
+      const unsigned long long t0 = global_ns();
+      unsigned polls = 0;
+      while (ld_acquire(c) < target) {
+        __nanosleep(polls < 64 ? 32 : 256);
+        if ((++polls & 255u) == 0 && global_ns() - t0 > kDepWaitNs) {
+          atomicExch(err, GB_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  const bool r = ok != 0;
+  __syncthreads();
+  return r;
+}
+
+// The block is done with its item: its writes, then the counter.
+__device__ __forceinline__ void block_signal(unsigned* c) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(c, 1u);
+  }
+}
+
+// The bodies out of line: each gets its own register allocation, and a call costs
+// once per work item.
+static __device__ __noinline__ void item_msq(const EvalArgs& a, VGrid vg, bool cd) {
+  if (cd) msq_affine_body<kGradCentralDifference>(a, vg);
+  else msq_affine_body<kGradImage>(a, vg);
+}
+static __device__ __noinline__ void item_pass1(const EvalArgs& a, VGrid vg, bool cd) {
+  if (cd) mattes_pass1_affine_body<kGradCentralDifference>(a, vg);
+  else mattes_pass1_affine_body<kGradImage>(a, vg);
+}
+static __device__ __noinline__ void item_pass2(const EvalArgs& a, VGrid vg) { mattes_pass2_affine_body<false>(a, vg); }
+static __device__ __noinline__ void item_step(const StepArgs* steps, int r) {
+  const StepArgs sarg = steps[r];
+  step_block<32>(sarg);  // every thread: its barrier is the block's
+}
+static __device__ __noinline__ void item_prepare(const EvalArgs* regs, int r, int e) {
+  const EvalArgs& a = regs[r];
+  affine_const_entry(e, a.params, a.center, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin,
+                     *const_cast<EvalConsts*>(a.consts));
+}
+
+// meta[r] = (virtual blocks of the MeanSquares pass or of Mattes pass 1, of Mattes pass 2 (0: MeanSquares))
+__global__ void __launch_bounds__(kBlock, 3) k_batch_persistent(const EvalArgs* __restrict__ regs,
+                                                             const StepArgs* __restrict__ steps,
+                                                             const ClearItem* __restrict__ clears,
+                                                             const int4* __restrict__ items,
+                                                             const int2* __restrict__ meta, unsigned per_iter,
+                                                             unsigned iters, LaunchSync* ls, RegSync* rs) {
+  __shared__ EvalArgs sa;
+  __shared__ unsigned s_q, s_base;
+  if (threadIdx.x == 0) s_base = *reinterpret_cast<volatile unsigned*>(&ls->base);
+  __syncthreads();
+  const unsigned base = s_base;
+  const unsigned total = per_iter * iters;
+  for (;;) {
+    if (threadIdx.x == 0) s_q = atomicAdd(&ls->next, 1u);
+    __syncthreads();
+    const unsigned q = s_q;
+    __syncthreads();
+    if (q >= total) break;
+    const unsigned it = base + q / per_iter;  // iteration since the tables were built
+    const int4 w = __ldg(items + q % per_iter);
+    const int r = w.y;
+    RegSync* R = rs + r;
+    const int2 nv = __ldg(meta + r);
+    switch (w.x) {
+      case kItClear:
+      case kItPrepare: {
+        const bool ok = block_wait_at_least(&R->step, it, &ls->error);
+        const ClearItem ci = clears[r];
+        if (ok && !__ldcg(ci.halt)) {
+          if (w.x == kItClear) {
+            for (long long k = threadIdx.x; k < ci.words; k += blockDim.x) ci.p[k] = 0ull;
+          } else if (threadIdx.x == 0) {
+            item_prepare(regs, r, w.z);
+          }
+        }
+        block_signal(&R->prep);
+        break;
+      }
+      case kItMsqImage:
+      case kItMsqCD:
+      case kItP1Image:
+      case kItP1CD: {
+        const bool ok = block_wait_at_least(&R->prep, (1u + kConstEntries) * (it + 1u), &ls->error);
+        if (ok) {
+          load_reg(regs, r, sa);
+          const VGrid vg{w.z, w.w};
+          if (w.x <= kItMsqCD) item_msq(sa, vg, w.x == kItMsqCD);
+          else item_pass1(sa, vg, w.x == kItP1CD);
+        }
+        block_signal(w.x <= kItMsqCD ? &R->eval : &R->p1);
+        break;
+      }
+      case kItP2: {
+        const bool ok = block_wait_at_least(&R->p1, (unsigned)nv.x * (it + 1u), &ls->error);
+        if (ok) {
+          load_reg(regs, r, sa);
+          item_pass2(sa, VGrid{w.z, w.w});
+        }
+        block_signal(&R->eval);
+        break;
+      }
+      default: {  // kItStep
+        const unsigned want = (unsigned)(nv.y > 0 ? nv.y : nv.x) * (it + 1u);
+        const bool ok = block_wait_at_least(&R->eval, want, &ls->error);
+        if (ok) item_step(steps, r);
+        block_signal(&R->step);
+        break;
+      }
+    }
+  }
+  // the last block to finish readies the counters for the next launch
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ls->finished, 1u) == gridDim.x - 1) {
+      ls->next = 0u;
+      ls->finished = 0u;
+      ls->base = base + iters;
+      __threadfence();
+    }
+  }
+}
+
+// out[r] = halt word of registration r; out[n] = the number still running;
+// out[n + 1] = the persistent launches' error word (0 without them).
+__global__ void __launch_bounds__(kBlock) k_batch_halts(const StepArgs* __restrict__ steps, int n, int* out,
+                                                        const LaunchSync* ls) {
   griddep_wait();
   __shared__ int running;
   if (threadIdx.x == 0) running = 0;
@@ -120,7 +308,10 @@ __global__ void __launch_bounds__(kBlock) k_batch_halts(const StepArgs* __restri
     if (!h) atomicAdd(&running, 1);
   }
   __syncthreads();
-  if (threadIdx.x == 0) out[n] = running;
+  if (threadIdx.x == 0) {
+    out[n] = running;
+    out[n + 1] = ls ? __ldcg(&ls->error) : 0;
+  }
 }
 
 static int cuda_fail(cudaError_t e, const char* where) {
@@ -165,6 +356,7 @@ struct gb_batch {
   cudaStream_t stream = nullptr;
   int64_t spb[3] = {8192, 8192, 8192};  // samples per virtual block: MeanSquares, Mattes pass 1, Mattes pass 2
   bool use_graph = true;
+  bool persistent = false;  // k_batch_persistent: several iterations per launch
   std::vector<Reg> regs;
   // tables of the running registrations
   std::vector<int> active;
@@ -173,7 +365,16 @@ struct gb_batch {
   DevBuf<ClearItem> d_clear;
   DevBuf<int4> d_work;
   DevBuf<int> d_halts;
-  int* h_halts = nullptr;  // pinned, 2 slots of (capacity + 1)
+  int* h_halts = nullptr;  // pinned, 2 slots of (capacity + 2)
+  // the persistent form's tables: one iteration's items, per-registration pass sizes,
+  // completion counters, the launch counters
+  DevBuf<int4> d_items;
+  DevBuf<int2> d_meta;
+  DevBuf<RegSync> d_rs;
+  DevBuf<LaunchSync> d_ls;
+  unsigned per_iter = 0;
+  int pgrid = 0;
+  size_t psmem = 0;
   size_t h_halts_cap = 0;
   int64_t goff[kGroups] = {}, gcnt[kGroups] = {};
   std::vector<int64_t> reg_work;  // work items of each running registration (all passes)
@@ -224,6 +425,26 @@ int enqueue_iteration(gb_batch* b, bool step) {
     GB_B_CUDA(launch_dep(st, k_batch_pass2, (unsigned)b->gcnt[kGrpP2], kBlock, b->smem2, regs, w + b->goff[kGrpP2]));
   if (step) GB_B_CUDA(launch_dep(st, k_batch_step, n, 32, 0, (const StepArgs*)b->d_step.p));
   return GB_OK;
+}
+
+// Kernel arguments of one persistent launch of `iters` iterations.
+struct PersistentArgs {
+  const EvalArgs* regs;
+  const StepArgs* steps;
+  const ClearItem* clears;
+  const int4* items;
+  const int2* meta;
+  unsigned per_iter, iters;
+  LaunchSync* ls;
+  RegSync* rs;
+  std::vector<void*> data() {
+    return {&regs, &steps, &clears, &items, &meta, &per_iter, &iters, &ls, &rs};
+  }
+};
+
+PersistentArgs persistent_args_of(gb_batch* b, unsigned iters) {
+  return PersistentArgs{b->d_eval.p, b->d_step.p, b->d_clear.p, b->d_items.p, b->d_meta.p, b->per_iter, iters,
+                        b->d_ls.p, b->d_rs.p};
 }
 
 // Tables of the registrations still running, uploaded; the iteration graph re-captured.
@@ -284,6 +505,32 @@ int rebuild_tables(gb_batch* b) {
     b->gcnt[g] = (int64_t)work[g].size();
     all.insert(all.end(), work[g].begin(), work[g].end());
   }
+  // the persistent form's items of one iteration: clears, constants, the first passes
+  // (largest registrations first, so the longest chains start earliest), pass 2, steps
+  std::vector<int> order(n);
+  for (size_t k = 0; k < n; ++k) order[k] = (int)k;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return b->regs[(size_t)b->active[(size_t)x]].m->nsamples > b->regs[(size_t)b->active[(size_t)y]].m->nsamples;
+  });
+  std::vector<int4> items;
+  std::vector<int2> meta(n, make_int2(0, 0));
+  for (size_t k = 0; k < n; ++k) items.push_back(make_int4(kItClear, (int)k, 0, 0));
+  for (size_t k = 0; k < n; ++k)
+    for (int e = 0; e < kConstEntries; ++e) items.push_back(make_int4(kItPrepare, (int)k, e, 0));
+  for (int k : order) {
+    gb_metric* m = b->regs[(size_t)b->active[(size_t)k]].m;
+    const bool cd = m->grad_source == GB_GRADIENT_CENTRAL_DIFFERENCE;
+    const bool msq = m->kind == GB_METRIC_MEAN_SQUARES;
+    const int64_t nv = vblocks(m->nsamples, b->spb[msq ? kSpbMsq : kSpbPass1]);
+    const int kind = msq ? (cd ? kItMsqCD : kItMsqImage) : (cd ? kItP1CD : kItP1Image);
+    for (int64_t v = 0; v < nv; ++v) items.push_back(make_int4(kind, k, (int)v, (int)nv));
+    meta[(size_t)k].x = (int)nv;
+    if (!msq) meta[(size_t)k].y = (int)vblocks(m->nsamples, b->spb[kSpbPass2]);
+  }
+  for (int k : order)
+    for (int v = 0; v < meta[(size_t)k].y; ++v) items.push_back(make_int4(kItP2, k, v, meta[(size_t)k].y));
+  for (size_t k = 0; k < n; ++k) items.push_back(make_int4(kItStep, (int)k, 0, 0));
+  b->per_iter = (unsigned)items.size();
   b->smem1 = sizeof(unsigned long long) * (size_t)(maxbins * maxbins + maxbins) + sizeof(unsigned) * (size_t)maxbins;
   b->smem2 = mattes_pass2_smem(maxbins);
   if (maxbins > 0) {
@@ -298,12 +545,23 @@ int rebuild_tables(gb_batch* b) {
   GB_B_CUDA(b->d_step.alloc_on(b->stream, n));
   GB_B_CUDA(b->d_clear.alloc_on(b->stream, n));
   GB_B_CUDA(b->d_work.alloc_on(b->stream, std::max<size_t>(all.size(), 1)));
-  GB_B_CUDA(b->d_halts.alloc_on(b->stream, n + 1));
-  if (b->h_halts_cap < n + 1) {
+  GB_B_CUDA(b->d_halts.alloc_on(b->stream, n + 2));
+  if (b->h_halts_cap < n + 2) {
     if (b->h_halts) cudaFreeHost(b->h_halts);
     b->h_halts = nullptr;
-    GB_B_CUDA(cudaMallocHost(&b->h_halts, 2 * sizeof(int) * (n + 1)));
-    b->h_halts_cap = n + 1;
+    GB_B_CUDA(cudaMallocHost(&b->h_halts, 2 * sizeof(int) * (n + 2)));
+    b->h_halts_cap = n + 2;
+  }
+  GB_B_CUDA(b->d_items.alloc_on(b->stream, items.size()));
+  GB_B_CUDA(b->d_meta.alloc_on(b->stream, n));
+  GB_B_CUDA(b->d_rs.alloc_on(b->stream, n));
+  GB_B_CUDA(b->d_ls.alloc_on(b->stream, 1));
+  if (b->persistent) {
+    b->psmem = std::max(b->smem1, b->smem2);
+    GB_B_CUDA(cudaFuncSetAttribute(k_batch_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->psmem));
+    int per_sm = 0;
+    GB_B_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persistent, kBlock, b->psmem));
+    b->pgrid = std::max(1, per_sm) * b->ctx->sm_count;
   }
   cudaStream_t st = b->stream;
   GB_B_CUDA(cudaMemcpyAsync(b->d_eval.p, ev.data(), sizeof(EvalArgs) * n, cudaMemcpyHostToDevice, st));
@@ -311,8 +569,12 @@ int rebuild_tables(gb_batch* b) {
   GB_B_CUDA(cudaMemcpyAsync(b->d_clear.p, ci.data(), sizeof(ClearItem) * n, cudaMemcpyHostToDevice, st));
   if (!all.empty())
     GB_B_CUDA(cudaMemcpyAsync(b->d_work.p, all.data(), sizeof(int4) * all.size(), cudaMemcpyHostToDevice, st));
+  GB_B_CUDA(cudaMemcpyAsync(b->d_items.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, st));
+  GB_B_CUDA(cudaMemcpyAsync(b->d_meta.p, meta.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st));
+  GB_B_CUDA(cudaMemsetAsync(b->d_rs.p, 0, sizeof(RegSync) * n, st));
+  GB_B_CUDA(cudaMemsetAsync(b->d_ls.p, 0, sizeof(LaunchSync), st));
   GB_B_CUDA(cudaStreamSynchronize(st));  // the host tables are pageable
-  if (b->use_graph) {
+  if (b->use_graph && !b->persistent) {
     bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess;
     if (ok) {
       const int rc = enqueue_iteration(b, true);
@@ -358,6 +620,10 @@ extern "C" int gb_batch_destroy(gb_batch* b) {
   b->d_clear.reset();
   b->d_work.reset();
   b->d_halts.reset();
+  b->d_items.reset();
+  b->d_meta.reset();
+  b->d_rs.reset();
+  b->d_ls.reset();
   cudaStreamSynchronize(b->stream);
   for (cudaEvent_t e : b->ev)
     if (e) cudaEventDestroy(e);
@@ -370,6 +636,13 @@ extern "C" int gb_batch_destroy(gb_batch* b) {
 extern "C" int gb_batch_set_graphs(gb_batch* b, int on) {
   if (!b) return fail(GB_ERR_BAD_ARG, "null batch");
   b->use_graph = on != 0;
+  b->dirty = true;
+  return GB_OK;
+}
+
+extern "C" int gb_batch_set_persistent(gb_batch* b, int on) {
+  if (!b) return fail(GB_ERR_BAD_ARG, "null batch");
+  b->persistent = on != 0;
   b->dirty = true;
   return GB_OK;
 }
@@ -426,8 +699,9 @@ static int collect_halted(gb_batch* b, bool& any) {
   any = false;
   if (n == 0) return GB_OK;
   GB_B_CUDA(cudaStreamSynchronize(st));
-  GB_B_CUDA(launch_dep(st, k_batch_halts, 1u, kBlock, 0, (const StepArgs*)b->d_step.p, n, b->d_halts.p));
-  GB_B_CUDA(cudaMemcpyAsync(b->h_halts, b->d_halts.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st));
+  GB_B_CUDA(launch_dep(st, k_batch_halts, 1u, kBlock, 0, (const StepArgs*)b->d_step.p, n, b->d_halts.p,
+                       (const LaunchSync*)b->d_ls.p));
+  GB_B_CUDA(cudaMemcpyAsync(b->h_halts, b->d_halts.p, sizeof(int) * (n + 2), cudaMemcpyDeviceToHost, st));
   GB_B_CUDA(cudaStreamSynchronize(st));
   std::vector<int> idx;
   for (int k = 0; k < n; ++k)
@@ -468,24 +742,35 @@ extern "C" int gb_batch_run(gb_batch* b, int64_t max_iterations, int64_t* runnin
     bool pending = false, shrink = false;
     while (max_iterations <= 0 || done < max_iterations) {
       const int64_t k = max_iterations <= 0 ? batch : std::min(batch, max_iterations - done);
-      for (int64_t i = 0; i < k; ++i) {
-        if (b->exec) {
-          GB_B_CUDA(cudaGraphLaunch(b->exec, st));
-        } else {
-          const int rc = enqueue_iteration(b, true);
-          if (rc) return rc;
+      if (b->persistent) {
+        // one launch for all k iterations (plain launch: the next must not start early)
+        PersistentArgs pa = persistent_args_of(b, (unsigned)k);
+        std::vector<void*> av = pa.data();
+        GB_B_CUDA(cudaLaunchKernel((const void*)k_batch_persistent, dim3((unsigned)b->pgrid), dim3(kBlock),
+                                   av.data(), b->psmem, st));
+      } else {
+        for (int64_t i = 0; i < k; ++i) {
+          if (b->exec) {
+            GB_B_CUDA(cudaGraphLaunch(b->exec, st));
+          } else {
+            const int rc = enqueue_iteration(b, true);
+            if (rc) return rc;
+          }
         }
       }
       done += k;
       b->iterations += k;
       batch = std::min<int64_t>(batch * 2, 16);
-      int* hh = b->h_halts + slot * (n + 1);
-      GB_B_CUDA(launch_dep(st, k_batch_halts, 1u, kBlock, 0, (const StepArgs*)b->d_step.p, n, b->d_halts.p));
-      GB_B_CUDA(cudaMemcpyAsync(hh, b->d_halts.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st));
+      int* hh = b->h_halts + slot * (n + 2);
+      GB_B_CUDA(launch_dep(st, k_batch_halts, 1u, kBlock, 0, (const StepArgs*)b->d_step.p, n, b->d_halts.p,
+                           (const LaunchSync*)b->d_ls.p));
+      GB_B_CUDA(cudaMemcpyAsync(hh, b->d_halts.p, sizeof(int) * (n + 2), cudaMemcpyDeviceToHost, st));
       GB_B_CUDA(cudaEventRecord(b->ev[slot], st));
       if (pending) {
         GB_B_CUDA(cudaEventSynchronize(b->ev[slot ^ 1]));
-        const int* ph = b->h_halts + (slot ^ 1) * (n + 1);
+        const int* ph = b->h_halts + (slot ^ 1) * (n + 2);
+        if (ph[n + 1] != 0)
+          return fail(GB_ERR_TIMEOUT, "batched iteration: a dependency wait ran out in the persistent kernel");
         if (ph[n] == 0) {  // all stopped
           shrink = true;
           break;

@@ -213,10 +213,12 @@ __global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
 
 #endif  // GB_KERNELS_HELPERS_ONLY
 
+// The constants through L2 (not the read-only path): the batched engine's
+// persistent kernel rewrites them between iterations within one launch.
 __device__ __forceinline__ void load_consts(const EvalConsts* g, EvalConsts& s) {
   const float* src = reinterpret_cast<const float*>(g);
   float* dst = reinterpret_cast<float*>(&s);
-  for (int k = threadIdx.x; k < (int)(sizeof(EvalConsts) / 4); k += blockDim.x) dst[k] = __ldg(src + k);
+  for (int k = threadIdx.x; k < (int)(sizeof(EvalConsts) / 4); k += blockDim.x) dst[k] = __ldcg(src + k);
 }
 
 // ---------------------------------------------------------------------------

@@ -196,14 +196,22 @@ __device__ __forceinline__ void step_apply(const StepArgs& s, const OptState* S,
 // One registration's whole step in one block of NT threads: the compensated sums,
 // the decisions, the update, then the NumberOfIterations stop that the reference
 // checks at the top of its next loop pass (itkGradientDescentOptimizerv4.hxx:82-89).
+// Called by every thread of the block; threads from NT on take part only in its
+// barrier (the batched engine's persistent kernel runs the step in larger blocks).
 template <int NT>
 __device__ __forceinline__ void step_block(const StepArgs& s) {
   OptState* S = s.st;
-  if (__ldcg(&S->halt)) return;
+  // thread 0 reads the halt word for the block: thread 0 itself may set it below,
+  // and every thread must take the same branch (the block's barrier follows)
+  __shared__ int halted_s;
+  if (threadIdx.x == 0) halted_s = __ldcg(&S->halt);
+  __syncthreads();
+  if (halted_s) return;
   const int status = __ldcg(s.status);
   const bool err = metric_error(s, status);
+  const bool mine = (int)threadIdx.x < NT;
   DD q = {0.0, 0.0}, r = {0.0, 0.0};
-  if (!err)
+  if (!err && mine)
     for (long long j = threadIdx.x; j < s.P; j += NT) {
       double qq, rr;
       step_terms(s, j, qq, rr);
@@ -225,7 +233,7 @@ __device__ __forceinline__ void step_block(const StepArgs& s) {
     fin_max = fm;
   }
   __syncthreads();
-  for (long long j = threadIdx.x; j < s.P; j += NT) {
+  for (long long j = threadIdx.x; mine && j < s.P; j += NT) {
     step_apply(s, S, act, j);
     if (fin_max && s.return_best) s.params[j] = __ldcg(s.best + j);
   }

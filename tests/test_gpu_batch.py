@@ -66,10 +66,11 @@ def result(U, o):
     return U.GetParameters().copy(), o.GetValue(), o.GetCurrentIteration(), o.GetStopCondition()
 
 
-def run_batch(pairs, idx, spb=(4096, 4096, 4096), graphs=True, chunk=0, **kw):
+def run_batch(pairs, idx, spb=(4096, 4096, 4096), graphs=True, chunk=0, persistent=True, **kw):
     b = RegistrationBatch()
     b.SetSamplesPerBlock(*spb)
     b.SetUseCudaGraphs(graphs)
+    b.SetPersistent(persistent)
     regs = [make(pairs, i, *SPECS[i], **kw) for i in idx]
     for U, o in regs:
         b.Add(o)
@@ -100,6 +101,20 @@ def test_graphs_direct_and_split_runs_agree(pairs):
     for x, y, z in zip(a, b, c):
         same(x, y)
         same(x, z)
+
+
+def test_persistent_and_per_phase_forms_agree(pairs):
+    """The persistent kernel (several iterations per launch, items ordered by
+    dependency) and the per-phase launches (graph and direct) give the same bits, for
+    the whole mix and with runs split into chunks of iterations."""
+    a = run_batch(pairs, range(6), persistent=True)
+    b = run_batch(pairs, range(6), persistent=False)
+    c = run_batch(pairs, range(6), persistent=False, graphs=False)
+    d = run_batch(pairs, range(6), persistent=True, chunk=5)
+    for w, x, y, z in zip(a, b, c, d):
+        same(w, x)
+        same(w, y)
+        same(w, z)
 
 
 @pytest.mark.parametrize("i", range(6))
