@@ -874,57 +874,114 @@ def run_served_form(args, inst):
     res, wall = srv.serve(reqs, list(arrivals))
     lat = np.array([r.latency for r in res])
     same = all(np.array_equal(a.parameters, b.parameters) for a, b in zip(res, res0))
-    # plain per-call path: the same requests first come first served (service times measured)
+    # the plain per-call path serving the same requests: W host worker threads (1, and
+    # as many as the server's set-up threads) each take the next arrived request first
+    # come first served and run it through the public per-call API (level set-up, then
+    # one GetValueAndDerivative call per iteration with RegularStep on the host).
     from itk_gb300 import MattesMutualInformationImageToImageMetricv4, MeanSquaresImageToImageMetricv4
     from itk_gb300.registration import setup_level
-    service_runs = [[] for _ in reqs]
-    for _ in range(REPEATS):
-        for i, r in enumerate(reqs):
-            t0 = time.perf_counter()
-            if r.metric == "msq":
-                m = MeanSquaresImageToImageMetricv4()
-            else:
-                m = MattesMutualInformationImageToImageMetricv4()
-                m.SetNumberOfHistogramBins(r.bins)
-            m.SetFixedImage(r.fixed)
-            m.SetMovingImage(r.moving)
-            T = identity_at_center(r.fixed)
-            m.SetMovingTransform(T)
-            seed = r.seed
-            for lv in range(r.levels):
-                _, seed = setup_level(m, r.fixed, (r.shrink_factors[lv],) * 3, r.smoothing_sigmas[lv], True,
-                                      r.sampling, r.sampling_percentage, seed)
-                plain_loop(m, T, r.iterations[lv], r.learning_rate, r.minimum_step_length, scales=r.scales)
-            service_runs[i].append(time.perf_counter() - t0)
-    service = [float(np.median(v)) for v in service_runs]
-    # the Mattes MI requests alone: capacity of the server against the plain path
+
+    def plain_request(r):
+        if r.metric == "msq":
+            m = MeanSquaresImageToImageMetricv4()
+        else:
+            m = MattesMutualInformationImageToImageMetricv4()
+            m.SetNumberOfHistogramBins(r.bins)
+        m.SetFixedImage(r.fixed)
+        m.SetMovingImage(r.moving)
+        T = identity_at_center(r.fixed)
+        m.SetMovingTransform(T)
+        seed = r.seed
+        for lv in range(r.levels):
+            _, seed = setup_level(m, r.fixed, (r.shrink_factors[lv],) * 3, r.smoothing_sigmas[lv], True,
+                                  r.sampling, r.sampling_percentage, seed)
+            plain_loop(m, T, r.iterations[lv], r.learning_rate, r.minimum_step_length, scales=r.scales)
+        return T.GetParameters()
+
+    def plain_serve(sel, arr, workers):
+        """Serves requests sel arriving at times arr (seconds from the start) on `workers`
+        threads; returns (latencies, wall seconds from the first arrival to the last completion)."""
+        import threading
+        order = sorted(range(len(sel)), key=lambda k: arr[k])
+        lock = threading.Lock()
+        nxt = [0]
+        lat = [0.0] * len(sel)
+        t0 = time.perf_counter()
+
+        def work():
+            while True:
+                with lock:
+                    if nxt[0] >= len(order):
+                        return
+                    k = order[nxt[0]]
+                    nxt[0] += 1
+                wait = arr[k] - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(wait)
+                plain_request(reqs[sel[k]])
+                lat[k] = time.perf_counter() - t0 - arr[k]
+
+        ths = [threading.Thread(target=work) for _ in range(workers)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        return np.array(lat), time.perf_counter() - t0
+
+    everyone = list(range(len(reqs)))
     mi = [i for i, r in enumerate(reqs) if r.metric == "mattes"]
+    plain = {}
+    for wk in (1, 4):
+        caps = [len(reqs) / plain_serve(everyone, [0.0] * len(reqs), wk)[1] for _ in range(REPEATS)]
+        caps_mi = [len(mi) / plain_serve(mi, [0.0] * len(mi), wk)[1] for _ in range(REPEATS)]
+        lat_p, wall_p = plain_serve(everyone, list(arrivals), wk)
+        plain[wk] = dict(capacity=caps, capacity_mi=caps_mi, lat=lat_p, wall=wall_p)
+    # the Mattes MI requests alone: capacity of the server against the plain path
     walls_mi = []
     for _ in range(REPEATS):
         srv_mi = RegistrationServer(hbm_budget_bytes=120e9)
         walls_mi.append(srv_mi.serve([reqs[i] for i in mi], [0.0] * len(mi))[1])
-    wall_mi = float(np.median(walls_mi))
-    cap_mi = {"served": len(mi) / wall_mi, "plain_per_call": len(mi) / float(sum(service[i] for i in mi))}
-    done, plain_lat = 0.0, []
-    for a, s in zip(arrivals, service):
-        start = max(a, done)
-        done = start + s
-        plain_lat.append(done - a)
-    plain_lat = np.array(plain_lat)
+    served_caps = [len(reqs) / w for _, w in runs]
+    served_caps_mi = [len(mi) / w for w in walls_mi]
+
+    def med(v):
+        return float(np.median(v))
+
+    def spread(v):
+        return [float(np.min(v)), float(np.max(v))]
+
+    p1, p4 = plain[1], plain[4]
     return {
         "requests": len(reqs),
         "workload": "64 requests, sizes log-uniform 48^3..256x256x200, half MeanSquares dense / half Mattes 50 bins "
                     "20% RANDOM, 1-3 levels (shrink 4/2/1, sigma 2/1/0), 50-200 iterations per level",
-        "arrivals": f"Poisson, {rate:.2f} req/s = 80% of the measured capacity {capacity:.2f} req/s",
-        "repeats": f"capacities and plain service times: medians of {REPEATS} runs (shared host cores)",
+        "arrivals": f"Poisson, {rate:.2f} req/s = 80% of the server's measured capacity {capacity:.2f} req/s; "
+                    "the same arrivals served by the server and by the plain per-call path",
+        "plain_per_call_path": "host worker threads (1, and 4 = the server's set-up threads) taking the next arrived "
+                               "request first come first served; each request set up level by level and optimized "
+                               "with one GetValueAndDerivative call per iteration (RegularStep on the host); latencies "
+                               "measured",
+        "repeats": f"capacities: medians of {REPEATS} runs with [min, max] (shared host cores)",
         "hbm_budget_gb": 120, "peak_admitted_gb": srv.peak_bytes / 1e9,
-        "regs_per_s": {"served": len(reqs) / wall, "plain_per_call": len(reqs) / max(done, sum(service))},
+        "regs_per_s": {"served": len(reqs) / wall, "plain_per_call": len(reqs) / p1["wall"],
+                       "plain_per_call_4_threads": len(reqs) / p4["wall"]},
         "latency_s": {"served_p50": float(np.percentile(lat, 50)), "served_p99": float(np.percentile(lat, 99)),
-                      "plain_p50": float(np.percentile(plain_lat, 50)),
-                      "plain_p99": float(np.percentile(plain_lat, 99))},
-        "capacity_regs_per_s": {"served": capacity, "plain_per_call": len(reqs) / float(sum(service))},
-        "capacity_mattes_only_regs_per_s": cap_mi,
-        "speedup_capacity_mattes_only": cap_mi["served"] / cap_mi["plain_per_call"],
+                      "plain_p50": float(np.percentile(p1["lat"], 50)),
+                      "plain_p99": float(np.percentile(p1["lat"], 99)),
+                      "plain_4_threads_p50": float(np.percentile(p4["lat"], 50)),
+                      "plain_4_threads_p99": float(np.percentile(p4["lat"], 99))},
+        "capacity_regs_per_s": {"served": med(served_caps), "served_range": spread(served_caps),
+                                "plain_per_call": med(p1["capacity"]), "plain_per_call_range": spread(p1["capacity"]),
+                                "plain_per_call_4_threads": med(p4["capacity"]),
+                                "plain_per_call_4_threads_range": spread(p4["capacity"])},
+        "capacity_mattes_only_regs_per_s": {"served": med(served_caps_mi), "served_range": spread(served_caps_mi),
+                                            "plain_per_call": med(p1["capacity_mi"]),
+                                            "plain_per_call_range": spread(p1["capacity_mi"]),
+                                            "plain_per_call_4_threads": med(p4["capacity_mi"]),
+                                            "plain_per_call_4_threads_range": spread(p4["capacity_mi"])},
+        "speedup_capacity_mattes_only": med(served_caps_mi) / med(p1["capacity_mi"]),
+        "speedup_capacity_mattes_only_vs_4_threads": med(served_caps_mi) / med(p4["capacity_mi"]),
+        "speedup_capacity_all": med(served_caps) / med(p1["capacity"]),
         "server_time_s": {"wall": wall, "batch_iterations": srv.run_seconds, "ticks": srv.ticks,
                           "level_setups_on_threads": srv.setup_seconds,
                           "of_which_metric_and_upload": srv.upload_seconds},

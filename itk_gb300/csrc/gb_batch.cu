@@ -721,6 +721,7 @@ static int collect_halted(gb_batch* b, bool& any) {
 }
 
 extern "C" int gb_batch_run(gb_batch* b, int64_t max_iterations, int64_t* running) {
+  NvtxRange range(__func__);
   if (!b) return fail(GB_ERR_BAD_ARG, "null batch");
   GB_B_CUDA(cudaSetDevice(b->ctx->device));
   cudaStream_t st = b->stream;

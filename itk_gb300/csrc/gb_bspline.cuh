@@ -241,7 +241,8 @@ __global__ void __launch_bounds__(kBlock, SMEM ? 4 : 3) k_mattes_pass1_bspline(E
     hist_add_aggregated(ok, fidx * B + pdfm, fidx, q, hist, fm);
     nv += ok ? 1u : 0u;
   }
-  mattes_pass1_epilogue(a, nv, hist, cs, fm);
+  // the derivative's table is formed by k_mattes_table, not by the last block
+  mattes_pass1_epilogue(a, nv, hist, cs, fm, hw_grid(), false);
 }
 
 // One block per chunk of same-cell samples (at most kChunkLen = blockDim).
@@ -253,78 +254,78 @@ __global__ void __launch_bounds__(kBlock, SMEM ? 4 : 3) k_mattes_pass1_bspline(E
 // load of the x weights, 12 FMAs.  The 16 slice sums of each output are then
 // added in slice order.
 constexpr int kChunkSlices = 16;
+// Grid-stride over the chunks (one full wave of blocks): block b forms chunks b, b + G, ...
 template <bool MATTES>
 __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
   __shared__ __align__(16) float W1[kChunkLen][12];
   __shared__ float4 AV[kChunkLen];
   __shared__ float qs[kChunkSlices][192];
-  griddep_wait();  // several waves of blocks: dependents are released at each block's end
+  griddep_wait();
   if (halted(a)) return;
-  if (MATTES) mattes_value_groups(a);  // the value's group partials (the grid has at least one block per group)
-  if ((int)blockIdx.x >= a.nchunks) {
-    griddep_launch_dependents();
-    return;
-  }
-  const int4 ch = a.chunks[blockIdx.x];
-  const int len = ch.y - ch.x;
+  if (MATTES) mattes_value_groups(a);  // the value's group partials (blocks b, b + G, ...)
   const int B = a.bins;
   const int t = threadIdx.x;
-  if (t < len) {
-    const int64_t i = (int64_t)ch.x + t;
-    const float4 su = __ldg(a.sup + i);
-    const float4 c = __ldcg(a.cache + i);
-    float4 av = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (MATTES) {
-      const int fbin = __float_as_int(__ldg(&a.samples[i].w));
-      if (c.x == c.x) {
-        int pdfm;
-        float tt, d[4];
-        parzen_window(c.x, B, pdfm, tt);
-        parzen_deriv(tt, d);
-        const float* row = a.pratio + fbin * B + pdfm;
-        const float w = __ldcg(row) * d[0] + __ldcg(row + 1) * d[1] + __ldcg(row + 2) * d[2] + __ldcg(row + 3) * d[3];
-        av = make_float4(w * c.y, w * c.z, w * c.w, 0.f);
+  for (int cidx = blockIdx.x; cidx < a.nchunks; cidx += gridDim.x) {
+    const int4 ch = a.chunks[cidx];
+    const int len = ch.y - ch.x;
+    if (t < len) {
+      const int64_t i = (int64_t)ch.x + t;
+      const float4 su = __ldg(a.sup + i);
+      const float4 c = __ldcg(a.cache + i);
+      float4 av = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (MATTES) {
+        const int fbin = __float_as_int(__ldg(&a.samples[i].w));
+        if (c.x == c.x) {
+          int pdfm;
+          float tt, d[4];
+          parzen_window(c.x, B, pdfm, tt);
+          parzen_deriv(tt, d);
+          const float* row = a.pratio + fbin * B + pdfm;
+          const float w = __ldcg(row) * d[0] + __ldcg(row + 1) * d[1] + __ldcg(row + 2) * d[2] + __ldcg(row + 3) * d[3];
+          av = make_float4(w * c.y, w * c.z, w * c.w, 0.f);
+        }
+      } else {
+        av = make_float4(c.x, c.y, c.z, 0.f);
       }
-    } else {
-      av = make_float4(c.x, c.y, c.z, 0.f);
+      bspline_basis(su.x, &W1[t][0]);
+      bspline_basis(su.y, &W1[t][4]);
+      bspline_basis(su.z, &W1[t][8]);
+      AV[t] = av;
     }
-    bspline_basis(su.x, &W1[t][0]);
-    bspline_basis(su.y, &W1[t][4]);
-    bspline_basis(su.z, &W1[t][8]);
-    AV[t] = av;
-  }
-  __syncthreads();
-  const int ky = t & 3, kz = (t >> 2) & 3, sl = t >> 4;
-  constexpr int kSlice = kChunkLen / kChunkSlices;
-  const int j0 = sl * kSlice, j1 = min(len, j0 + kSlice);
-  float acc[4][3];
+    __syncthreads();
+    const int ky = t & 3, kz = (t >> 2) & 3, sl = t >> 4;
+    constexpr int kSlice = kChunkLen / kChunkSlices;
+    const int j0 = sl * kSlice, j1 = min(len, j0 + kSlice);
+    float acc[4][3];
 #pragma unroll
-  for (int kx = 0; kx < 4; ++kx) acc[kx][0] = acc[kx][1] = acc[kx][2] = 0.f;
-  for (int j = j0; j < j1; ++j) {
-    const float4 wx = *reinterpret_cast<const float4*>(&W1[j][0]);
-    const float wyz = W1[j][4 + ky] * W1[j][8 + kz];
-    const float4 v = AV[j];
-    const float w[4] = {wx.x * wyz, wx.y * wyz, wx.z * wyz, wx.w * wyz};
+    for (int kx = 0; kx < 4; ++kx) acc[kx][0] = acc[kx][1] = acc[kx][2] = 0.f;
+    for (int j = j0; j < j1; ++j) {
+      const float4 wx = *reinterpret_cast<const float4*>(&W1[j][0]);
+      const float wyz = W1[j][4 + ky] * W1[j][8 + kz];
+      const float4 v = AV[j];
+      const float w[4] = {wx.x * wyz, wx.y * wyz, wx.z * wyz, wx.w * wyz};
+#pragma unroll
+      for (int kx = 0; kx < 4; ++kx) {
+        acc[kx][0] = fmaf(w[kx], v.x, acc[kx][0]);
+        acc[kx][1] = fmaf(w[kx], v.y, acc[kx][1]);
+        acc[kx][2] = fmaf(w[kx], v.z, acc[kx][2]);
+      }
+    }
+    const int k0 = 4 * ky + 16 * kz;
 #pragma unroll
     for (int kx = 0; kx < 4; ++kx) {
-      acc[kx][0] = fmaf(w[kx], v.x, acc[kx][0]);
-      acc[kx][1] = fmaf(w[kx], v.y, acc[kx][1]);
-      acc[kx][2] = fmaf(w[kx], v.z, acc[kx][2]);
+      qs[sl][k0 + kx] = acc[kx][0];
+      qs[sl][64 + k0 + kx] = acc[kx][1];
+      qs[sl][128 + k0 + kx] = acc[kx][2];
     }
-  }
-  const int k0 = 4 * ky + 16 * kz;
+    __syncthreads();
+    if (t < 192) {
+      float s = qs[0][t];
 #pragma unroll
-  for (int kx = 0; kx < 4; ++kx) {
-    qs[sl][k0 + kx] = acc[kx][0];
-    qs[sl][64 + k0 + kx] = acc[kx][1];
-    qs[sl][128 + k0 + kx] = acc[kx][2];
-  }
-  __syncthreads();
-  if (t < 192) {
-    float s = qs[0][t];
-#pragma unroll
-    for (int q = 1; q < kChunkSlices; ++q) s = __fadd_rn(s, qs[q][t]);
-    a.chunk_part[(size_t)blockIdx.x * 192 + t] = s;
+      for (int q = 1; q < kChunkSlices; ++q) s = __fadd_rn(s, qs[q][t]);
+      a.chunk_part[(size_t)cidx * 192 + t] = s;
+    }
+    __syncthreads();  // the next chunk overwrites W1, AV and qs
   }
   griddep_launch_dependents();
 }

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cstdint>
@@ -83,14 +84,25 @@ cudaError_t sort_pairs_u64(const uint64_t* keys_in, uint64_t* keys_out, const ui
 
 // Per-thread last-error text (gb_last_error()).  While an entry point that takes a
 // metric handle runs, an ErrorScope names that handle, and fail() records the text
-// on the handle as well (gb_metric_last_error).
+// on the handle as well (gb_metric_last_error).  The scope is also an NVTX range
+// named after the entry point, so a timeline (Nsight Systems, ncu's NVTX filters)
+// shows every C-ABI call; without an attached tool a range costs a few nanoseconds.
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
 gb_metric* error_scope();
 void set_error_scope(gb_metric* m);
+
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 struct ErrorScope {
   gb_metric* prev;
-  explicit ErrorScope(gb_metric* m) : prev(error_scope()) { set_error_scope(m); }
+  NvtxRange range;
+  ErrorScope(gb_metric* m, const char* name) : prev(error_scope()), range(name) { set_error_scope(m); }
   ~ErrorScope() { set_error_scope(prev); }
   ErrorScope(const ErrorScope&) = delete;
   ErrorScope& operator=(const ErrorScope&) = delete;

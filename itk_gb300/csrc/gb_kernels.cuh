@@ -1013,6 +1013,30 @@ __global__ void __launch_bounds__(kBlock, GRAD == kGradImage ? 5 : 4) k_mattes_p
 }
 
 #ifndef GB_KERNELS_HELPERS_ONLY
+// The derivative's log(p / pm) table in global memory, one entry per thread (the
+// same arithmetic as mattes_pratio_build), for the derivative kernels that read it
+// from global memory (B-spline chunk sums).  A few blocks launched after pass 1,
+// instead of pass 1's last block forming all bins^2 entries alone on one SM.
+__global__ void __launch_bounds__(kBlock) k_mattes_table(EvalArgs a) {
+  griddep_wait();
+  if (halted(a)) return;
+  griddep_launch_dependents();
+  const int B = a.bins;
+  const double T = __ldcg(&a.marg[0]);
+  const unsigned long long N = __ldcg(a.acc_n);
+  const bool bad = N == 0 || !(T * kQInv >= DBL_EPSILON);
+  const unsigned long long hthr = (unsigned long long)(DBL_EPSILON * T);
+  const unsigned long long fthr = (unsigned long long)(DBL_EPSILON * T * kQInv);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < B * B; k += gridDim.x * blockDim.x) {
+    const int f = k / B, m = k - f * B;
+    const unsigned long long cs = __ldcg(&a.colsum[m]);
+    const float c = cs > hthr ? u64_to_float(cs) : 0.f;
+    const bool fok = __ldcg(&a.fmarg[f]) > fthr;
+    const unsigned long long h = bad ? 0ull : __ldcg(&a.hist[k]);
+    a.pratio[k] = (h > hthr && c > 0.f && fok) ? __logf(__fdividef(u64_to_float(h), c)) : 0.f;
+  }
+}
+
 // Mattes value without the derivative: one warp per group of 32 joint-histogram
 // bins (mattes_group_partial), the last block adds the group partials.  With the
 // derivative the same groups are formed by spare warps of the derivative pass

@@ -325,7 +325,7 @@ extern "C" int gb_metric_destroy(gb_metric* m) {
 }
 
 extern "C" int gb_metric_set_floating_point_correction(gb_metric* m, int on, double resolution) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (on && !(resolution > 0.0)) return fail(GB_ERR_BAD_ARG, "floating point correction resolution must be > 0");
   m->fp_res = on ? resolution : 0.0;
@@ -334,7 +334,7 @@ extern "C" int gb_metric_set_floating_point_correction(gb_metric* m, int on, dou
 }
 
 extern "C" int gb_metric_set_joint_pdf_smoothing_variance(gb_metric* m, double variance) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (!(variance == variance)) return fail(GB_ERR_BAD_ARG, "variance is NaN");
   m->jhmi_variance = variance;
@@ -343,7 +343,7 @@ extern "C" int gb_metric_set_joint_pdf_smoothing_variance(gb_metric* m, double v
 }
 
 extern "C" int gb_metric_set_number_of_histogram_bins(gb_metric* m, uint64_t bins) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (bins < 5) bins = 5;  // itkSetClampMacro(NumberOfHistogramBins, SizeValueType, 5, max)
   if (bins > 4096) return fail(GB_ERR_BAD_ARG, "number of histogram bins above 4096");
@@ -376,19 +376,19 @@ static int set_image_common(gb_metric* m, int which, const float* src, bool devi
 
 extern "C" int gb_metric_set_image(gb_metric* m, int which, const float* voxels, const int64_t size[3],
                                    const double spacing[3], const double origin[3], const double direction[9]) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   return set_image_common(m, which, voxels, false, size, spacing, origin, direction);
 }
 
 extern "C" int gb_metric_set_image_device(gb_metric* m, int which, const float* device_voxels, const int64_t size[3],
                                           const double spacing[3], const double origin[3],
                                           const double direction[9]) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   return set_image_common(m, which, device_voxels, true, size, spacing, origin, direction);
 }
 
 extern "C" int gb_metric_set_gradient_source(gb_metric* m, int source) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (source != GB_GRADIENT_IMAGE && source != GB_GRADIENT_CENTRAL_DIFFERENCE &&
       source != GB_GRADIENT_RECURSIVE_GAUSSIAN)
@@ -399,7 +399,7 @@ extern "C" int gb_metric_set_gradient_source(gb_metric* m, int source) {
 }
 
 extern "C" int gb_metric_set_moving_gradient_image(gb_metric* m, const double* gradient_xyz) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !gradient_xyz) return fail(GB_ERR_BAD_ARG, "null argument");
   if (!m->moving.set) return fail(GB_ERR_BAD_ARG, "set the moving image before its gradient image");
   GB_CUDA(cudaSetDevice(m->ctx->device));
@@ -415,7 +415,7 @@ extern "C" int gb_metric_set_moving_gradient_image(gb_metric* m, const double* g
 
 extern "C" int gb_metric_set_virtual_domain(gb_metric* m, const int64_t size[3], const double spacing[3],
                                             const double origin[3], const double direction[9]) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !size || !spacing || !origin || !direction) return fail(GB_ERR_BAD_ARG, "null argument");
   Geom g;
   int rc = geom_init(g, size, spacing, origin, direction);
@@ -427,7 +427,7 @@ extern "C" int gb_metric_set_virtual_domain(gb_metric* m, const int64_t size[3],
 }
 
 extern "C" int gb_metric_set_level_smoothing(gb_metric* m, double sigma, int sigma_in_physical_units) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (!(sigma >= 0.0) || !std::isfinite(sigma)) return fail(GB_ERR_BAD_ARG, "smoothing sigma must be >= 0");
   m->level_sigma = sigma;
@@ -437,7 +437,7 @@ extern "C" int gb_metric_set_level_smoothing(gb_metric* m, double sigma, int sig
 }
 
 extern "C" int gb_metric_set_level_shrink(gb_metric* m, const int64_t factors[3]) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !factors) return fail(GB_ERR_BAD_ARG, "null argument");
   for (int i = 0; i < 3; ++i) m->level_shrink[i] = factors[i] < 1 ? 1 : factors[i];  // ShrinkImageFilter clamps to 1
   m->initialized = false;
@@ -445,7 +445,7 @@ extern "C" int gb_metric_set_level_shrink(gb_metric* m, const int64_t factors[3]
 }
 
 extern "C" int gb_metric_set_sampled_points(gb_metric* m, const float* xyz, int64_t n, int virtual_space) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (n < 0 || (n > 0 && !xyz)) return fail(GB_ERR_BAD_ARG, "bad point array");
   if (n > (int64_t)0x7fffffff) return fail(GB_ERR_BAD_ARG, "more than 2^31-1 sample points");
@@ -456,7 +456,7 @@ extern "C" int gb_metric_set_sampled_points(gb_metric* m, const float* xyz, int6
 }
 
 extern "C" int gb_metric_use_sampled_point_set(gb_metric* m, int on) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   m->use_sampled = on != 0;
   m->initialized = false;
@@ -465,7 +465,7 @@ extern "C" int gb_metric_use_sampled_point_set(gb_metric* m, int on) {
 
 extern "C" int gb_metric_set_moving_transform(gb_metric* m, int kind, const double* params, int64_t nparams,
                                               const double* fixed, int64_t nfixed) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !params || !fixed) return fail(GB_ERR_BAD_ARG, "null argument");
   if (kind == GB_TRANSFORM_AFFINE) {
     if (nparams != 12 || nfixed != 3) return fail(GB_ERR_BAD_ARG, "affine transform takes 12 parameters and a 3-D centre");
@@ -510,7 +510,7 @@ extern "C" int gb_metric_set_moving_transform(gb_metric* m, int kind, const doub
 }
 
 extern "C" int gb_metric_set_parameters(gb_metric* m, const double* params, int64_t nparams) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !params) return fail(GB_ERR_BAD_ARG, "null argument");
   if (m->tkind < 0) return fail(GB_ERR_BAD_ARG, "no moving transform set");
   if ((size_t)nparams != m->tparams.size()) return fail(GB_ERR_BAD_ARG, "parameter count mismatch");
@@ -520,7 +520,7 @@ extern "C" int gb_metric_set_parameters(gb_metric* m, const double* params, int6
 
 extern "C" int gb_metric_update_transform_parameters(gb_metric* m, const double* update, int64_t nparams,
                                                      double factor) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !update) return fail(GB_ERR_BAD_ARG, "null argument");
   if ((size_t)nparams != m->tparams.size())
     return fail(GB_ERR_BAD_ARG, "Parameter update size must be same as transform parameter size");
@@ -532,7 +532,7 @@ extern "C" int gb_metric_update_transform_parameters(gb_metric* m, const double*
 }
 
 extern "C" int gb_metric_get_parameters(gb_metric* m, double* params, int64_t nparams) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !params) return fail(GB_ERR_BAD_ARG, "null argument");
   if ((size_t)nparams != m->tparams.size()) return fail(GB_ERR_BAD_ARG, "parameter count mismatch");
   copy_parallel(params, m->tparams.data(), sizeof(double) * m->tparams.size());
@@ -540,7 +540,7 @@ extern "C" int gb_metric_get_parameters(gb_metric* m, double* params, int64_t np
 }
 
 extern "C" int gb_metric_get_number_of_parameters(gb_metric* m, int64_t* nparams) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !nparams) return fail(GB_ERR_BAD_ARG, "null argument");
   *nparams = (int64_t)m->tparams.size();
   return GB_OK;
@@ -561,7 +561,7 @@ static size_t acc_layout_bytes(const gb_metric* m) {
 }
 
 extern "C" int gb_metric_initialize(gb_metric* m) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   m->drop_host_graphs();  // they hold this level's buffers and arguments
   if (!m->fixed.set) return fail(GB_ERR_BAD_ARG, "FixedImage is not present");
@@ -1138,9 +1138,20 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
     }
   }
   if (!deriv) return GB_OK;
-  // Mattes: at least one chunk-kernel block per value group
-  const int64_t cblocks = mattes ? std::max<int64_t>(m->nchunks, mattes_groups((int)m->bins)) : m->nchunks;
-  if (cblocks > 0) {
+  if (mattes) {  // the derivative's log(p / pm) table
+    const int BB = (int)(m->bins * m->bins);
+    GB_CUDA(launch_chain(m, k_mattes_table, (unsigned)((BB + kBlock - 1) / kBlock), kBlock, 0, a));
+    m->mark();
+  }
+  // the chunk sums, grid-stride over one full wave (Mattes: at least one block per value group)
+  const int64_t want = mattes ? std::max<int64_t>(m->nchunks, mattes_groups((int)m->bins)) : m->nchunks;
+  if (want > 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mattes ? k_bspline_chunks<true> : k_bspline_chunks<false>,
+                                                      kChunkLen, 0) != cudaSuccess || per_sm < 1)
+      per_sm = 4;
+    const int64_t wave = (int64_t)m->ctx->sm_count * per_sm;
+    const int64_t cblocks = std::min<int64_t>(want, std::max<int64_t>(wave, mattes ? mattes_groups((int)m->bins) : 1));
     GB_CUDA(mattes ? launch_chain(m, k_bspline_chunks<true>, (unsigned)cblocks, kChunkLen, 0, a)
                    : launch_chain(m, k_bspline_chunks<false>, (unsigned)cblocks, kChunkLen, 0, a));
     m->mark();
@@ -1382,7 +1393,7 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
 }
 
 extern "C" int gb_metric_set_fault_injection(gb_metric* m, int fault) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   if (fault != GB_FAULT_NONE && fault != GB_FAULT_STALLED_COPY) return fail(GB_ERR_BAD_ARG, "unknown fault");
   if (fault != m->inject_fault) m->drop_host_graphs();  // the graphs hold the kernels' arguments
@@ -1391,7 +1402,7 @@ extern "C" int gb_metric_set_fault_injection(gb_metric* m, int fault) {
 }
 
 extern "C" int gb_metric_set_profiling(gb_metric* m, int on) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   m->profiling = on != 0;
   m->nevents = 0;
@@ -1399,7 +1410,7 @@ extern "C" int gb_metric_set_profiling(gb_metric* m, int on) {
 }
 
 extern "C" int gb_metric_get_kernel_times(gb_metric* m, double* ms, int max_kernels, int* count) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !count) return fail(GB_ERR_BAD_ARG, "null argument");
   GB_CUDA(cudaSetDevice(m->ctx->device));
   const int n = m->nevents > 1 ? m->nevents - 1 : 0;
@@ -1520,33 +1531,33 @@ static int eval_host(gb_metric* m, double* value, double* derivative, int64_t np
 }
 
 extern "C" int gb_metric_get_value_and_derivative(gb_metric* m, double* value, double* derivative, int64_t nparams) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!derivative || !value) return fail(GB_ERR_BAD_ARG, "null output");
   return eval_host(m, value, derivative, nparams, true);
 }
 
 extern "C" int gb_metric_get_value(gb_metric* m, double* value) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!value) return fail(GB_ERR_BAD_ARG, "null output");
   return eval_host(m, value, nullptr, 0, false);
 }
 
 extern "C" int gb_metric_get_number_of_valid_points(gb_metric* m, uint64_t* nvalid) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !nvalid) return fail(GB_ERR_BAD_ARG, "null argument");
   *nvalid = m->last_nvalid;
   return GB_OK;
 }
 
 extern "C" int gb_metric_get_number_of_domain_points(gb_metric* m, uint64_t* n) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !n) return fail(GB_ERR_BAD_ARG, "null argument");
   *n = (uint64_t)m->ndomain;
   return GB_OK;
 }
 
 extern "C" int gb_metric_get_joint_pdf(gb_metric* m, double* out, int64_t n) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !out) return fail(GB_ERR_BAD_ARG, "null argument");
   if (m->kind != GB_METRIC_MATTES && m->kind != GB_METRIC_JOINT_HISTOGRAM_MI)
     return fail(GB_ERR_BAD_ARG, "joint PDF exists for the Mattes and joint-histogram metrics only");
@@ -1559,7 +1570,7 @@ extern "C" int gb_metric_get_joint_pdf(gb_metric* m, double* out, int64_t n) {
 }
 
 extern "C" int gb_metric_get_mattes_state(gb_metric* m, double out8[8]) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !out8) return fail(GB_ERR_BAD_ARG, "null argument");
   if (m->kind != GB_METRIC_MATTES) return fail(GB_ERR_BAD_ARG, "Mattes metric only");
   for (int i = 0; i < 8; ++i) out8[i] = m->mstate[i];
@@ -1577,14 +1588,14 @@ size_t gb_metric::device_bytes() const {
 }
 
 extern "C" int gb_metric_get_device_bytes(gb_metric* m, uint64_t* bytes) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !bytes) return fail(GB_ERR_BAD_ARG, "null argument");
   *bytes = (uint64_t)m->device_bytes();
   return GB_OK;
 }
 
 extern "C" int gb_metric_get_stream(gb_metric* m, uint64_t* stream) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !stream) return fail(GB_ERR_BAD_ARG, "null argument");
   *stream = (uint64_t)(uintptr_t)m->stream;
   return GB_OK;
@@ -1592,7 +1603,7 @@ extern "C" int gb_metric_get_stream(gb_metric* m, uint64_t* stream) {
 
 extern "C" int gb_metric_evaluate_device(gb_metric* m, const double* device_params, double* device_out,
                                          int with_derivative) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m || !device_params || !device_out) return fail(GB_ERR_BAD_ARG, "null argument");
   if (!m->initialized) return fail(GB_ERR_NOT_INITIALIZED, "call gb_metric_initialize first");
   GB_CUDA(cudaSetDevice(m->ctx->device));
@@ -1600,7 +1611,7 @@ extern "C" int gb_metric_evaluate_device(gb_metric* m, const double* device_para
 }
 
 extern "C" int gb_metric_synchronize(gb_metric* m) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   GB_CUDA(cudaSetDevice(m->ctx->device));
   GB_CUDA(cudaMemcpyAsync(m->h_status, m->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));

@@ -322,7 +322,7 @@ int opt_collect(gb_metric* m, const StepArgs& a, gb_optimizer_report* report) {
 using namespace gb;
 
 extern "C" int gb_metric_set_optimizer_graphs(gb_metric* m, int on) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   if (!m) return fail(GB_ERR_BAD_ARG, "null metric");
   m->opt_graphs = on != 0;
   return GB_OK;
@@ -330,7 +330,7 @@ extern "C" int gb_metric_set_optimizer_graphs(gb_metric* m, int on) {
 
 extern "C" int gb_metric_optimize_regular_step(gb_metric* m, const gb_regular_step_settings* cfg,
                                                const double* scales, int64_t nscales, gb_optimizer_report* report) {
-  gb::ErrorScope scope_(m);
+  gb::ErrorScope scope_(m, __func__);
   StepArgs a;
   int rc = opt_setup(m, cfg, scales, nscales, a);
   if (rc) return rc;
