@@ -255,41 +255,69 @@ __global__ void __launch_bounds__(kBlock, SMEM ? 4 : 3) k_mattes_pass1_bspline(E
 // added in slice order.
 constexpr int kChunkSlices = 16;
 // Grid-stride over the chunks (one full wave of blocks): block b forms chunks b, b + G, ...
+// The next chunk's per-sample inputs are loaded into registers while the current
+// chunk is summed, and (Mattes) the log(p / pm) table is staged in shared memory
+// (dynamic shared memory, bins^2 floats) once per block.
 template <bool MATTES>
 __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
+  extern __shared__ float pr_sh[];
   __shared__ __align__(16) float W1[kChunkLen][12];
   __shared__ float4 AV[kChunkLen];
   __shared__ float qs[kChunkSlices][192];
   griddep_wait();
   if (halted(a)) return;
-  if (MATTES) mattes_value_groups(a);  // the value's group partials (blocks b, b + G, ...)
   const int B = a.bins;
   const int t = threadIdx.x;
+  if (MATTES) {
+    mattes_value_groups(a);  // the value's group partials (blocks b, b + G, ...)
+    for (int k = t; k < B * B; k += blockDim.x) pr_sh[k] = __ldcg(a.pratio + k);
+  }
+  // this thread's inputs of one chunk: the run, the sample's support, cache and fixed bin
+  struct In {
+    int4 ch;
+    float4 su, c;
+    int fbin;
+  };
+  auto fetch = [&](int cidx) {
+    In in;
+    in.ch = make_int4(0, 0, 0, 0);
+    in.su = in.c = make_float4(0.f, 0.f, 0.f, 0.f);
+    in.fbin = 0;
+    if (cidx < a.nchunks) {
+      in.ch = __ldg(a.chunks + cidx);
+      if (t < in.ch.y - in.ch.x) {
+        const int64_t i = (int64_t)in.ch.x + t;
+        in.su = __ldg(a.sup + i);
+        in.c = __ldcg(a.cache + i);
+        if (MATTES) in.fbin = __float_as_int(__ldg(&a.samples[i].w));
+      }
+    }
+    return in;
+  };
+  In cur = fetch(blockIdx.x);
+  __syncthreads();  // the staged table
   for (int cidx = blockIdx.x; cidx < a.nchunks; cidx += gridDim.x) {
-    const int4 ch = a.chunks[cidx];
-    const int len = ch.y - ch.x;
+    const In nxt = fetch(cidx + gridDim.x);  // in flight while this chunk is summed
+    const int len = cur.ch.y - cur.ch.x;
     if (t < len) {
-      const int64_t i = (int64_t)ch.x + t;
-      const float4 su = __ldg(a.sup + i);
-      const float4 c = __ldcg(a.cache + i);
       float4 av = make_float4(0.f, 0.f, 0.f, 0.f);
       if (MATTES) {
-        const int fbin = __float_as_int(__ldg(&a.samples[i].w));
+        const float4 c = cur.c;
         if (c.x == c.x) {
           int pdfm;
           float tt, d[4];
           parzen_window(c.x, B, pdfm, tt);
           parzen_deriv(tt, d);
-          const float* row = a.pratio + fbin * B + pdfm;
-          const float w = __ldcg(row) * d[0] + __ldcg(row + 1) * d[1] + __ldcg(row + 2) * d[2] + __ldcg(row + 3) * d[3];
+          const float* row = pr_sh + cur.fbin * B + pdfm;
+          const float w = row[0] * d[0] + row[1] * d[1] + row[2] * d[2] + row[3] * d[3];
           av = make_float4(w * c.y, w * c.z, w * c.w, 0.f);
         }
       } else {
-        av = make_float4(c.x, c.y, c.z, 0.f);
+        av = make_float4(cur.c.x, cur.c.y, cur.c.z, 0.f);
       }
-      bspline_basis(su.x, &W1[t][0]);
-      bspline_basis(su.y, &W1[t][4]);
-      bspline_basis(su.z, &W1[t][8]);
+      bspline_basis(cur.su.x, &W1[t][0]);
+      bspline_basis(cur.su.y, &W1[t][4]);
+      bspline_basis(cur.su.z, &W1[t][8]);
       AV[t] = av;
     }
     __syncthreads();
@@ -320,12 +348,13 @@ __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
     }
     __syncthreads();
     if (t < 192) {
-      float s = qs[0][t];
+      float sum = qs[0][t];
 #pragma unroll
-      for (int q = 1; q < kChunkSlices; ++q) s = __fadd_rn(s, qs[q][t]);
-      a.chunk_part[(size_t)cidx * 192 + t] = s;
+      for (int q = 1; q < kChunkSlices; ++q) sum = __fadd_rn(sum, qs[q][t]);
+      a.chunk_part[(size_t)cidx * 192 + t] = sum;
     }
     __syncthreads();  // the next chunk overwrites W1, AV and qs
+    cur = nxt;
   }
   griddep_launch_dependents();
 }

@@ -1143,17 +1143,19 @@ static int enqueue_eval_bspline(gb_metric* m, const EvalArgs& a, bool cd, bool d
     GB_CUDA(launch_chain(m, k_mattes_table, (unsigned)((BB + kBlock - 1) / kBlock), kBlock, 0, a));
     m->mark();
   }
-  // the chunk sums, grid-stride over one full wave (Mattes: at least one block per value group)
+  // the chunk sums, grid-stride over one full wave (Mattes: at least one block per value
+  // group; the table staged in dynamic shared memory)
   const int64_t want = mattes ? std::max<int64_t>(m->nchunks, mattes_groups((int)m->bins)) : m->nchunks;
   if (want > 0) {
+    auto kc = mattes ? k_bspline_chunks<true> : k_bspline_chunks<false>;
+    const size_t csm = mattes ? sizeof(float) * (size_t)(m->bins * m->bins) : 0;
+    GB_CUDA(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mattes ? k_bspline_chunks<true> : k_bspline_chunks<false>,
-                                                      kChunkLen, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kc, kChunkLen, csm) != cudaSuccess || per_sm < 1)
       per_sm = 4;
     const int64_t wave = (int64_t)m->ctx->sm_count * per_sm;
     const int64_t cblocks = std::min<int64_t>(want, std::max<int64_t>(wave, mattes ? mattes_groups((int)m->bins) : 1));
-    GB_CUDA(mattes ? launch_chain(m, k_bspline_chunks<true>, (unsigned)cblocks, kChunkLen, 0, a)
-                   : launch_chain(m, k_bspline_chunks<false>, (unsigned)cblocks, kChunkLen, 0, a));
+    GB_CUDA(launch_chain(m, kc, (unsigned)cblocks, kChunkLen, csm, a));
     m->mark();
   }
   // one warp per node, or one block per node when the nodes hold many chunk entries
