@@ -209,15 +209,21 @@ __global__ void __launch_bounds__(kBlock, SMEM ? 4 : 3) k_mattes_pass1_bspline(E
   unsigned nv = 0;
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < a.n; base += stride) {
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  // the next iteration's record and support travel while this one is evaluated
+  float4 s_next = base + lane < a.n ? __ldcs(a.samples + base + lane) : zero;
+  float4 su_next = base + lane < a.n ? __ldcs(a.sup + base + lane) : zero;
+  for (; base < a.n; base += stride) {
     const int64_t i = base + lane;
     const bool live = i < a.n;
-    const float4 s = live ? __ldcs(a.samples + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 s = s_next, su = su_next;
+    s_next = i + stride < a.n ? __ldcs(a.samples + i + stride) : zero;
+    su_next = i + stride < a.n ? __ldcs(a.sup + i + stride) : zero;
     float m = 0.f;
     float3 g = make_float3(0.f, 0.f, 0.f);
     bool ok = false, has_jac = false;
     if (live) {
-      const float4 su = __ldcs(a.sup + i);
       const DFPos p = bspline_position(K, nodes, a, s, su, has_jac);
       ok = eval_moving<GRAD>(a, p, a.with_derivative != 0 && has_jac, m, g);
       ok = ok && !(m < a.mmin) && !(m > a.mmax);  // Mattes...Threader.hxx:238-245
