@@ -192,6 +192,9 @@ struct EvalArgs {
   // fault injection (gb_metric_set_fault_injection): GB_FAULT_STALLED_COPY makes the
   // affine Mattes derivative pass issue none of its record copies
   int inject_stall;
+  // the affine Mattes derivative pass takes the final histogram and marginals (hist,
+  // fmarg, colsum: contiguous, 16-byte aligned) into shared memory with one bulk copy
+  int hist_bulk;
 };
 
 // The optimizer's stop flag (read once per block, after the launch dependency).
@@ -342,6 +345,121 @@ __device__ __forceinline__ bool grid_sums(const double* blk, double* part, doubl
   return true;
 }
 
+// Double-float values: hi + lo, two FP32 numbers with |lo| <= ulp(hi) / 2, about 48
+// significant bits.  The Mattes derivative pass sums its block partials this way:
+// FP32 adds at the FP32 rate, where GB300's FP64 rate (about 1/64 of it) makes an
+// FP64 chain over a few hundred partials take microseconds in the one block that
+// forms the sums.  Addition: Knuth's two-sum of the high parts, the low parts added
+// in, Dekker's fast two-sum to renormalize (the _rn intrinsics are never contracted
+// or reassociated).
+struct DFloat {
+  float hi, lo;
+};
+__device__ __forceinline__ DFloat df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return DFloat{s, e};
+}
+__device__ __forceinline__ DFloat df_add(DFloat a, DFloat b) {
+  const DFloat s = df_two_sum(a.hi, b.hi);
+  const float lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  const float hi = __fadd_rn(s.hi, lo);
+  return DFloat{hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
+}
+__device__ __forceinline__ double df_to_double(DFloat v) { return (double)v.hi + (double)v.lo; }
+
+// block_sums with the block's compensated FP32 sums kept exactly: s - c as a double-float.
+template <int NV>
+__device__ __forceinline__ void block_sums_df(KahanF (&acc)[NV], float (*red)[NV], DFloat* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const float v = warp_sum(acc[k].value());
+    if (lane == 0) red[warp][k] = v;
+  }
+  __syncthreads();
+  const int nwarps = blockDim.x >> 5;
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) {
+    KahanF s;
+    s.zero();
+    for (int w = 0; w < nwarps; ++w) s.add(red[w][k]);
+    out[k] = df_two_sum(s.s, -s.c);
+  }
+  __syncthreads();
+}
+
+// strided_sums in double-float: dst[k] = sum_{j < cnt} src[j * NV + k], one warp per k,
+// lane l adding entries l, l + 32, ... (loads in flight together), then a fixed XOR tree.
+template <int NV>
+__device__ __forceinline__ void strided_sums_df(const DFloat* src, int cnt, DFloat* dst) {
+  constexpr int kBatch = 4;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int k = warp; k < NV; k += nwarps) {
+    DFloat s{0.f, 0.f};
+    for (int j0 = lane; j0 < cnt; j0 += kBatch * 32) {
+      float2 v[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int j = j0 + u * 32;
+        v[u] = j < cnt ? __ldcg(reinterpret_cast<const float2*>(src + j * NV + k)) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u)
+        if (j0 + u * 32 < cnt) s = df_add(s, DFloat{v[u].x, v[u].y});
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      s = df_add(s, DFloat{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)});
+    if (lane == 0) dst[k] = s;
+  }
+}
+
+// strided_sums_df over partials staged in shared memory, by warps [0, nwarps).
+template <int NV>
+__device__ __forceinline__ void strided_sums_df_shared(const DFloat* src, int cnt, DFloat* dst, int nwarps) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = warp; k < NV; k += nwarps) {
+    DFloat s{0.f, 0.f};
+    for (int j = lane; j < cnt; j += 32) s = df_add(s, src[j * NV + k]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      s = df_add(s, DFloat{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)});
+    if (lane == 0) dst[k] = s;
+  }
+}
+
+// grid_sums / grid_sums_flat over double-float partials (part and grp hold DFloat);
+// `fin` receives the sums as doubles.
+template <int NV>
+__device__ __forceinline__ bool grid_sums_df(const DFloat* blk, DFloat* part, DFloat* grp, unsigned* tick,
+                                             double* fin, VGrid vg = hw_grid()) {
+  __shared__ unsigned t;
+  const int b = vg.b, g = b / kGroup;
+  const int ng = (vg.n + kGroup - 1) / kGroup;
+  const int gsize = min(kGroup, vg.n - g * kGroup);
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) part[b * NV + k] = blk[k];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) t = atomicAdd(&tick[g], 1u);
+  __syncthreads();
+  if (t != (unsigned)(gsize - 1)) return false;
+  __threadfence();
+  strided_sums_df<NV>(part + g * kGroup * NV, gsize, grp + g * NV);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) t = atomicAdd(&tick[ng], 1u);
+  __syncthreads();
+  if (t != (unsigned)(ng - 1)) return false;
+  __threadfence();
+  __shared__ DFloat fin_s[NV];
+  strided_sums_df<NV>(grp, ng, fin_s);
+  __syncthreads();
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) fin[k] = df_to_double(fin_s[k]);
+  __syncthreads();
+  return true;
+}
+
 // One-level form of grid_sums for grids of at most kFlatMaxBlocks blocks: every block
 // writes its partials and takes one ticket; the last sums all blocks' partials in
 // block order (lane-strided, fixed XOR trees).  One global round trip fewer than
@@ -362,6 +480,58 @@ __device__ __forceinline__ bool grid_sums_flat(const double* blk, double* part, 
   strided_sums<NV>(part, vg.n, fin_s);
   __syncthreads();
   for (int k = threadIdx.x; k < NV; k += blockDim.x) fin[k] = fin_s[k];
+  __syncthreads();
+  return true;
+}
+
+// The flat form's first half: this block's partials and its ticket; true in the last block.
+template <int NV>
+__device__ __forceinline__ bool grid_ticket_flat_df(const DFloat* blk, DFloat* part, unsigned* tick, VGrid vg) {
+  __shared__ unsigned t;
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) part[vg.b * NV + k] = blk[k];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) t = atomicAdd(tick, 1u);
+  __syncthreads();
+  if (t != (unsigned)(vg.n - 1)) return false;
+  __threadfence();
+  return true;
+}
+
+// dst[0, n) <- src[0, n) (global, 8-byte entries), every entry requested before the
+// first lands: one L2 round trip for a few thousand entries.
+__device__ __forceinline__ void stage_u64(const unsigned long long* src, int n, unsigned long long* dst) {
+  constexpr int kLoads = 16;
+  for (int e0 = threadIdx.x; e0 < n; e0 += kLoads * blockDim.x) {
+    unsigned long long v[kLoads];
+#pragma unroll
+    for (int u = 0; u < kLoads; ++u) {
+      const int e = e0 + u * (int)blockDim.x;
+      v[u] = e < n ? __ldcg(src + e) : 0ull;
+    }
+#pragma unroll
+    for (int u = 0; u < kLoads; ++u) {
+      const int e = e0 + u * (int)blockDim.x;
+      if (e < n) dst[e] = v[u];
+    }
+  }
+}
+
+template <int NV>
+__device__ __forceinline__ bool grid_sums_flat_df(const DFloat* blk, DFloat* part, unsigned* tick, double* fin,
+                                                  VGrid vg = hw_grid()) {
+  __shared__ unsigned t;
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) part[vg.b * NV + k] = blk[k];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) t = atomicAdd(tick, 1u);
+  __syncthreads();
+  if (t != (unsigned)(vg.n - 1)) return false;
+  __threadfence();
+  __shared__ DFloat fin_s[NV];
+  strided_sums_df<NV>(part, vg.n, fin_s);
+  __syncthreads();
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) fin[k] = df_to_double(fin_s[k]);
   __syncthreads();
   return true;
 }
@@ -773,6 +943,22 @@ __device__ __forceinline__ void hist_add_aggregated(bool ok, int key, int fidx, 
 // __syncthreads, which would also wait for the block's group warp).
 __device__ __forceinline__ void stream_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(kBlock) : "memory"); }
 
+// The table's validity thresholds from the fixed-point total T and the valid count N:
+// p > eps <=> h > floor(eps T), pf > eps <=> count > floor(eps T / 2^26), and no
+// table at all when N = 0 or the joint PDF sums to zero.  FP64 (a handful of
+// operations at GB300's FP64 rate): formed by one thread and shared.
+struct PratioThresholds {
+  unsigned long long hthr, fthr;
+  int bad;
+};
+__device__ __forceinline__ PratioThresholds pratio_thresholds(double T, unsigned long long N) {
+  PratioThresholds t;
+  t.bad = (N == 0 || !(T * kQInv >= DBL_EPSILON)) ? 1 : 0;
+  t.hthr = (unsigned long long)(DBL_EPSILON * T);
+  t.fthr = (unsigned long long)(DBL_EPSILON * T * kQInv);
+  return t;
+}
+
 template <bool STREAMERS>
 static __device__ __noinline__ void mattes_pratio_build(const EvalArgs& a, double T, float* dst, float* colf,
                                                         unsigned* fmask);
@@ -821,7 +1007,9 @@ __device__ __forceinline__ void mattes_pass1_epilogue(const EvalArgs& a, unsigne
   __syncthreads();
   unsigned long long t = 0ull;
   for (int k = threadIdx.x; k < B; k += blockDim.x) t += __ldcg(&a.colsum[k]);
-  atomicAdd(&tot_sh, t);
+  // one shared atomic per warp: a block's worth of same-address atomics would serialize
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0 && t) atomicAdd(&tot_sh, t);
   __syncthreads();
   const double T = (double)tot_sh;
   if (threadIdx.x == 0) {
@@ -848,11 +1036,11 @@ static __device__ __noinline__ void mattes_pratio_build(const EvalArgs& a, doubl
     if (STREAMERS) stream_barrier();
     else __syncthreads();
   };
-  const unsigned long long N = __ldcg(a.acc_n);
-  const bool bad = N == 0 || !(T * kQInv >= DBL_EPSILON);
-  const unsigned long long hthr = (unsigned long long)(DBL_EPSILON * T);
-  const unsigned long long fthr = (unsigned long long)(DBL_EPSILON * T * kQInv);
-  sync();  // colf / fmask may alias scratch the caller has just used
+  __shared__ PratioThresholds th_s;
+  if (threadIdx.x == 0) th_s = pratio_thresholds(T, __ldcg(a.acc_n));  // FP64: once per block
+  sync();  // the thresholds; colf / fmask may alias scratch the caller has just used
+  const bool bad = th_s.bad != 0;
+  const unsigned long long hthr = th_s.hthr, fthr = th_s.fthr;
   // marginals into shared memory: column sums as floats (0 where pm is not above
   // eps), fixed-bin validity
   for (int k = threadIdx.x; k < B; k += nt) {
@@ -929,8 +1117,16 @@ __host__ __device__ inline int mattes_groups(int bins) { return (bins * bins + 3
 
 // Sum of the group partials part[0, ngroups): lane-strided, then a fixed XOR tree.
 __device__ __forceinline__ double mattes_value_sum(const double* part, int ngroups, int lane) {
+  constexpr int kBatch = 8;  // loads in flight together, added in the same order
   double s = 0.0;
-  for (int r = lane; r < ngroups; r += 32) s += __ldcg(&part[r]);
+  for (int r0 = lane; r0 < ngroups; r0 += kBatch * 32) {
+    double v[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) v[u] = r0 + u * 32 < ngroups ? __ldcg(&part[r0 + u * 32]) : 0.0;
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u)
+      if (r0 + u * 32 < ngroups) s += v[u];
+  }
   return warp_sum_d(s);
 }
 
@@ -1022,11 +1218,11 @@ __global__ void __launch_bounds__(kBlock) k_mattes_table(EvalArgs a) {
   if (halted(a)) return;
   griddep_launch_dependents();
   const int B = a.bins;
-  const double T = __ldcg(&a.marg[0]);
-  const unsigned long long N = __ldcg(a.acc_n);
-  const bool bad = N == 0 || !(T * kQInv >= DBL_EPSILON);
-  const unsigned long long hthr = (unsigned long long)(DBL_EPSILON * T);
-  const unsigned long long fthr = (unsigned long long)(DBL_EPSILON * T * kQInv);
+  __shared__ PratioThresholds th_s;
+  if (threadIdx.x == 0) th_s = pratio_thresholds(__ldcg(&a.marg[0]), __ldcg(a.acc_n));  // FP64: once per block
+  __syncthreads();
+  const bool bad = th_s.bad != 0;
+  const unsigned long long hthr = th_s.hthr, fthr = th_s.fthr;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < B * B; k += gridDim.x * blockDim.x) {
     const int f = k / B, m = k - f * B;
     const unsigned long long cs = __ldcg(&a.colsum[m]);
@@ -1076,6 +1272,55 @@ __host__ __device__ inline size_t mattes_pass2_smem(int bins) {
   return kStreamBytes + sizeof(float) * (size_t)bins * bins + 8 * (size_t)bins;
 }
 
+// With EvalArgs::hist_bulk: the copied histogram and marginals (B^2 + 2B u64, rounded
+// up to 16 bytes; the accumulator buffer is padded for the rounding) after the above,
+// at a 16-byte boundary.
+__host__ __device__ inline size_t mattes_pass2_hist_offset(int bins) { return (mattes_pass2_smem(bins) + 15) / 16 * 16; }
+__host__ __device__ inline size_t mattes_pass2_hist_bytes(int bins) {
+  return (8 * ((size_t)bins * bins + 2 * (size_t)bins) + 15) / 16 * 16;
+}
+
+// The derivative's log(p / pm) table (the same bits as mattes_pratio_build) formed by
+// the kBlock streaming threads from the copied histogram hs (then fmarg, colsum).
+__device__ __forceinline__ void mattes_pratio_from_copy(const EvalArgs& a, double T, unsigned long long N,
+                                                        const unsigned long long* hs, float* dst, float* colf,
+                                                        unsigned* fmask) {
+  const int B = a.bins;
+  const int BB = B * B;
+  __shared__ PratioThresholds th_s;
+  if (threadIdx.x == 0) th_s = pratio_thresholds(T, N);  // FP64: once per block
+  stream_barrier();
+  const PratioThresholds th = th_s;
+  const unsigned long long* fs = hs + BB;
+  const unsigned long long* cs = fs + B;
+  for (int k = threadIdx.x; k < B; k += kBlock) {
+    colf[k] = cs[k] > th.hthr ? u64_to_float(cs[k]) : 0.f;
+    fmask[k] = fs[k] > th.fthr ? 1u : 0u;
+  }
+  stream_barrier();
+  // kBatch independent entries per thread in flight; f = k / B by a multiply-high
+  // (exact: k < 2^32 / B)
+  constexpr int kBatch = 4;
+  const unsigned long long inv = (0x100000000ull + (unsigned)B - 1u) / (unsigned)B;
+  for (int k0 = threadIdx.x; k0 < BB; k0 += kBatch * kBlock) {
+    unsigned long long h[kBatch];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int k = k0 + j * kBlock;
+      h[j] = (!th.bad && k < BB) ? hs[k] : 0ull;
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int k = k0 + j * kBlock;
+      if (k >= BB) break;
+      const int f = (int)(((unsigned long long)k * inv) >> 32), m = k - f * B;
+      const float c = colf[m];
+      dst[k] = (h[j] > th.hthr && c > 0.f && fmask[f]) ? __logf(__fdividef(u64_to_float(h[j]), c)) : 0.f;
+    }
+  }
+  stream_barrier();
+}
+
 // Whole tiles spread evenly: block b gets tiles [b T / G, (b + 1) T / G).
 __device__ __forceinline__ void block_range(int64_t n, int64_t& b0, int64_t& b1, VGrid vg) {
   const int64_t tiles = (n + kStreamTile - 1) / kStreamTile;
@@ -1106,10 +1351,12 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
   float* colf = pr + B * B;
   unsigned* fmask = reinterpret_cast<unsigned*>(colf + B);
   __shared__ unsigned long long full[kStreamStages];
+  __shared__ unsigned long long hbar;  // the histogram copy (hist_bulk)
   __shared__ int failed;
   __shared__ EvalConsts K;
   __shared__ float red[kWarps][12];
-  __shared__ double blk[12], fin[12];
+  __shared__ DFloat blk[12];
+  __shared__ double fin[12];
   int64_t b0, b1;
   block_range(a.n, b0, b1, vg);
   const int ntiles = (int)((b1 - b0 + kStreamTile - 1) / kStreamTile);
@@ -1117,6 +1364,8 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
   const bool stall = a.inject_stall != 0;
   const unsigned limit = stall ? kInjectWaitPolls : kWaitLimit;
   const bool streamer = !GROUP_WARP || (int)threadIdx.x < kBlock;
+  const bool hb = GROUP_WARP && a.hist_bulk != 0;
+  unsigned long long* hsh = reinterpret_cast<unsigned long long*>(smem_raw + mattes_pass2_hist_offset(B));
   int issued = 0;  // thread 0: tiles whose copies are issued
   // tile t -> stage t % kStreamStages; the stage's phase parity is (t / kStreamStages) & 1
   auto issue = [&](int t) {
@@ -1131,26 +1380,48 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
   };
   if (threadIdx.x == 0) {
     for (int st = 0; st < kStreamStages; ++st) mbar_init(&full[st], 1);
+    mbar_init(&hbar, 1);
     mbar_init_fence();
     failed = 0;
   }
   griddep_wait();
   if (halted(a)) return;
   griddep_launch_dependents();
-  // the first tiles travel while the table and the constants are formed
-  if (threadIdx.x == 0 && !stall)
+  // this thread's word of the transform constants, the fixed-point total and the valid
+  // count are requested before the bulk copies, so that their replies do not queue
+  // behind the copies' data
+  constexpr int kConstWords = (int)(sizeof(EvalConsts) / 4);
+  const int cw = (int)threadIdx.x;
+  const float cword = cw < kConstWords ? __ldcg(reinterpret_cast<const float*>(a.consts) + cw) : 0.f;
+  const double T = streamer ? __ldcg(&a.marg[0]) : 0.0;
+  const unsigned long long N = streamer ? __ldcg(a.acc_n) : 0ull;
+  // the histogram (first), then the first tiles
+  if (threadIdx.x == 0 && !stall) {
+    if (hb) {
+      const unsigned hbytes = (unsigned)mattes_pass2_hist_bytes(B);
+      mbar_arrive_expect_tx(&hbar, hbytes);
+      bulk_g2s(hsh, a.hist, hbytes, &hbar);
+    }
     for (int t = 0; t < min(kStreamStages, ntiles); ++t) issue(t);
-  load_consts(a.consts, K);
+  }
+  for (int k = cw; k < kConstWords; k += blockDim.x)
+    reinterpret_cast<float*>(&K)[k] = k == cw ? cword : __ldcg(reinterpret_cast<const float*>(a.consts) + k);
   __syncthreads();  // the barriers' initialization and the constants
   float acc[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k] = 0.f;
   if (!GROUP_WARP) {
-    mattes_pratio_build<false>(a, __ldcg(&a.marg[0]), pr, colf, fmask);
+    mattes_pratio_build<false>(a, T, pr, colf, fmask);
     mattes_value_groups(a, vg);  // the value's FP64 group partials, last warp
     __syncthreads();
   } else if (streamer) {
-    mattes_pratio_build<true>(a, __ldcg(&a.marg[0]), pr, colf, fmask);
+    if (hb) {
+      if (!mbar_wait(&hbar, 0u, limit)) failed = 1;
+      stream_barrier();
+      if (!failed) mattes_pratio_from_copy(a, T, N, hsh, pr, colf, fmask);
+    } else {
+      mattes_pratio_build<true>(a, T, pr, colf, fmask);
+    }
   } else {
     // the group warp: its FP64 chain runs while the other warps stream
     const int ng = mattes_groups(B);
@@ -1160,7 +1431,8 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
     }
   }
   int t = 0;
-  if (streamer) {
+  const bool looped = streamer && !failed;  // uniform: `failed` is read after a barrier
+  if (looped) {
     // plain FP32 per thread (a thread adds a few dozen samples; the warp tree and the
     // FP64 cross-block sums follow)
     for (; t < ntiles; ++t) {
@@ -1204,7 +1476,9 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
     // a copy never completed: report, wait (bounded) for the copies still in flight, leave
     if (threadIdx.x == 0) {
       atomicExch(a.status, GB_ERR_TIMEOUT);
-      for (int u = t + 1; u < issued; ++u) mbar_wait(&full[u % kStreamStages], (unsigned)(u / kStreamStages) & 1u);
+      // the tile (or, before the loop, the histogram) whose wait ran out is not waited on again
+      for (int u = looped ? t + 1 : 0; u < issued; ++u)
+        mbar_wait(&full[u % kStreamStages], (unsigned)(u / kStreamStages) & 1u);
     }
     return;
   }
@@ -1214,29 +1488,55 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
     kacc[k].s = acc[k];
     kacc[k].c = 0.f;
   }
-  block_sums<12>(kacc, red, blk);
-  const bool last = vg.n <= kFlatMaxBlocks
-                        ? grid_sums_flat<12>(blk, a.part + kPartPass2, a.tickets + kTicketPass2, fin, vg)
-                        : grid_sums<12>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin, vg);
-  if (!last) return;
-  // last block: the value from the group partials (all blocks wrote theirs before their tickets)
+  block_sums_df<12>(kacc, red, blk);
+  DFloat* part = reinterpret_cast<DFloat*>(a.part + kPartPass2);
+  const int ng = mattes_groups(B);
+  // staged form: the last block requests every block partial and value group partial at
+  // once into the (now idle) record stages, then sums them from shared memory, the value
+  // (FP64) in the last warp while the other warps form the derivative
+  const bool staged = vg.n <= kFlatMaxBlocks && (size_t)(vg.n * 12 + ng) * 8 <= kStreamBytes;
+  __shared__ double vsum_s;
+  if (staged) {
+    if (!grid_ticket_flat_df<12>(blk, part, a.tickets + kTicketPass2, vg)) return;
+    DFloat* sp = reinterpret_cast<DFloat*>(smem_raw);
+    double* sv = reinterpret_cast<double*>(sp + vg.n * 12);
+    stage_u64(reinterpret_cast<const unsigned long long*>(part), vg.n * 12,
+              reinterpret_cast<unsigned long long*>(sp));
+    stage_u64(reinterpret_cast<const unsigned long long*>(a.part), ng, reinterpret_cast<unsigned long long*>(sv));
+    __syncthreads();
+    __shared__ DFloat fin_s[12];
+    if ((int)threadIdx.x < (kWarps - 1) * 32) {
+      strided_sums_df_shared<12>(sp, vg.n, fin_s, kWarps - 1);
+    } else {
+      double v = 0.0;
+      for (int r = threadIdx.x & 31; r < ng; r += 32) v += sv[r];
+      v = warp_sum_d(v);
+      if ((threadIdx.x & 31) == 0) vsum_s = v;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 12; k += blockDim.x) fin[k] = df_to_double(fin_s[k]);
+    __syncthreads();
+  } else {
+    const bool last = vg.n <= kFlatMaxBlocks
+                          ? grid_sums_flat_df<12>(blk, part, a.tickets + kTicketPass2, fin, vg)
+                          : grid_sums_df<12>(blk, part, reinterpret_cast<DFloat*>(a.grp), a.tickets + kTicketPass2,
+                                             fin, vg);
+    if (!last) return;
+  }
+  // last block: the value from the group partials (all blocks wrote theirs before their
+  // tickets); warp 0, one derivative entry per lane
   if (threadIdx.x < 32) {
-    const double s = mattes_value_sum(a.part, mattes_groups(B), threadIdx.x);
-    if (threadIdx.x == 0) {
-      const unsigned long long N = __ldcg(a.acc_n);
-      const int st = mattes_status(a);
+    const int lane = threadIdx.x;
+    const int st = N == 0 ? GB_ERR_NO_VALID_POINTS : T * kQInv >= DBL_EPSILON ? GB_OK : GB_ERR_JOINT_PDF_SUM_ZERO;
+    const double s = staged ? vsum_s : mattes_value_sum(a.part, ng, lane);
+    // nFactor = -1 / (MovingImageBinSize * N), Mattes...Threader.hxx:446-457
+    const double nFactor = -1.0 / (a.m_bs * (double)N);
+    if (lane == 0) {
       *a.status = st;
       a.out[1] = (double)N;
-      if (st != GB_OK) {
-        a.out[0] = 0.0;
-        for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = 0.0;
-        return;
-      }
-      // nFactor = -1 / (MovingImageBinSize * N), Mattes...Threader.hxx:446-457
-      const double nFactor = -1.0 / (a.m_bs * (double)N);
-      a.out[0] = -1.0 * s;
-      for (int p = 0; p < a.nparams; ++p) a.out[2 + p] = fin[p] * nFactor;
+      a.out[0] = st == GB_OK ? -1.0 * s : 0.0;
     }
+    for (int p = lane; p < a.nparams; p += 32) a.out[2 + p] = st == GB_OK ? fin[p] * nFactor : 0.0;
   }
 }
 

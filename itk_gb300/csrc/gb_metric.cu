@@ -550,14 +550,16 @@ extern "C" int gb_metric_get_number_of_parameters(gb_metric* m, int64_t* nparams
 // Initialize
 
 // Accumulators cleared before every evaluation:
-// acc_n u64 | tickets kTicketCount u32 | hist B*B u64 | fmarg B u64 | colsum B u64
+// acc_n u64 | tickets kTicketCount u32 | hist B*B u64 | fmarg B u64 | colsum B u64 | 16 bytes
+// The histogram starts at a 16-byte boundary and the padding covers the Mattes
+// derivative pass's bulk copy of hist..colsum rounded up to 16 bytes.
 static size_t acc_offset_tickets() { return 8; }
-static size_t acc_offset_hist() { return 8 + (sizeof(unsigned) * kTicketCount + 7) / 8 * 8; }
+static size_t acc_offset_hist() { return (8 + sizeof(unsigned) * kTicketCount + 15) / 16 * 16; }
 static size_t acc_offset_fmarg(int64_t B) { return acc_offset_hist() + 8 * (size_t)(B * B); }
 static size_t acc_offset_colsum(int64_t B) { return acc_offset_fmarg(B) + 8 * (size_t)B; }
 static size_t acc_layout_bytes(const gb_metric* m) {
   const int64_t B = (m->kind == GB_METRIC_MATTES || m->kind == GB_METRIC_JOINT_HISTOGRAM_MI) ? m->bins : 0;
-  return acc_offset_colsum(B) + 8 * (size_t)B;
+  return acc_offset_colsum(B) + 8 * (size_t)B + 16;
 }
 
 extern "C" int gb_metric_initialize(gb_metric* m) {
@@ -1089,16 +1091,33 @@ static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalAr
 // Mattes pass 2 (affine): kPass2Threads threads per block (the streaming threads and
 // the value's group warp), one full wave, at most kFlatMaxBlocks blocks (the one-level
 // cross-block sums).
-static cudaError_t launch_pass2(gb_metric* m, size_t smem, const EvalArgs& a) {
+// The derivative pass copies the final histogram into shared memory with one bulk
+// copy where that costs no resident block per SM; otherwise each block reads it
+// from global memory.
+static cudaError_t launch_pass2(gb_metric* m, const EvalArgs& a) {
+  const int B = (int)m->bins;
+  const size_t plain = mattes_pass2_smem(B);
+  const size_t bulk = mattes_pass2_hist_offset(B) + mattes_pass2_hist_bytes(B);
+  auto blocks_per_sm = [](size_t smem) {
+    int n = 0;
+    if (cudaFuncSetAttribute(k_mattes_pass2_affine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mattes_pass2_affine, kPass2Threads, smem) != cudaSuccess)
+      n = 0;
+    return n;
+  };
+  const int n_plain = blocks_per_sm(plain);
+  const bool aligned = (reinterpret_cast<uintptr_t>(a.hist) & 15) == 0;
+  const int n_bulk = aligned ? blocks_per_sm(bulk) : 0;
+  EvalArgs a2 = a;
+  a2.hist_bulk = n_bulk >= 1 && n_bulk >= n_plain ? 1 : 0;
+  const size_t smem = a2.hist_bulk ? bulk : plain;
   cudaError_t e = cudaFuncSetAttribute(k_mattes_pass2_affine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mattes_pass2_affine, kPass2Threads, smem) !=
-          cudaSuccess ||
-      per_sm < 1)
-    per_sm = 2;
+  int per_sm = a2.hist_bulk ? n_bulk : n_plain;
+  if (per_sm < 1) per_sm = 2;
   const int grid = std::min(grid_for(m, m->nsamples, per_sm), kFlatMaxBlocks);
-  return launch_chain(m, k_mattes_pass2_affine, (unsigned)grid, kPass2Threads, smem, a);
+  return launch_chain(m, k_mattes_pass2_affine, (unsigned)grid, kPass2Threads, smem, a2);
 }
 
 // B-spline / composite evaluation: node conversion (large grids), the per-sample
@@ -1379,7 +1398,6 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
   // Mattes: pass 1, finalize, pass 2
   const int B = (int)m->bins;
   const size_t sh1 = sizeof(unsigned long long) * (B * B + B) + sizeof(unsigned) * B;
-  const size_t sh2 = mattes_pass2_smem(B);  // record stages + log(p/pm) table
   if (sh1 > 200 * 1024) return fail(GB_ERR_UNSUPPORTED, "histogram too large for shared memory (bins > 160)");
   GB_CUDA(cd ? launch_wave(m, k_mattes_pass1_affine<kGradCentralDifference>, sh1, a)
              : launch_wave(m, k_mattes_pass1_affine<kGradImage>, sh1, a));
@@ -1388,7 +1406,7 @@ int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool d
     GB_CUDA(launch_chain(m, k_mattes_finalize, (unsigned)mattes_groups(B), kFinalizeThreads, 0, a));
     m->mark();
   } else {
-    GB_CUDA(launch_pass2(m, sh2, a));
+    GB_CUDA(launch_pass2(m, a));
     m->mark();
   }
   return GB_OK;
