@@ -1141,6 +1141,42 @@ __device__ __forceinline__ void mattes_value_groups(const EvalArgs& a, VGrid vg 
   }
 }
 
+// One sample of Mattes pass 1 (affine and displacement-field maps): position, moving
+// value and gradient, range reject, cache write, Parzen weights into the block
+// histogram `hist` (warp-aggregated), valid count.  Called by all 32 lanes of a warp.
+template <int GRAD, int TK>
+__device__ __forceinline__ void mattes_pass1_sample(const EvalArgs& a, const EvalConsts& K, const float4& s, int64_t i,
+                                                    bool live, unsigned long long* hist, unsigned* fm, unsigned& nv) {
+  const int B = a.bins;
+  float m = 0.f;
+  float3 g = make_float3(0.f, 0.f, 0.f);
+  bool ok = false;
+  if (live) {
+    unsigned voxel;
+    const DFPos p = sample_pos<TK>(a, K, s, i, voxel);
+    ok = eval_moving<GRAD>(a, p, a.with_derivative != 0, m, g);
+    if (TK != kMapAffine) g = field_grad(K, g);
+    // reject moving values outside [MovingImageTrueMin, MovingImageTrueMax], Mattes...Threader.hxx:238-245
+    ok = ok && !(m < a.mmin) && !(m > a.mmax);
+  }
+  // m / binsize - normalizedMin == (m - min) / binsize + 2 (padding), Mattes...v4.hxx:309-317
+  const float term = fmaf(m - a.mmin, a.m_inv_bs, 2.f);
+  if (a.with_derivative && live)
+    __stcs(a.cache + i, ok ? make_float4(term, g.x, g.y, g.z) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f));
+  int pdfm = 0;
+  unsigned q[4] = {0u, 0u, 0u, 0u};
+  const int fidx = __float_as_int(s.w);
+  if (ok) {
+    float t, w6[4];
+    parzen_window(term, B, pdfm, t);
+    parzen6(t, w6);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) q[k] = (__float2uint_rn(w6[k] * kQScale) + 3u) / 6u;  // unbiased 1/6
+  }
+  hist_add_aggregated(ok, fidx * B + pdfm, fidx, q, hist, fm);
+  nv += ok ? 1u : 0u;
+}
+
 template <int GRAD, int TK = kMapAffine>
 __device__ __forceinline__ void mattes_pass1_affine_body(const EvalArgs& a, VGrid vg) {
   extern __shared__ unsigned long long smem_u64[];
@@ -1172,33 +1208,7 @@ __device__ __forceinline__ void mattes_pass1_affine_body(const EvalArgs& a, VGri
     const float4 s = s_next;
     // prefetch the next record so its latency overlaps this iteration's gathers
     s_next = i + stride < a.n ? __ldcs(a.samples + i + stride) : make_float4(0.f, 0.f, 0.f, 0.f);
-    float m = 0.f;
-    float3 g = make_float3(0.f, 0.f, 0.f);
-    bool ok = false;
-    if (live) {
-      unsigned voxel;
-      const DFPos p = sample_pos<TK>(a, K, s, i, voxel);
-      ok = eval_moving<GRAD>(a, p, a.with_derivative != 0, m, g);
-      if (TK != kMapAffine) g = field_grad(K, g);
-      // reject moving values outside [MovingImageTrueMin, MovingImageTrueMax], Mattes...Threader.hxx:238-245
-      ok = ok && !(m < a.mmin) && !(m > a.mmax);
-    }
-    // m / binsize - normalizedMin == (m - min) / binsize + 2 (padding), Mattes...v4.hxx:309-317
-    const float term = fmaf(m - a.mmin, a.m_inv_bs, 2.f);
-    if (a.with_derivative && live)
-      __stcs(a.cache + i, ok ? make_float4(term, g.x, g.y, g.z) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f));
-    int pdfm = 0;
-    unsigned q[4] = {0u, 0u, 0u, 0u};
-    const int fidx = __float_as_int(s.w);
-    if (ok) {
-      float t, w6[4];
-      parzen_window(term, B, pdfm, t);
-      parzen6(t, w6);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) q[k] = (__float2uint_rn(w6[k] * kQScale) + 3u) / 6u;  // unbiased 1/6
-    }
-    hist_add_aggregated(ok, fidx * B + pdfm, fidx, q, hist, fm);
-    nv += ok ? 1u : 0u;
+    mattes_pass1_sample<GRAD, TK>(a, K, s, i, live, hist, fm, nv);
   }
   mattes_pass1_epilogue(a, nv, hist, cs, fm, vg, !kOwnTable);
 }

@@ -1090,10 +1090,9 @@ static cudaError_t launch_wave(gb_metric* m, K kernel, size_t smem, const EvalAr
 
 // Mattes pass 2 (affine): kPass2Threads threads per block (the streaming threads and
 // the value's group warp), one full wave, at most kFlatMaxBlocks blocks (the one-level
-// cross-block sums).
-// The derivative pass copies the final histogram into shared memory with one bulk
-// copy where that costs no resident block per SM; otherwise each block reads it
-// from global memory.
+// cross-block sums).  The histogram comes into shared memory with one bulk copy where
+// that costs no resident block per SM; otherwise each block reads it from global
+// memory.
 static cudaError_t launch_pass2(gb_metric* m, const EvalArgs& a) {
   const int B = (int)m->bins;
   const size_t plain = mattes_pass2_smem(B);
