@@ -58,6 +58,7 @@ __global__ void k_prepare_bspline(EvalArgs a) {
   griddep_wait();
   if (halted(a)) return;
   griddep_launch_dependents();
+  if (a.clear_acc) clear_accumulators(a);
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n < a.nper) a.nodes[n] = node_from_params(a.params, a.nper, n);
 }

@@ -160,7 +160,8 @@ inline void copy_parallel(void* dst, const void* src, size_t bytes) {
 // Enqueues one metric evaluation on the handle's stream (gb_metric.cu); results
 // land in d_out = [value, nvalid, derivative...] and the handle's status word.
 namespace gb {
-int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_params);
+int enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_params,
+                 bool acc_cleared = false);
 struct EvalArgs;
 void batch_eval_args(gb_metric* m, EvalArgs& a);
 }

@@ -192,6 +192,11 @@ struct EvalArgs {
   // fault injection (gb_metric_set_fault_injection): GB_FAULT_STALLED_COPY makes the
   // affine Mattes derivative pass issue none of its record copies
   int inject_stall;
+  // the per-evaluation accumulators (acc_n, tickets, histogram, marginals) as 16-byte
+  // words; with clear_acc the chain's first kernel zeroes them (no memset node)
+  uint4* acc;
+  int acc_words;
+  int clear_acc;
   // the affine Mattes derivative pass takes the final histogram and marginals (hist,
   // fmarg, colsum: contiguous, 16-byte aligned) into shared memory with one bulk copy
   int hist_bulk;
@@ -205,10 +210,18 @@ __device__ __forceinline__ bool halted(const EvalArgs& a) { return a.halt != nul
 // 13 threads, one output each, so the FP64 dependency chains run side by side.
 // One block (one warp, lane 0) per output: the entries take different code
 // paths, and one SM's FP64 pipe would serve them one after another.
+// Zeroes the accumulators, grid-strided over the launch (after the launch dependency,
+// so no kernel of the previous evaluation still reads them).
+__device__ __forceinline__ void clear_accumulators(const EvalArgs& a) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.acc_words; k += gridDim.x * blockDim.x)
+    a.acc[k] = make_uint4(0u, 0u, 0u, 0u);
+}
+
 __global__ void k_prepare_affine(EvalArgs a, EvalConsts* out) {
   griddep_wait();
   if (halted(a)) return;
   griddep_launch_dependents();
+  if (a.clear_acc) clear_accumulators(a);
   const int e = blockIdx.x;
   if (threadIdx.x == 0 && e < kConstEntries)
     affine_const_entry(e, a.params, a.center, a.m_p2i, a.m_origin, a.dense ? a.v_i2p : nullptr, a.v_origin, *out);

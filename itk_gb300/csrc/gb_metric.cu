@@ -559,7 +559,7 @@ static size_t acc_offset_fmarg(int64_t B) { return acc_offset_hist() + 8 * (size
 static size_t acc_offset_colsum(int64_t B) { return acc_offset_fmarg(B) + 8 * (size_t)B; }
 static size_t acc_layout_bytes(const gb_metric* m) {
   const int64_t B = (m->kind == GB_METRIC_MATTES || m->kind == GB_METRIC_JOINT_HISTOGRAM_MI) ? m->bins : 0;
-  return acc_offset_colsum(B) + 8 * (size_t)B + 16;
+  return (acc_offset_colsum(B) + 8 * (size_t)B + 16 + 15) / 16 * 16;
 }
 
 extern "C" int gb_metric_initialize(gb_metric* m) {
@@ -1017,6 +1017,8 @@ static void fill_eval_args(gb_metric* m, EvalArgs& a, const double* d_params, do
   unsigned char* base = m->d_acc.p;
   a.acc_n = reinterpret_cast<unsigned long long*>(base);
   a.tickets = reinterpret_cast<unsigned*>(base + acc_offset_tickets());
+  a.acc = reinterpret_cast<uint4*>(base);
+  a.acc_words = (int)(m->acc_bytes / 16);
   a.hist = reinterpret_cast<unsigned long long*>(base + acc_offset_hist());
   a.fmarg = reinterpret_cast<unsigned long long*>(base + acc_offset_fmarg(m->bins));
   a.colsum = reinterpret_cast<unsigned long long*>(base + acc_offset_colsum(m->bins));
@@ -1345,15 +1347,26 @@ static int enqueue_eval_jhmi(gb_metric* m, const EvalArgs& a, bool cd, bool deri
   return GB_OK;
 }
 
+// The evaluation chains whose first kernel can zero the accumulators and whose host
+// call can stage its inputs and results through prologue / epilogue kernels.
+static bool chain_clears_in_prepare(const gb_metric* m) {
+  return (m->kind == GB_METRIC_MATTES || m->kind == GB_METRIC_MEAN_SQUARES) && !is_field(m) && m->nsamples > 0;
+}
+
 // Enqueues one evaluation; results land in d_out = [value, nvalid, derivative...].
 // device_params: the parameters are in device memory (d_params), so the affine
 // constants or the B-spline nodes are formed on the device; otherwise the host
 // has uploaded them.
-int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_params) {
+int gb::enqueue_eval(gb_metric* m, const double* d_params, double* d_out, bool deriv, bool device_params,
+                     bool acc_cleared) {
   cudaStream_t st = m->stream;
   EvalArgs a;
   fill_eval_args(m, a, d_params, d_out, deriv);
-  GB_CUDA(cudaMemsetAsync(m->d_acc.p, 0, m->acc_bytes, st));
+  // MeanSquares / Mattes under an affine or B-spline transform with device parameters:
+  // the prepare kernel zeroes the accumulators (one node fewer, and the chain stays
+  // kernel-to-kernel); otherwise a memset unless the caller has cleared them
+  if (device_params && chain_clears_in_prepare(m)) a.clear_acc = 1;
+  else if (!acc_cleared || m->nsamples == 0) GB_CUDA(cudaMemsetAsync(m->d_acc.p, 0, m->acc_bytes, st));
   if (device_params && !is_bspline(m) && !is_field(m))
     GB_CUDA(launch_chain(m, k_prepare_affine, kConstEntries, 32, 0, a, m->d_consts.p));
   if (m->nsamples == 0) {
@@ -1444,12 +1457,53 @@ extern "C" int gb_metric_get_kernel_times(gb_metric* m, double* ms, int max_kern
   return GB_OK;
 }
 
+static_assert(sizeof(EvalConsts) % 16 == 0, "the host prologue copies the constants in 16-byte words");
+
+// The host call's prologue: zero the accumulators and bring the constants (affine) or
+// float4 nodes (B-spline) from pinned host memory into device memory.
+__global__ void k_host_prologue(EvalArgs a, const uint4* src, uint4* dst, int words) {
+  griddep_wait();
+  griddep_launch_dependents();
+  clear_accumulators(a);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < words; k += gridDim.x * blockDim.x) dst[k] = src[k];
+}
+
+// The host call's epilogue: value, count, derivative and status into pinned host memory.
+__global__ void k_host_epilogue(const double* out, int n, const int* status, double* h_out, int* h_status) {
+  griddep_wait();
+  griddep_launch_dependents();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) h_out[k] = __ldcg(out + k);
+  if (threadIdx.x == 0) *h_status = __ldcg(status);
+}
+
 // The host call's device work: the constants (affine) or float4 nodes (B-spline)
 // up from pinned memory, the evaluation, value / derivative / status down into
-// pinned memory.
+// pinned memory.  MeanSquares / Mattes under affine and B-spline transforms do it with
+// a prologue and an epilogue kernel (pinned memory read and written by the device), so
+// that every node of the chain is a kernel launched with a programmatic dependency;
+// the other chains with copies and a memset.
 static int host_chain(gb_metric* m, bool deriv) {
   cudaStream_t st = m->stream;
   const size_t P = m->tparams.size();
+  if (chain_clears_in_prepare(m)) {
+    const void* src = is_bspline(m) ? (const void*)m->h_params : (const void*)m->h_consts;
+    void* dst = is_bspline(m) ? (void*)m->d_nodes.p : (void*)m->d_consts.p;
+    const size_t bytes = is_bspline(m) ? sizeof(float4) * m->nper : sizeof(EvalConsts);
+    void *src_dev = nullptr, *out_dev = nullptr, *status_dev = nullptr;
+    GB_CUDA(cudaHostGetDevicePointer(&src_dev, const_cast<void*>(src), 0));
+    GB_CUDA(cudaHostGetDevicePointer(&out_dev, m->h_out, 0));
+    GB_CUDA(cudaHostGetDevicePointer(&status_dev, m->h_status, 0));
+    EvalArgs a;
+    fill_eval_args(m, a, nullptr, m->d_out.p, deriv);
+    const int words = (int)(bytes / 16);
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(32, (std::max(words, a.acc_words) + 255) / 256));
+    GB_CUDA(launch_chain(m, k_host_prologue, grid, 256, 0, a, (const uint4*)src_dev, (uint4*)dst, words));
+    int rc = enqueue_eval(m, nullptr, m->d_out.p, deriv, false, true);
+    if (rc) return rc;
+    GB_CUDA(launch_chain(m, k_host_epilogue, 1u, 256, 0, (const double*)m->d_out.p, (int)(2 + (deriv ? P : 0)),
+                         (const int*)m->d_status.p, (double*)out_dev, (int*)status_dev));
+    return GB_OK;
+  }
   if (is_bspline(m))
     GB_CUDA(cudaMemcpyAsync(m->d_nodes.p, m->h_params, sizeof(float4) * m->nper, cudaMemcpyHostToDevice, st));
   else if (is_field(m))
