@@ -32,8 +32,10 @@ constexpr int kTicketMain = 0;            // grid_sums of the MeanSquares kernel
 constexpr int kTicketFinalize = 160;      // last_block of the Mattes finalize
 constexpr int kTicketPass2 = 192;         // grid_sums of Mattes pass 2: [192, 320]
 constexpr int kTicketPass1 = 176;         // last_block of Mattes pass 1
+constexpr int kTicketValue = 340;         // the Mattes derivative pass's value groups done
 constexpr int kTicketCount = 352;
 constexpr int kPartPass2 = 4096;          // offset of pass-2 partials (finalize blocks use [0, 4096))
+constexpr int kPartValue = kPartPass2 - 1;  // the Mattes derivative pass's value (sum of the groups)
 constexpr size_t kGroupOffset = kPartPass2 + (size_t)kMaxBlocks * 16;  // per-group partials: 128 groups x 16
 constexpr size_t kMargOffset = kGroupOffset + 2048;     // [T, 1/T]
 constexpr size_t kScratchDoubles = kMargOffset + 8;
@@ -1144,6 +1146,25 @@ __device__ __forceinline__ double mattes_value_sum(const double* part, int ngrou
 }
 
 // Group partials computed by the last warp of blocks b, b + gridDim.x, ... (all blocks participate).
+// After a warp has written the partial of one group: the warp that completes the last
+// group sums all of them into part[kPartValue] (the same order as mattes_value_sum at
+// the end of the pass), so the derivative pass's last block only reads the value.
+// It writes before its block takes its cross-block ticket, so the last block sees it.
+__device__ __forceinline__ void mattes_value_group_done(const EvalArgs& a, int ng) {
+  const int lane = threadIdx.x & 31;
+  __threadfence();
+  unsigned t = 0u;
+  if (lane == 0) t = atomicAdd(&a.tickets[kTicketValue], 1u);
+  t = __shfl_sync(0xffffffffu, t, 0);
+  if (t != (unsigned)(ng - 1)) return;
+  __threadfence();
+  const double s = mattes_value_sum(a.part, ng, lane);
+  if (lane == 0) a.part[kPartValue] = s;
+}
+
+// SUM: the derivative pass's form, with the value summed by the warp completing the
+// last group (mattes_value_group_done).
+template <bool SUM = false>
 __device__ __forceinline__ void mattes_value_groups(const EvalArgs& a, VGrid vg = hw_grid()) {
   if ((int)(threadIdx.x >> 5) != (int)(blockDim.x >> 5) - 1) return;
   const int lane = threadIdx.x & 31;
@@ -1151,6 +1172,7 @@ __device__ __forceinline__ void mattes_value_groups(const EvalArgs& a, VGrid vg 
   for (int g = vg.b; g < ng; g += vg.n) {
     const double s = mattes_group_partial(a, g, lane);
     if (lane == 0) a.part[g] = s;
+    if (SUM) mattes_value_group_done(a, ng);
   }
 }
 
@@ -1418,6 +1440,9 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
   const float cword = cw < kConstWords ? __ldcg(reinterpret_cast<const float*>(a.consts) + cw) : 0.f;
   const double T = streamer ? __ldcg(&a.marg[0]) : 0.0;
   const unsigned long long N = streamer ? __ldcg(a.acc_n) : 0ull;
+  // nFactor = -1 / (MovingImageBinSize * N), Mattes...Threader.hxx:446-457: formed now,
+  // off the last block's tail (FP64 division)
+  __shared__ double nfac_s;
   // the histogram (first), then the first tiles
   if (threadIdx.x == 0 && !stall) {
     if (hb) {
@@ -1434,10 +1459,12 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k] = 0.f;
   if (!GROUP_WARP) {
+    if (threadIdx.x == 0) nfac_s = -1.0 / (a.m_bs * (double)N);
     mattes_pratio_build<false>(a, T, pr, colf, fmask);
-    mattes_value_groups(a, vg);  // the value's FP64 group partials, last warp
+    mattes_value_groups<true>(a, vg);  // the value's FP64 group partials and sum, last warp
     __syncthreads();
   } else if (streamer) {
+    if (threadIdx.x == 0) nfac_s = -1.0 / (a.m_bs * (double)N);
     if (hb) {
       if (!mbar_wait(&hbar, 0u, limit)) failed = 1;
       stream_barrier();
@@ -1451,6 +1478,7 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
     for (int g = vg.b; g < ng; g += vg.n) {
       const double sg = mattes_group_partial(a, g, threadIdx.x & 31);
       if ((threadIdx.x & 31) == 0) a.part[g] = sg;
+      mattes_value_group_done(a, ng);
     }
   }
   int t = 0;
@@ -1513,29 +1541,17 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
   }
   block_sums_df<12>(kacc, red, blk);
   DFloat* part = reinterpret_cast<DFloat*>(a.part + kPartPass2);
-  const int ng = mattes_groups(B);
-  // staged form: the last block requests every block partial and value group partial at
-  // once into the (now idle) record stages, then sums them from shared memory, the value
-  // (FP64) in the last warp while the other warps form the derivative
-  const bool staged = vg.n <= kFlatMaxBlocks && (size_t)(vg.n * 12 + ng) * 8 <= kStreamBytes;
-  __shared__ double vsum_s;
+  // staged form: the last block requests every block partial at once into the (now idle)
+  // record stages, then sums them from shared memory
+  const bool staged = vg.n <= kFlatMaxBlocks && (size_t)(vg.n * 12) * 8 <= kStreamBytes;
   if (staged) {
     if (!grid_ticket_flat_df<12>(blk, part, a.tickets + kTicketPass2, vg)) return;
     DFloat* sp = reinterpret_cast<DFloat*>(smem_raw);
-    double* sv = reinterpret_cast<double*>(sp + vg.n * 12);
     stage_u64(reinterpret_cast<const unsigned long long*>(part), vg.n * 12,
               reinterpret_cast<unsigned long long*>(sp));
-    stage_u64(reinterpret_cast<const unsigned long long*>(a.part), ng, reinterpret_cast<unsigned long long*>(sv));
     __syncthreads();
     __shared__ DFloat fin_s[12];
-    if ((int)threadIdx.x < (kWarps - 1) * 32) {
-      strided_sums_df_shared<12>(sp, vg.n, fin_s, kWarps - 1);
-    } else {
-      double v = 0.0;
-      for (int r = threadIdx.x & 31; r < ng; r += 32) v += sv[r];
-      v = warp_sum_d(v);
-      if ((threadIdx.x & 31) == 0) vsum_s = v;
-    }
+    strided_sums_df_shared<12>(sp, vg.n, fin_s, kWarps);
     __syncthreads();
     for (int k = threadIdx.x; k < 12; k += blockDim.x) fin[k] = df_to_double(fin_s[k]);
     __syncthreads();
@@ -1546,14 +1562,13 @@ __device__ __forceinline__ void mattes_pass2_affine_body(const EvalArgs& a, VGri
                                              fin, vg);
     if (!last) return;
   }
-  // last block: the value from the group partials (all blocks wrote theirs before their
-  // tickets); warp 0, one derivative entry per lane
+  // last block: the value summed by the warp that completed the last group (written before
+  // its block's ticket); warp 0, one derivative entry per lane
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     const int st = N == 0 ? GB_ERR_NO_VALID_POINTS : T * kQInv >= DBL_EPSILON ? GB_OK : GB_ERR_JOINT_PDF_SUM_ZERO;
-    const double s = staged ? vsum_s : mattes_value_sum(a.part, ng, lane);
-    // nFactor = -1 / (MovingImageBinSize * N), Mattes...Threader.hxx:446-457
-    const double nFactor = -1.0 / (a.m_bs * (double)N);
+    const double s = __ldcg(&a.part[kPartValue]);
+    const double nFactor = nfac_s;
     if (lane == 0) {
       *a.status = st;
       a.out[1] = (double)N;
