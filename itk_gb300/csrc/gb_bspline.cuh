@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
   const int B = a.bins;
   const int t = threadIdx.x;
   if (MATTES) {
-    mattes_value_groups(a);  // the value's group partials (blocks b, b + G, ...)
+    mattes_value_groups<true>(a);  // the value's group partials (blocks b, b + G, ...) and their sum
     for (int k = t; k < B * B; k += blockDim.x) pr_sh[k] = __ldcg(a.pratio + k);
   }
   // this thread's inputs of one chunk: the run, the sample's support, cache and fixed bin
@@ -382,18 +382,23 @@ __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
   griddep_wait();
   if (halted(a)) return;
   griddep_launch_dependents();
-  const unsigned long long N = __ldcg(a.acc_n);
-  // MeanSquares: the status of the value pass; Mattes: from the pass-1 totals, and
-  // block 0 forms the value from the chunk kernel's group partials
-  const int st = MATTES ? mattes_status(a) : __ldcg(a.status);
-  if (blockIdx.x == 0 && threadIdx.x < 32) {
-    const double v = MATTES ? mattes_value_sum(a.part, mattes_groups(a.bins), threadIdx.x) : 0.0;
-    if (threadIdx.x == 0) {
-      a.out[1] = (double)N;
-      if (MATTES) {
-        *a.status = st;
-        a.out[0] = st == GB_OK ? -1.0 * v : 0.0;
-      }
+  // MeanSquares: the status of the value pass, scale 1 / N; Mattes: the scale formed by
+  // the table kernel (0 unless the status is OK), and block 0 writes the value summed by
+  // the chunk kernel's last group warp, the count and the status
+  double scale;
+  if (MATTES) {
+    scale = __ldcg(&a.marg[2]);
+  } else {
+    const unsigned long long N = __ldcg(a.acc_n);
+    scale = (__ldcg(a.status) == GB_OK && N > 0) ? 1.0 / (double)N : 0.0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned long long N = __ldcg(a.acc_n);
+    a.out[1] = (double)N;
+    if (MATTES) {
+      const int st = mattes_status(a);
+      *a.status = st;
+      a.out[0] = st == GB_OK ? -1.0 * __ldcg(&a.part[kPartValue]) : 0.0;
     }
   }
   if (n >= a.nper) return;
@@ -436,8 +441,6 @@ __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
     t2 = b2.value();
   }
   if (lane == 0) {
-    double scale = 0.0;
-    if (st == GB_OK && N > 0) scale = MATTES ? -1.0 / (a.m_bs * (double)N) : 1.0 / (double)N;
     a.out[2 + n] = (double)t0 * scale;
     a.out[2 + a.nper + n] = (double)t1 * scale;
     a.out[2 + 2 * a.nper + n] = (double)t2 * scale;

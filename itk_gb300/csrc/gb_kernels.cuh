@@ -37,7 +37,7 @@ constexpr int kTicketCount = 352;
 constexpr int kPartPass2 = 4096;          // offset of pass-2 partials (finalize blocks use [0, 4096))
 constexpr int kPartValue = kPartPass2 - 1;  // the Mattes derivative pass's value (sum of the groups)
 constexpr size_t kGroupOffset = kPartPass2 + (size_t)kMaxBlocks * 16;  // per-group partials: 128 groups x 16
-constexpr size_t kMargOffset = kGroupOffset + 2048;     // [T, 1/T]
+constexpr size_t kMargOffset = kGroupOffset + 2048;     // [T, 1/T, derivative scale]
 constexpr size_t kScratchDoubles = kMargOffset + 8;
 constexpr int kFinalizeThreads = 32;
 constexpr float kQScale = 67108864.f;  // 2^26 fixed point of histogram weights
@@ -1264,7 +1264,14 @@ __global__ void __launch_bounds__(kBlock) k_mattes_table(EvalArgs a) {
   griddep_launch_dependents();
   const int B = a.bins;
   __shared__ PratioThresholds th_s;
-  if (threadIdx.x == 0) th_s = pratio_thresholds(__ldcg(&a.marg[0]), __ldcg(a.acc_n));  // FP64: once per block
+  if (threadIdx.x == 0) {
+    const double T = __ldcg(&a.marg[0]);
+    const unsigned long long N = __ldcg(a.acc_n);
+    th_s = pratio_thresholds(T, N);  // FP64: once per block
+    // the derivative scale for the parameter gather: nFactor = -1 / (MovingImageBinSize
+    // * N), Mattes...Threader.hxx:446-457, 0 when the status is not OK (formed once here)
+    if (blockIdx.x == 0) a.marg[2] = th_s.bad ? 0.0 : -1.0 / (a.m_bs * (double)N);
+  }
   __syncthreads();
   const bool bad = th_s.bad != 0;
   const unsigned long long hthr = th_s.hthr, fthr = th_s.fthr;
