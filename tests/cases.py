@@ -77,3 +77,16 @@ def perturbed(T: AffineTransform, seed, scale=0.02, trans=1.0):
     U.SetMatrix(M)
     U.SetTranslation(rng.uniform(-trans, trans, size=3))
     return U
+
+
+def shared_voxel_points(image: Image, fraction, seed, per_voxel=3, jitter=0.4):
+    """A point set with `per_voxel` points in each of a random set of voxels (each moved by
+    up to `jitter` voxel along each index axis, so the nearest voxel stays the same): the
+    local-support derivative then sums several points' blocks into one voxel."""
+    nx, ny, nz = image.GetSize()
+    total = nx * ny * nz
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(total, size=max(1, int(total * fraction)), replace=False))
+    ijk = np.stack([idx % nx, (idx // nx) % ny, idx // (nx * ny)], axis=1).astype(np.float64)
+    ijk = np.repeat(ijk, per_voxel, axis=0) + rng.uniform(-jitter, jitter, size=(len(idx) * per_voxel, 3))
+    return (ijk @ image.index_to_physical().T + image.origin).astype(np.float32)

@@ -83,6 +83,24 @@ def test_matches_oracle(pair, kind, sampled, gradient_image):
     assert m.GetValue() == v
 
 
+def test_meansquares_several_points_per_voxel(pair):
+    """Three points in each sampled voxel: MeanSquares sums their blocks into the voxel as
+    the reference's local-support branch does, against the oracle (the FP64 atomics make
+    the last bits order-dependent).  Mattes is left out: the reference keeps one joint-PDF
+    index per voxel there, whichever point's thread wrote last."""
+    from cases import shared_voxel_points
+    fixed, moving = pair
+    T = field_transform(fixed, data.smooth_displacement_field(fixed, seed=7, max_disp=2.5).array)
+    grad = data.gradient_image(moving)
+    pts = shared_voxel_points(fixed, 0.1, seed=4)
+    m = make("msq", fixed, moving, T, grad, pts)
+    v, d = m.GetValueAndDerivative()
+    rc, rv, rd, nv = oracle("msq", fixed, moving, T, grad, pts)
+    assert rc == 0 and m.GetNumberOfValidPoints() == nv
+    assert_value_close(v, rv)
+    assert_deriv_close(d, rd)
+
+
 def test_identity_field_meansquares_truth(pair):
     fixed, moving = pair
     grad = data.gradient_image(moving)

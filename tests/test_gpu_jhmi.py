@@ -194,6 +194,24 @@ def test_bspline_matches_oracle(pair, composite, sampled, gradient):
     assert m.GetValue() == v
 
 
+def test_displacement_field_several_points_per_voxel(pair):
+    """Three points in each sampled voxel: the local-support derivative sums their blocks
+    into the voxel (Derivatives[offset + i] +=), against the oracle; the FP64 atomics make
+    the last bits depend on the order, so the comparison is within the usual tolerance."""
+    from cases import shared_voxel_points
+    from itk_gb300 import DisplacementFieldImage, DisplacementFieldTransform
+    fixed, moving, _ = pair
+    F = DisplacementFieldTransform()
+    F.SetDisplacementField(DisplacementFieldImage.like(fixed, data.smooth_displacement_field(fixed, 21, 2.0).array))
+    pts = shared_voxel_points(fixed, 0.1, seed=8)
+    m = make(fixed, moving, F, "image", pts)
+    v, d = m.GetValueAndDerivative()
+    rc, rv, rd, nv, pdf = oracle(fixed, moving, F, "image", pts)
+    assert rc == 0 and m.GetNumberOfValidPoints() == nv
+    assert_value_close(v, rv)
+    assert_deriv_close(d, rd)
+
+
 @pytest.mark.parametrize("sampled", [False, True])
 @pytest.mark.parametrize("gradient", ["image", "cd"])
 def test_displacement_field_matches_oracle(pair, sampled, gradient):
