@@ -257,9 +257,9 @@ __global__ void __launch_bounds__(kBlock, SMEM ? 4 : 3) k_mattes_pass1_bspline(E
 // a_s = 2 (f - m) M^T g (MeanSquares) or w(term) M^T g (Mattes,
 // w = sum_k log(p/pm)[f][m_k] beta3'(m_k - term)).  Sum phase: thread t owns
 // the 4 x-adjacent support nodes of row (ky, kz) = (t & 3, (t >> 2) & 3) over
-// the sample slice t >> 4 (16 slices of 16 samples): per sample one 16-byte
-// load of the x weights, 12 FMAs.  The 16 slice sums of each output are then
-// added in slice order.
+// the sample slice t >> 4 (16 slices, slice s holding samples s, s + 16, ...): per
+// sample one 16-byte load of the x weights, 12 FMAs.  The 16 slice sums of each
+// output are then added in slice order.
 constexpr int kChunkSlices = 16;
 // Grid-stride over the chunks (one full wave of blocks): block b forms chunks b, b + G, ...
 // The next chunk's per-sample inputs are loaded into registers while the current
@@ -328,13 +328,13 @@ __global__ void __launch_bounds__(kChunkLen) k_bspline_chunks(EvalArgs a) {
       AV[t] = av;
     }
     __syncthreads();
+    // slice sl sums samples sl, sl + 16, ...: the two half-warps read adjacent rows of
+    // W1 and AV, in different shared-memory banks
     const int ky = t & 3, kz = (t >> 2) & 3, sl = t >> 4;
-    constexpr int kSlice = kChunkLen / kChunkSlices;
-    const int j0 = sl * kSlice, j1 = min(len, j0 + kSlice);
     float acc[4][3];
 #pragma unroll
     for (int kx = 0; kx < 4; ++kx) acc[kx][0] = acc[kx][1] = acc[kx][2] = 0.f;
-    for (int j = j0; j < j1; ++j) {
+    for (int j = sl; j < len; j += kChunkSlices) {
       const float4 wx = *reinterpret_cast<const float4*>(&W1[j][0]);
       const float wyz = W1[j][4 + ky] * W1[j][8 + kz];
       const float4 v = AV[j];
