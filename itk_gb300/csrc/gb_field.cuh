@@ -61,8 +61,13 @@ __global__ void __launch_bounds__(kBlock) k_msq_field(EvalArgs a) {
   unsigned nv = 0;
   const bool deriv = a.with_derivative != 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-    const float4 s = __ldcs(a.samples + i);
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float4 s_next = i < a.n ? __ldcs(a.samples + i) : zero;
+  for (; i < a.n; i += stride) {
+    // the next record travels while this sample is formed
+    const float4 s = s_next;
+    s_next = i + stride < a.n ? __ldcs(a.samples + i + stride) : zero;
     unsigned voxel = ~0u;
     const DFPos p = sample_pos<TK>(a, K, s, i, voxel);
     float m = 0.f;

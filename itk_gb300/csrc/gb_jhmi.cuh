@@ -82,8 +82,13 @@ __device__ __forceinline__ void jhmi_pass1_body(const EvalArgs& a, const JhmiCon
   __syncthreads();
   unsigned nv = 0;
   const int64_t stride = (int64_t)vg.n * blockDim.x;
-  for (int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-    const float4 s = __ldcs(a.samples + i);
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x;
+  float4 s_next = i < a.n ? __ldcs(a.samples + i) : zero;
+  for (; i < a.n; i += stride) {
+    // the next record travels while this sample is formed
+    const float4 s = s_next;
+    s_next = i + stride < a.n ? __ldcs(a.samples + i + stride) : zero;
     float m = 0.f;
     float3 g = make_float3(0.f, 0.f, 0.f);
     unsigned voxel;
@@ -257,14 +262,15 @@ __device__ __forceinline__ bool jhmi_scaling(const JhmiConsts& C, const float* p
   const float delta = r - l;
   if (delta > 0.f) {
     const float cl = (l - C.origin_f) * C.inv_spacing_f, cr = (r - C.origin_f) * C.inv_spacing_f;
-    dj = (jhmi_interp2(pdf, B, ca, cr) - jhmi_interp2(pdf, B, ca, cl)) / delta;
-    dm = (jhmi_interp1(mm, B, cr) - jhmi_interp1(mm, B, cl)) / delta;
+    // fast FP32 divisions (within 2 ulp; the divisors are spacing-sized or above 1e-16)
+    dj = __fdividef(jhmi_interp2(pdf, B, ca, cr) - jhmi_interp2(pdf, B, ca, cl), delta);
+    dm = __fdividef(jhmi_interp1(mm, B, cr) - jhmi_interp1(mm, B, cl), delta);
   }
   const float mv = jhmi_interp1(mm, B, cb);
   sf = 0.f;
   if (jv > 1e-16f && mv > 1e-16f) {
-    const float t1 = fminf(fmaxf(dj / jv, -max_slope), max_slope);
-    const float t2 = fminf(fmaxf(dm / mv, -max_slope), max_slope);
+    const float t1 = fminf(fmaxf(__fdividef(dj, jv), -max_slope), max_slope);
+    const float t2 = fminf(fmaxf(__fdividef(dm, mv), -max_slope), max_slope);
     sf = (t1 - t2) * inv_scale;
   }
   return true;
@@ -300,9 +306,16 @@ __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiCon
   for (int k = 0; k < 12; ++k) acc[k] = 0.f;
   unsigned nv = 0;
   const int64_t stride = (int64_t)vg.n * blockDim.x;
-  for (int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-    const float4 cc = __ldcs(a.cache + i);
-    const float4 s = __ldcs(a.samples + i);
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  int64_t i = (int64_t)vg.b * blockDim.x + threadIdx.x;
+  float4 cc_next = i < a.n ? __ldcs(a.cache + i) : zero;
+  float4 s_next = i < a.n ? __ldcs(a.samples + i) : zero;
+  for (; i < a.n; i += stride) {
+    // the next cache entry and record travel while this sample is formed
+    const float4 cc = cc_next;
+    const float4 s = s_next;
+    cc_next = i + stride < a.n ? __ldcs(a.cache + i + stride) : zero;
+    s_next = i + stride < a.n ? __ldcs(a.samples + i + stride) : zero;
     float sf;
     if (!jhmi_scaling(C, pdf, mm, B, s.w, cc.x, mlo, mhi, max_slope, inv_scale, sf)) continue;
     ++nv;
