@@ -276,6 +276,26 @@ __device__ __forceinline__ bool jhmi_scaling(const JhmiConsts& C, const float* p
   return true;
 }
 
+// The derivative passes' scalars: the slope clamp -log(1e-16) / spacing, the scale
+// 1 / (log 2 (max - min)) and the moving range (exact: the true min / max are float
+// values).  FP64, formed by one thread and shared (a block's worth of FP64 divisions
+// would cost microseconds at GB300's FP64 rate); the caller has synchronized on C.
+__device__ __forceinline__ void jhmi_pass2_scalars(const JhmiConsts& C, float& max_slope, float& inv_scale,
+                                                   float& mlo, float& mhi) {
+  __shared__ float sc_s[4];
+  if (threadIdx.x == 0) {
+    sc_s[0] = (float)(36.841361487904734 / C.spacing);
+    sc_s[1] = (float)(1.0 / (0.69314718055994530942 * (C.mmax - C.mmin)));
+    sc_s[2] = (float)C.mmin;
+    sc_s[3] = (float)C.mmax;
+  }
+  __syncthreads();
+  max_slope = sc_s[0];
+  inv_scale = sc_s[1];
+  mlo = sc_s[2];
+  mhi = sc_s[3];
+}
+
 // k_jhmi_pass2: the derivative.  Dynamic shared memory: the B^2 + B FP32 tables.
 template <int GRAD>
 __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiConsts* __restrict__ gC, VGrid vg) {
@@ -298,9 +318,8 @@ __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiCon
   __syncthreads();
   const float* pdf = tab;
   const float* mm = tab + B * B;
-  const float max_slope = (float)(36.841361487904734 / C.spacing);  // -log(1e-16) / spacing
-  const float inv_scale = (float)(1.0 / (0.69314718055994530942 * (C.mmax - C.mmin)));
-  const float mlo = (float)C.mmin, mhi = (float)C.mmax;  // exact: the true min / max are float values
+  float max_slope, inv_scale, mlo, mhi;
+  jhmi_pass2_scalars(C, max_slope, inv_scale, mlo, mhi);
   float acc[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k] = 0.f;
@@ -431,9 +450,8 @@ __global__ void __launch_bounds__(kBlock) k_jhmi_pass2_bspline(EvalArgs a, const
   for (int k = threadIdx.x; k < B * B + B; k += blockDim.x) tab[k] = __ldcg(&a.pratio[k]);
   load_jhmi(gC, C);
   __syncthreads();
-  const float max_slope = (float)(36.841361487904734 / C.spacing);  // -log(1e-16) / spacing
-  const float inv_scale = (float)(1.0 / (0.69314718055994530942 * (C.mmax - C.mmin)));
-  const float mlo = (float)C.mmin, mhi = (float)C.mmax;
+  float max_slope, inv_scale, mlo, mhi;
+  jhmi_pass2_scalars(C, max_slope, inv_scale, mlo, mhi);
   unsigned nv = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
@@ -484,9 +502,8 @@ __global__ void __launch_bounds__(kBlock) k_jhmi_pass2_field(EvalArgs a, const J
   for (int k = threadIdx.x; k < B * B + B; k += blockDim.x) tab[k] = __ldcg(&a.pratio[k]);
   load_jhmi(gC, C);
   __syncthreads();
-  const float max_slope = (float)(36.841361487904734 / C.spacing);  // -log(1e-16) / spacing
-  const float inv_scale = (float)(1.0 / (0.69314718055994530942 * (C.mmax - C.mmin)));
-  const float mlo = (float)C.mmin, mhi = (float)C.mmax;
+  float max_slope, inv_scale, mlo, mhi;
+  jhmi_pass2_scalars(C, max_slope, inv_scale, mlo, mhi);
   unsigned nv = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
