@@ -646,20 +646,17 @@ __device__ __forceinline__ void msq_affine_body(const EvalArgs& a, VGrid vg) {
     __syncthreads();
   }
   if (!grid_sums<13>(blk, a.part, a.grp, a.tickets + kTicketMain, fin, vg)) return;
-  if (threadIdx.x == 0) {
-    // AfterThreadedExecution + VerifyNumberOfValidPoints (ThreaderBase.hxx:116-172)
+  if (threadIdx.x < 32) {
+    // AfterThreadedExecution + VerifyNumberOfValidPoints (ThreaderBase.hxx:116-172); lane
+    // k divides entry k (the FP64 divisions side by side, not one after another)
+    const int lane = threadIdx.x;
     const unsigned long long N = __ldcg(a.acc_n);
     const int P = a.with_derivative ? a.nparams : 0;
-    if (N == 0) {
-      a.out[0] = DBL_MAX;
-      a.out[1] = 0.0;
-      for (int p = 0; p < P; ++p) a.out[2 + p] = 0.0;
-      *a.status = GB_ERR_NO_VALID_POINTS;
-    } else {
-      a.out[0] = fin[0] / (double)N;
+    for (int k = lane; k < 1 + P; k += 32) a.out[k == 0 ? 0 : 1 + k] = N == 0 ? (k == 0 ? DBL_MAX : 0.0)
+                                                                               : fin[k] / (double)N;
+    if (lane == 0) {
       a.out[1] = (double)N;
-      for (int p = 0; p < P; ++p) a.out[2 + p] = fin[1 + p] / (double)N;
-      *a.status = GB_OK;
+      *a.status = N == 0 ? GB_ERR_NO_VALID_POINTS : GB_OK;
     }
   }
 }
