@@ -389,8 +389,13 @@ __global__ void __launch_bounds__(kParamsBlock) k_bspline_params(EvalArgs a) {
   if (MATTES) {
     scale = __ldcg(&a.marg[2]);
   } else {
-    const unsigned long long N = __ldcg(a.acc_n);
-    scale = (__ldcg(a.status) == GB_OK && N > 0) ? 1.0 / (double)N : 0.0;
+    __shared__ double scale_s;  // FP64 division: once per block
+    if (threadIdx.x == 0) {
+      const unsigned long long N = __ldcg(a.acc_n);
+      scale_s = (__ldcg(a.status) == GB_OK && N > 0) ? 1.0 / (double)N : 0.0;
+    }
+    __syncthreads();
+    scale = scale_s;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const unsigned long long N = __ldcg(a.acc_n);
