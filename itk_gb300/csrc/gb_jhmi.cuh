@@ -356,18 +356,18 @@ __device__ __forceinline__ void jhmi_pass2_body(const EvalArgs& a, const JhmiCon
   kacc[12].c = 0.f;
   block_sums<13>(kacc, red, blk);
   if (!grid_sums<13>(blk, a.part + kPartPass2, a.grp, a.tickets + kTicketPass2, fin, vg)) return;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    // one derivative entry per lane (the FP64 divisions side by side)
+    const int lane = threadIdx.x;
     const double N = fin[12];
     const int P = a.nparams;
-    a.out[1] = N;
-    if (N == 0.0) {  // VerifyNumberOfValidPoints: a warning, value max, zero derivative
-      a.out[0] = DBL_MAX;
-      for (int p = 0; p < P; ++p) a.out[2 + p] = 0.0;
-      *a.status = GB_ERR_NO_VALID_POINTS;
-      return;
+    // VerifyNumberOfValidPoints: with no valid point a warning, value max, zero derivative
+    for (int p = lane; p < P; p += 32) a.out[2 + p] = N == 0.0 ? 0.0 : fin[p] / N;
+    if (lane == 0) {
+      a.out[1] = N;
+      if (N == 0.0) a.out[0] = DBL_MAX;
+      *a.status = N == 0.0 ? GB_ERR_NO_VALID_POINTS : GB_OK;
     }
-    *a.status = GB_OK;
-    for (int p = 0; p < P; ++p) a.out[2 + p] = fin[p] / N;
   }
 }
 

@@ -767,26 +767,23 @@ __device__ __forceinline__ void corr_body(const EvalArgs& a, VGrid vg) {
   }
   block_sums<27>(kacc, red, blk);
   if (!grid_sums<27>(blk, a.part, a.grp, a.tickets + kTicketPass2, fin, vg)) return;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    // one derivative entry per lane (every lane forms the same FP64 factors)
+    const int lane = threadIdx.x;
     const unsigned long long N = __ldcg(a.acc_n);
     const int P = a.with_derivative ? a.nparams : 0;
-    a.out[1] = (double)N;
-    for (int p = 0; p < P; ++p) a.out[2 + p] = 0.0;
-    if (N == 0) {  // VerifyNumberOfValidPoints: a warning, value max
-      a.out[0] = DBL_MAX;
-      *a.status = GB_ERR_NO_VALID_POINTS;
-      return;
-    }
-    *a.status = GB_OK;
     const double fm = fin[0], f2 = fin[1], m2 = fin[2];
     const double m2f2 = m2 * f2;
-    if (m2f2 <= DBL_EPSILON) {
-      a.out[0] = 0.0;
-      return;
+    // VerifyNumberOfValidPoints (no valid point: a warning, value max, derivative 0); a
+    // zero denominator gives value 0 and derivative 0
+    const bool live = N != 0 && !(m2f2 <= DBL_EPSILON);
+    const double sc = live ? 2.0 * fm / (f2 * m2) : 0.0, r = live ? fm / m2 : 0.0;
+    for (int p = lane; p < P; p += 32) a.out[2 + p] = live ? sc * (fin[3 + p] - r * fin[15 + p]) : 0.0;
+    if (lane == 0) {
+      a.out[1] = (double)N;
+      *a.status = N == 0 ? GB_ERR_NO_VALID_POINTS : GB_OK;
+      a.out[0] = N == 0 ? DBL_MAX : (live ? -1.0 * fm * fm / m2f2 : 0.0);
     }
-    a.out[0] = -1.0 * fm * fm / m2f2;
-    const double sc = 2.0 * fm / (f2 * m2), r = fm / m2;
-    for (int p = 0; p < P; ++p) a.out[2 + p] = sc * (fin[3 + p] - r * fin[15 + p]);
   }
 }
 
